@@ -1,0 +1,278 @@
+"""DEReK GB300: the plane-wave Kohn-Sham hot path of DEReK on one GB300 GPU.
+
+The compute path is ``libderek_gpu.so`` (hand-written sm_103a CUDA behind the
+C ABI in ``include/derek_gpu.h``).  This package is a thin ctypes mirror of
+that ABI, named after the reference's Fortran module routines it replaces
+(fft_3d, pot_apply_wfn, density_calculate, wave_dot, electronic_scf).  There
+is no CPU fallback: loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import (DEREK_PREC_FP64, DEREK_PREC_MIXED, DEREK_GRID_REFERENCE,  # noqa: F401
+                   DEREK_GRID_SMOOTH23, DerekError, lib, lib_path)
+
+__all__ = ["Handle", "SystemSpec", "DerekError", "lib", "lib_path", "host_grid_sizes",
+           "host_gsphere", "host_prime_fact", "DEREK_PREC_FP64", "DEREK_PREC_MIXED",
+           "DEREK_GRID_REFERENCE", "DEREK_GRID_SMOOTH23"]
+
+
+class SystemSpec:
+    """One independent system (the fields of current_structure/current_params
+    the hot path reads, Source/io.f90:63-114,171-194), in Ha/bohr."""
+
+    def __init__(self, cell, ecut, kpts, nbands, nelec, kT=0.01, wk=None, vext=None,
+                 wells=None, n_fine=None, grid_policy=DEREK_GRID_SMOOTH23, g_fine_scale=2.0,
+                 inv_cell=None):
+        self.cell = np.asarray(cell, dtype=np.float64).reshape(3, 3)
+        self.inv_cell = None if inv_cell is None else np.asarray(inv_cell, dtype=np.float64).reshape(3, 3)
+        self.ecut = float(ecut)
+        self.kpts = np.ascontiguousarray(np.asarray(kpts, dtype=np.float64).reshape(-1, 3))
+        self.wk = None if wk is None else np.ascontiguousarray(np.asarray(wk, dtype=np.float64))
+        self.nbands = int(nbands)
+        self.nelec = float(nelec)
+        self.kT = float(kT)
+        self.vext = None if vext is None else np.ascontiguousarray(np.asarray(vext, dtype=np.float64))
+        self.wells = (np.zeros((0, 5)) if wells is None
+                      else np.ascontiguousarray(np.asarray(wells, dtype=np.float64).reshape(-1, 5)))
+        self.n_fine = (0, 0, 0) if n_fine is None else tuple(int(x) for x in n_fine)
+        self.grid_policy = int(grid_policy)
+        self.g_fine_scale = float(g_fine_scale)
+
+    def to_desc(self, keep):
+        d = _abi.SysDesc()
+        # column-major storage of cell(3,3): cell[3*j+i] = cell(i+1, j+1)
+        for i in range(3):
+            for j in range(3):
+                d.cell[3 * j + i] = self.cell[i, j]
+                if self.inv_cell is not None:
+                    d.inv_cell[3 * j + i] = self.inv_cell[i, j]
+        d.ecut = self.ecut
+        d.g_fine_scale = self.g_fine_scale
+        for i in range(3):
+            d.n_fine[i] = self.n_fine[i]
+        d.grid_policy = self.grid_policy
+        d.nk = len(self.kpts)
+        keep.append(self.kpts)
+        d.kpts = self.kpts.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        if self.wk is not None:
+            keep.append(self.wk)
+            d.wk = self.wk.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.nbands = self.nbands
+        d.nspinor = 1
+        d.nelec = self.nelec
+        d.kT = self.kT
+        if self.vext is not None:
+            keep.append(self.vext)
+            d.vext = self.vext.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.nwells = len(self.wells)
+        keep.append(self.wells)
+        d.wells = self.wells.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        return d
+
+
+def _check(status, h=None, what=""):
+    if status != 0:
+        detail = lib.derek_gpu_last_error(h).decode() if lib is not None else ""
+        raise DerekError(status, f"{what}: {lib.derek_gpu_strerror(status).decode()} {detail}".strip())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Handle:
+    """Owns one derek_gpu_t over a batch of systems."""
+
+    def __init__(self, systems, precision=DEREK_PREC_FP64, **opts):
+        if isinstance(systems, SystemSpec):
+            systems = [systems]
+        self.systems = list(systems)
+        o = _abi.ScfOpts()
+        lib.derek_gpu_default_opts(ctypes.byref(o))
+        o.precision = int(precision)
+        for k, v in opts.items():
+            if not hasattr(o, k):
+                raise TypeError(f"unknown option {k}")
+            setattr(o, k, v)
+        self.opts = o
+        keep = []
+        arr = (_abi.SysDesc * len(self.systems))(*[s.to_desc(keep) for s in self.systems])
+        h = ctypes.c_void_p()
+        st = lib.derek_gpu_create(ctypes.byref(h), arr, len(self.systems), ctypes.byref(o))
+        if st != 0:
+            raise DerekError(st, f"derek_gpu_create: {lib.derek_gpu_strerror(st).decode()} "
+                                 f"{lib.derek_gpu_last_error(None).decode()}")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.derek_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- sizes and tables
+    def grid(self, sys=0):
+        nf = (ctypes.c_int * 3)()
+        ns = (ctypes.c_int * 3)()
+        _check(lib.derek_gpu_grid(self._h, sys, nf, ns), self._h, "grid")
+        return tuple(nf), tuple(ns)
+
+    def npw(self, sys=0, k=0):
+        n = ctypes.c_int()
+        _check(lib.derek_gpu_npw(self._h, sys, k, ctypes.byref(n)), self._h, "npw")
+        return n.value
+
+    def gsphere(self, sys=0, k=0):
+        n = self.npw(sys, k)
+        rows = np.zeros(n, dtype=np.int32)
+        fidx = np.zeros(n, dtype=np.int32)
+        kin = np.zeros(n, dtype=np.float64)
+        _check(lib.derek_gpu_gsphere(self._h, sys, k, rows.ctypes.data_as(ctypes.c_void_p),
+                                     fidx.ctypes.data_as(ctypes.c_void_p), _dptr(kin)),
+               self._h, "gsphere")
+        return rows, fidx, kin
+
+    # ---- reference-facing operations
+    def fft_3d(self, grid_values, direction, sys=0):
+        """fft_3d(in_grid, 'FINE', dir) of Source/fft.f90:222-303 (unnormalised)."""
+        a = np.ascontiguousarray(np.asarray(grid_values, dtype=np.complex128)).copy()
+        _check(lib.derek_gpu_fft3d(self._h, sys, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   int(direction)), self._h, "fft3d")
+        return a
+
+    def set_vloc(self, v, sys=0):
+        v = np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+        _check(lib.derek_gpu_set_vloc(self._h, sys, _dptr(v)), self._h, "set_vloc")
+
+    def get_vloc(self, sys=0):
+        nf, _ = self.grid(sys)
+        v = np.zeros(int(np.prod(nf)))
+        _check(lib.derek_gpu_get_vloc(self._h, sys, _dptr(v)), self._h, "get_vloc")
+        return v
+
+    def set_wfn(self, psi, sys=0, k=0):
+        psi = np.ascontiguousarray(np.asarray(psi, dtype=np.complex128))
+        _check(lib.derek_gpu_set_wfn(self._h, sys, k, psi.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+               self._h, "set_wfn")
+
+    def get_wfn(self, sys=0, k=0):
+        nb = self.systems[sys].nbands
+        psi = np.zeros((nb, self.npw(sys, k)), dtype=np.complex128)
+        _check(lib.derek_gpu_get_wfn(self._h, sys, k, psi.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+               self._h, "get_wfn")
+        return psi
+
+    def pot_apply_wfn(self, sys=0, k=0):
+        """H psi of the stored wavefunctions (pot_apply_wfn + kinetic)."""
+        nb = self.systems[sys].nbands
+        out = np.zeros((nb, self.npw(sys, k)), dtype=np.complex128)
+        _check(lib.derek_gpu_apply_h(self._h, sys, k, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+               self._h, "apply_h")
+        return out
+
+    def density_calculate(self, occ, sys=0):
+        """n(r) from the stored wavefunctions and occ(nbands, nk)."""
+        s = self.systems[sys]
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.float64).reshape(len(s.kpts), s.nbands))
+        nf, _ = self.grid(sys)
+        rho = np.zeros(int(np.prod(nf)))
+        _check(lib.derek_gpu_density(self._h, sys, _dptr(occ), _dptr(rho)), self._h, "density")
+        return rho
+
+    def xc_lda(self, rho):
+        rho = np.ascontiguousarray(np.asarray(rho, dtype=np.float64))
+        exc = np.zeros_like(rho)
+        vxc = np.zeros_like(rho)
+        _check(lib.derek_gpu_xc_lda(self._h, ctypes.c_long(rho.size), _dptr(rho), _dptr(exc), _dptr(vxc)),
+               self._h, "xc_lda")
+        return exc, vxc
+
+    def wave_dot(self, sys=0, k=0):
+        """Full overlap matrix S = psi^H psi of the stored wavefunctions."""
+        nb = self.systems[sys].nbands
+        s = np.zeros((nb, nb), dtype=np.complex128)
+        _check(lib.derek_gpu_overlap(self._h, sys, k, s.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+               self._h, "overlap")
+        return s
+
+    # ---- SCF
+    def electronic_scf(self, max_scf=100, etol=1e-8):
+        """Run the SCF to |dF| < etol (Source/electronic.f90:86-175)."""
+        rep = (_abi.ScfReport * len(self.systems))()
+        st = lib.derek_gpu_scf_run(self._h, int(max_scf), float(etol), rep)
+        if st not in (0, _abi.DEREK_ERR_NOT_CONVERGED):
+            _check(st, self._h, "scf_run")
+        return [_abi.report_dict(r) for r in rep]
+
+    def scf_iterate(self):
+        rep = (_abi.ScfReport * len(self.systems))()
+        _check(lib.derek_gpu_scf_iterate(self._h, rep), self._h, "scf_iterate")
+        return [_abi.report_dict(r) for r in rep]
+
+    def eigenvalues(self, sys=0):
+        s = self.systems[sys]
+        e = np.zeros((len(s.kpts), s.nbands))
+        _check(lib.derek_gpu_get_eigenvalues(self._h, sys, _dptr(e)), self._h, "eigenvalues")
+        return e
+
+    def occupations(self, sys=0):
+        s = self.systems[sys]
+        e = np.zeros((len(s.kpts), s.nbands))
+        _check(lib.derek_gpu_get_occupations(self._h, sys, _dptr(e)), self._h, "occupations")
+        return e
+
+    def density(self, sys=0):
+        nf, _ = self.grid(sys)
+        rho = np.zeros(int(np.prod(nf)))
+        _check(lib.derek_gpu_get_density(self._h, sys, _dptr(rho)), self._h, "density")
+        return rho
+
+
+def host_prime_fact(n: int) -> int:
+    return int(lib.derek_host_prime_fact(int(n)))
+
+
+def host_grid_sizes(cell, ecut, g_fine_scale=2.0, policy=DEREK_GRID_REFERENCE):
+    c = (ctypes.c_double * 9)()
+    cell = np.asarray(cell, dtype=np.float64).reshape(3, 3)
+    for i in range(3):
+        for j in range(3):
+            c[3 * j + i] = cell[i, j]
+    ns = (ctypes.c_int * 3)()
+    nf = (ctypes.c_int * 3)()
+    _check(lib.derek_host_grid_sizes(c, float(ecut), float(g_fine_scale), int(policy), ns, nf),
+           None, "grid_sizes")
+    return tuple(ns), tuple(nf)
+
+
+def host_gsphere(inv_cell, ecut, kfrac, n_std):
+    c = (ctypes.c_double * 9)()
+    inv_cell = np.asarray(inv_cell, dtype=np.float64).reshape(3, 3)
+    for i in range(3):
+        for j in range(3):
+            c[3 * j + i] = inv_cell[i, j]
+    k = (ctypes.c_double * 3)(*[float(x) for x in kfrac])
+    ns = (ctypes.c_int * 3)(*[int(x) for x in n_std])
+    n = ctypes.c_int()
+    _check(lib.derek_host_gsphere(c, float(ecut), k, ns, 0, None, ctypes.byref(n)), None, "gsphere")
+    rows = np.zeros(n.value, dtype=np.int32)
+    _check(lib.derek_host_gsphere(c, float(ecut), k, ns, n.value, rows.ctypes.data_as(ctypes.c_void_p),
+                                  ctypes.byref(n)), None, "gsphere")
+    return rows

@@ -1,0 +1,113 @@
+"""ctypes declarations of include/derek_gpu.h and the library loader.
+
+Loading is strict: a missing or unloadable ``libderek_gpu.so`` raises
+ImportError -- there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+DEREK_OK = 0
+DEREK_ERR_BAD_ARG = 1
+DEREK_ERR_OOM = 2
+DEREK_ERR_CUDA = 3
+DEREK_ERR_NOT_CONVERGED = 4
+DEREK_ERR_CHOLESKY = 5
+DEREK_ERR_NAN = 6
+DEREK_ERR_TIMEOUT = 7
+DEREK_ERR_UNSUPPORTED = 8
+
+DEREK_PREC_FP64 = 0
+DEREK_PREC_MIXED = 1
+DEREK_GRID_REFERENCE = 0
+DEREK_GRID_SMOOTH23 = 1
+
+
+class DerekError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status
+
+
+_d = ctypes.c_double
+_i = ctypes.c_int
+_pd = ctypes.POINTER(ctypes.c_double)
+
+
+class SysDesc(ctypes.Structure):
+    _fields_ = [
+        ("cell", _d * 9), ("inv_cell", _d * 9), ("ecut", _d), ("g_fine_scale", _d),
+        ("n_fine", _i * 3), ("grid_policy", _i), ("nk", _i), ("kpts", _pd), ("wk", _pd),
+        ("nbands", _i), ("nspinor", _i), ("nelec", _d), ("kT", _d), ("vext", _pd),
+        ("nwells", _i), ("wells", _pd),
+    ]
+
+
+class ScfOpts(ctypes.Structure):
+    _fields_ = [
+        ("precision", _i), ("mix_alpha", _d), ("kerker_q0", _d), ("pulay_history", _i),
+        ("cheb_degree", _i), ("first_passes", _i), ("first_degree", _i),
+        ("seed", ctypes.c_uint64), ("use_graph", _i), ("use_tensor_cores", _i),
+    ]
+
+
+class ScfReport(ctypes.Structure):
+    _fields_ = [
+        ("energy", _d), ("free_energy", _d), ("delta", _d), ("efermi", _d), ("entropy", _d),
+        ("e_band", _d), ("e_hartree", _d), ("e_xc", _d), ("e_dc", _d),
+        ("iterations", _i), ("converged", _i),
+    ]
+
+
+def report_dict(r: ScfReport) -> dict:
+    return {name: getattr(r, name) for name, _ in ScfReport._fields_}
+
+
+# name -> (restype, argtypes)
+_vp = ctypes.c_void_p
+SIGNATURES = {
+    "derek_gpu_default_opts": (None, [ctypes.POINTER(ScfOpts)]),
+    "derek_gpu_strerror": (ctypes.c_char_p, [_i]),
+    "derek_gpu_last_error": (ctypes.c_char_p, [_vp]),
+    "derek_gpu_create": (_i, [ctypes.POINTER(_vp), ctypes.POINTER(SysDesc), _i, ctypes.POINTER(ScfOpts)]),
+    "derek_gpu_destroy": (_i, [_vp]),
+    "derek_gpu_grid": (_i, [_vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "derek_gpu_npw": (_i, [_vp, _i, _i, ctypes.POINTER(_i)]),
+    "derek_gpu_gsphere": (_i, [_vp, _i, _i, _vp, _vp, _pd]),
+    "derek_gpu_fft3d": (_i, [_vp, _i, _pd, _i]),
+    "derek_gpu_set_vloc": (_i, [_vp, _i, _pd]),
+    "derek_gpu_get_vloc": (_i, [_vp, _i, _pd]),
+    "derek_gpu_set_wfn": (_i, [_vp, _i, _i, _pd]),
+    "derek_gpu_get_wfn": (_i, [_vp, _i, _i, _pd]),
+    "derek_gpu_apply_h": (_i, [_vp, _i, _i, _pd]),
+    "derek_gpu_density": (_i, [_vp, _i, _pd, _pd]),
+    "derek_gpu_xc_lda": (_i, [_vp, ctypes.c_long, _pd, _pd, _pd]),
+    "derek_gpu_overlap": (_i, [_vp, _i, _i, _pd]),
+    "derek_gpu_scf_iterate": (_i, [_vp, ctypes.POINTER(ScfReport)]),
+    "derek_gpu_scf_run": (_i, [_vp, _i, _d, ctypes.POINTER(ScfReport)]),
+    "derek_gpu_get_eigenvalues": (_i, [_vp, _i, _pd]),
+    "derek_gpu_get_occupations": (_i, [_vp, _i, _pd]),
+    "derek_gpu_get_density": (_i, [_vp, _i, _pd]),
+    "derek_host_prime_fact": (_i, [_i]),
+    "derek_host_grid_sizes": (_i, [ctypes.POINTER(_d), _d, _d, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "derek_host_gsphere": (_i, [ctypes.POINTER(_d), _d, ctypes.POINTER(_d), ctypes.POINTER(_i), _i, _vp,
+                                ctypes.POINTER(_i)]),
+}
+
+lib_path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libderek_gpu.so")
+
+
+def _load():
+    if not os.path.exists(lib_path):
+        raise ImportError(f"{lib_path} is missing: run derek_gb300/build.py "
+                          "(there is no CPU fallback for the GPU path)")
+    L = ctypes.CDLL(lib_path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+lib = _load()

@@ -1,0 +1,617 @@
+// Handle creation and the primitive C-ABI entry points (tables, FFT, H.psi,
+// density, XC).  The SCF entry points live in scf.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <new>
+
+#include "basis.h"
+#include "handle.h"
+
+using derek::KSetDev;
+using derek::SysDev;
+
+namespace derek {
+
+int cuda_status(cudaError_t e, derek_gpu *h, const char *what) {
+  if (h) h->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? DEREK_ERR_OOM : DEREK_ERR_CUDA;
+}
+
+__global__ void k_reduce_partials(const SysDev *__restrict__ sys, const KSetDev *__restrict__ ks,
+                                  int s, const double *__restrict__ partial,
+                                  const long long *__restrict__ poff, double *__restrict__ rho) {
+  const SysDev &S = sys[s];
+  if (!S.active) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < S.nr;
+       i += (long long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int k = 0; k < S.nk; ++k) acc += partial[poff[S.ks0 + k] + i];
+    rho[S.grid_off + i] = acc;
+  }
+}
+
+__global__ void k_to_float(long long n, const double *__restrict__ a, float *__restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
+                  void *out, const Axpby *coef) {
+  if (h->prec == DEREK_PREC_FP64) {
+    launch_inv_yz<double>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
+                          (const double2 *)in, (double2 *)h->d_planes, nullptr, h->stream);
+    launch_vmul_x<double>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2],
+                          (double2 *)h->d_planes, h->d_vloc, h->stream);
+    launch_fwd_yz<double>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
+                          (const double2 *)h->d_planes, (const double2 *)in,
+                          (const double2 *)prev, (double2 *)out, coef, h->stream);
+  } else {
+    launch_inv_yz<float>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
+                         (const float2 *)in, (float2 *)h->d_planes, nullptr, h->stream);
+    launch_vmul_x<float>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2],
+                         (float2 *)h->d_planes, h->d_vloc32, h->stream);
+    launch_fwd_yz<float>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
+                         (const float2 *)h->d_planes, (const float2 *)in, (const float2 *)prev,
+                         (float2 *)out, coef, h->stream);
+  }
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+int density_items(derek_gpu *h, const void *psi, double *rho) {
+  if (h->prec == DEREK_PREC_FP64) {
+    launch_inv_yz<double>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const double2 *)psi,
+                          (double2 *)h->d_planes, h->d_occw, h->stream);
+    launch_density_x<double>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
+                             (const double2 *)h->d_planes, h->d_occw, h->d_partial,
+                             h->d_partial_off, h->stream);
+  } else {
+    launch_inv_yz<float>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const float2 *)psi,
+                         (float2 *)h->d_planes, h->d_occw, h->stream);
+    launch_density_x<float>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
+                            (const float2 *)h->d_planes, h->d_occw, h->d_partial,
+                            h->d_partial_off, h->stream);
+  }
+  for (int s = 0; s < h->nsys; ++s)
+    k_reduce_partials<<<152, 256, 0, h->stream>>>(h->d_sys, h->d_ks, s, h->d_partial,
+                                                  h->d_partial_off, rho);
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+int refresh_vloc32(derek_gpu *h) {
+  if (h->prec != DEREK_PREC_FP64)
+    k_to_float<<<152 * 4, 256, 0, h->stream>>>(h->total_grid, h->d_vloc, h->d_vloc32);
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+}  // namespace derek
+
+using namespace derek;
+
+static thread_local std::string g_create_error;
+
+template <typename T> static cudaError_t upload(T **d, const std::vector<T> &v) {
+  size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void **)d, bytes);
+  if (e != cudaSuccess) return e;
+  if (!v.empty()) return cudaMemcpy(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return cudaSuccess;
+}
+
+extern "C" int derek_scf_alloc(derek_gpu_t *);
+extern "C" void derek_scf_free(derek_gpu_t *);
+
+extern "C" {
+
+void derek_gpu_default_opts(derek_scf_opts *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = DEREK_PREC_FP64;
+  o->mix_alpha = 0.3;
+  o->kerker_q0 = 0.0;
+  o->pulay_history = 8;
+  o->cheb_degree = 8;
+  o->first_passes = 4;
+  o->first_degree = 10;
+  o->seed = 20240101ULL;
+  o->use_graph = 1;
+  o->use_tensor_cores = 1;
+}
+
+const char *derek_gpu_strerror(int s) {
+  switch (s) {
+    case DEREK_OK: return "ok";
+    case DEREK_ERR_BAD_ARG: return "invalid argument";
+    case DEREK_ERR_OOM: return "out of device memory";
+    case DEREK_ERR_CUDA: return "CUDA error";
+    case DEREK_ERR_NOT_CONVERGED: return "SCF not converged";
+    case DEREK_ERR_CHOLESKY: return "overlap matrix not positive definite (Cholesky failed)";
+    case DEREK_ERR_NAN: return "NaN detected";
+    case DEREK_ERR_TIMEOUT: return "device wait timed out";
+    case DEREK_ERR_UNSUPPORTED: return "unsupported configuration";
+    default: return "unknown status";
+  }
+}
+
+const char *derek_gpu_last_error(derek_gpu_t *h) {
+  return h ? h->last_error.c_str() : g_create_error.c_str();
+}
+
+int derek_gpu_destroy(derek_gpu_t *h) {
+  if (!h) return DEREK_ERR_BAD_ARG;
+  void *ptrs[] = {h->d_sys,   h->d_ks,      h->d_item_ks, h->d_item_band, h->d_pidx,
+                  h->d_xstart, h->d_rowstart, h->d_rows,  h->d_kin64,     h->d_kin32,
+                  h->d_tw64,  h->d_tw32,    h->d_vext,    h->d_vloc,      h->d_vhxc,
+                  h->d_vloc32, h->d_rho_in, h->d_rho_out, h->d_exc,       h->d_vxc,
+                  h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
+                  h->d_Yp,    h->d_HX,      h->d_planes,  h->d_occw,      h->d_eig,
+                  h->d_occ,   h->d_coef};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  derek_scf_free(h);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return DEREK_OK;
+}
+
+#define FAIL(code, msg)          \
+  do {                           \
+    g_create_error = (msg);      \
+    derek_gpu_destroy(h);        \
+    return (code);               \
+  } while (0)
+
+#define CK(call)                                                         \
+  do {                                                                   \
+    cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess) {                                             \
+      int _c = _e == cudaErrorMemoryAllocation ? DEREK_ERR_OOM : DEREK_ERR_CUDA; \
+      FAIL(_c, std::string(#call) + ": " + cudaGetErrorString(_e));     \
+    }                                                                    \
+  } while (0)
+
+int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
+                     const derek_scf_opts *opts) {
+  if (!out || !desc || nsys <= 0) return DEREK_ERR_BAD_ARG;
+  *out = nullptr;
+  derek_gpu *h = new (std::nothrow) derek_gpu();
+  if (!h) return DEREK_ERR_OOM;
+  if (opts)
+    h->opts = *opts;
+  else
+    derek_gpu_default_opts(&h->opts);
+  h->prec = h->opts.precision;
+  if (h->prec != DEREK_PREC_FP64 && h->prec != DEREK_PREC_MIXED) FAIL(DEREK_ERR_BAD_ARG, "precision");
+  h->nsys = nsys;
+
+  std::vector<int> pidx, xstart, rowstart;
+  std::vector<short> rows;
+  std::vector<float> kin32;
+  std::vector<double> tw64;
+  std::map<int, long long> tw_of;  // n -> offset
+  std::vector<long long> partial_off;
+
+  long long grid_off = 0, psi_off = 0, ent_off = 0, plane_off = 0, row_off = 0, t_off = 0,
+            part_off = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const derek_sys_desc &d = desc[s];
+    if (d.nspinor != 1) FAIL(DEREK_ERR_UNSUPPORTED, "nspinor must be 1");
+    if (d.nk <= 0 || !d.kpts || d.nbands <= 0 || d.ecut <= 0 || !(d.kT > 0) || d.nelec <= 0)
+      FAIL(DEREK_ERR_BAD_ARG, "system " + std::to_string(s) + ": bad sizes");
+    if (d.nelec > 2.0 * d.nbands) FAIL(DEREK_ERR_BAD_ARG, "more electrons than 2 * nbands");
+    SysDev S{};
+    double inv[9];
+    bool have_inv = false;
+    for (int i = 0; i < 9; ++i) have_inv |= d.inv_cell[i] != 0.0;
+    if (have_inv)
+      std::memcpy(inv, d.inv_cell, sizeof(inv));
+    else
+      inverse_cell(d.cell, inv);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) S.B[i * 3 + j] = inv[3 * j + i];
+    int nstd[3], nfine[3];
+    grid_sizes(d.cell, d.ecut, d.g_fine_scale > 0 ? d.g_fine_scale : 2.0, d.grid_policy, nstd, nfine);
+    if (d.n_fine[0] > 0 && d.n_fine[1] > 0 && d.n_fine[2] > 0)
+      for (int i = 0; i < 3; ++i) nfine[i] = d.n_fine[i];
+    for (int i = 0; i < 3; ++i) {
+      if (nfine[i] < 2 || nfine[i] > kMaxDim)
+        FAIL(DEREK_ERR_UNSUPPORTED, "grid size outside 2.." + std::to_string(kMaxDim));
+      // the sphere must fit without wrapping onto itself
+      if (nfine[i] < nstd[i]) FAIL(DEREK_ERR_BAD_ARG, "fine grid smaller than standard box");
+    }
+    const size_t plane_bytes_max = (size_t)std::max({nfine[0] * nfine[2], nfine[1] * nfine[2]}) *
+                                   (h->prec == DEREK_PREC_FP64 ? 16 : 8);
+    if (2 * plane_bytes_max + 8 * (size_t)nfine[0] * nfine[2] + 4096 > 227 * 1024)
+      FAIL(DEREK_ERR_UNSUPPORTED, "grid planes exceed shared memory");
+    for (int i = 0; i < 3; ++i) {
+      S.n[i] = nfine[i];
+      h->n_std.push_back(nstd[i]);
+      h->max_n[i] = std::max(h->max_n[i], nfine[i]);
+      h->max_nmax = std::max(h->max_nmax, nfine[i]);
+      FftPlan &p = S.plan[i];
+      p.n = nfine[i];
+      if (!radix_plan(nfine[i], p.radix, &p.nstages))
+        FAIL(DEREK_ERR_UNSUPPORTED, "grid size " + std::to_string(nfine[i]) + " not 13-smooth");
+      auto it = tw_of.find(nfine[i]);
+      if (it == tw_of.end()) {
+        std::vector<double> w;
+        twiddles(nfine[i], w);
+        long long off = (long long)tw64.size() / 2;
+        tw64.insert(tw64.end(), w.begin(), w.end());
+        tw_of[nfine[i]] = off;
+        p.tw_off = off;
+      } else {
+        p.tw_off = it->second;
+      }
+    }
+    h->max_plane_yz = std::max(h->max_plane_yz, nfine[1] * nfine[2]);
+    S.nr = nfine[0] * nfine[1] * nfine[2];
+    S.nk = d.nk;
+    S.nb = d.nbands;
+    S.ks0 = (int)h->ks.size();
+    S.active = 1;
+    S.volume = cell_volume(d.cell);
+    S.ecut = d.ecut;
+    S.nelec = d.nelec;
+    S.kT = d.kT;
+    S.grid_off = grid_off;
+    grid_off += S.nr;
+    h->max_nb = std::max(h->max_nb, d.nbands);
+
+    std::vector<double> v;
+    if (d.vext)
+      v.assign(d.vext, d.vext + S.nr);
+    else
+      build_vext(d.cell, nfine, d.nelec, d.nwells, d.wells, v);
+    h->vext_host.insert(h->vext_host.end(), v.begin(), v.end());
+
+    for (int k = 0; k < d.nk; ++k) {
+      Sphere sp;
+      build_sphere(inv, d.ecut, d.kpts + 3 * k, nstd, sp);
+      const int npw = (int)sp.box_row.size();
+      if (npw < d.nbands) FAIL(DEREK_ERR_BAD_ARG, "fewer plane waves than bands");
+      KSetDev K{};
+      K.sys = s;
+      K.kidx = k;
+      K.npw = npw;
+      K.npw_pad = (npw + 31) / 32 * 32;
+      K.nb = d.nbands;
+      K.wk = d.wk ? d.wk[k] : 1.0 / d.nk;
+      for (int i = 0; i < 3; ++i) K.kfrac[i] = d.kpts[3 * k + i];
+      const int mxmin = sp.mx.front(), mxmax = sp.mx.back();
+      K.mx_min = mxmin;
+      K.nxr = mxmax - mxmin + 1;
+      if (K.nxr > nfine[0]) FAIL(DEREK_ERR_BAD_ARG, "sphere wider than the fine grid");
+      K.item0 = h->nitems;
+      K.psi_off = psi_off;
+      K.ent_off = ent_off;
+      K.plane_off = plane_off;
+      K.row_off = row_off;
+      K.t_off = t_off;
+      // per-entry tables; entries are sorted by mx (x outermost)
+      std::vector<int> xs(K.nxr + 1, 0), rsv(K.nxr + 1, 0);
+      int e = 0;
+      for (int j = 0; j < K.nxr; ++j) {
+        xs[j] = e;
+        rsv[j] = (int)(rows.size() - row_off);
+        int last_row = -1;
+        while (e < npw && sp.mx[e] == mxmin + j) {
+          const int iy = ((sp.my[e] % nfine[1]) + nfine[1]) % nfine[1];
+          const int iz = ((sp.mz[e] % nfine[2]) + nfine[2]) % nfine[2];
+          pidx.push_back(iy * nfine[2] + iz);
+          if (iy != last_row) {
+            // entries of one (mx,my) are contiguous, so each row appears once
+            rows.push_back((short)iy);
+            last_row = iy;
+          }
+          ++e;
+        }
+      }
+      xs[K.nxr] = e;
+      rsv[K.nxr] = (int)(rows.size() - row_off);
+      xstart.insert(xstart.end(), xs.begin(), xs.end());
+      rowstart.insert(rowstart.end(), rsv.begin(), rsv.end());
+      for (int i = 0; i < npw; ++i) {
+        const int ix = ((sp.mx[i] % nfine[0]) + nfine[0]) % nfine[0];
+        const int iy = ((sp.my[i] % nfine[1]) + nfine[1]) % nfine[1];
+        const int iz = ((sp.mz[i] % nfine[2]) + nfine[2]) % nfine[2];
+        h->box_rows.push_back(sp.box_row[i]);
+        h->fft_index.push_back((ix * nfine[1] + iy) * nfine[2] + iz);
+        h->kin64.push_back(sp.kinetic[i]);
+        kin32.push_back((float)sp.kinetic[i]);
+      }
+      h->max_nxr = std::max(h->max_nxr, K.nxr);
+      ent_off += npw;
+      plane_off += K.nxr + 1;
+      row_off = (long long)rows.size();
+      psi_off += (long long)d.nbands * K.npw_pad;
+      t_off += (long long)d.nbands * K.nxr * nfine[1] * nfine[2];
+      partial_off.push_back(part_off);
+      part_off += S.nr;
+      for (int b = 0; b < d.nbands; ++b) {
+        h->item_ks.push_back((int)h->ks.size());
+        h->item_band.push_back(b);
+      }
+      h->nitems += d.nbands;
+      h->ks.push_back(K);
+    }
+    h->sys.push_back(S);
+  }
+  h->nks = (int)h->ks.size();
+  h->total_psi = psi_off;
+  h->total_planes = t_off;
+  h->total_grid = grid_off;
+  std::vector<float> tw32(tw64.begin(), tw64.end());
+
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK(upload(&h->d_sys, h->sys));
+  CK(upload(&h->d_ks, h->ks));
+  CK(upload(&h->d_item_ks, h->item_ks));
+  CK(upload(&h->d_item_band, h->item_band));
+  CK(upload(&h->d_pidx, pidx));
+  CK(upload(&h->d_xstart, xstart));
+  CK(upload(&h->d_rowstart, rowstart));
+  CK(upload(&h->d_rows, rows));
+  CK(upload(&h->d_kin64, h->kin64));
+  CK(upload(&h->d_kin32, kin32));
+  {
+    std::vector<double2> t(tw64.size() / 2);
+    std::vector<float2> t32(tw64.size() / 2);
+    for (size_t i = 0; i < t.size(); ++i) {
+      t[i] = make_double2(tw64[2 * i], tw64[2 * i + 1]);
+      t32[i] = make_float2((float)tw64[2 * i], (float)tw64[2 * i + 1]);
+    }
+    CK(upload(&h->d_tw64, t));
+    CK(upload(&h->d_tw32, t32));
+  }
+  CK(upload(&h->d_vext, h->vext_host));
+  CK(upload(&h->d_partial_off, partial_off));
+  const size_t gbytes = (size_t)grid_off * sizeof(double);
+  CK(cudaMalloc((void **)&h->d_vloc, gbytes));
+  CK(cudaMemcpy(h->d_vloc, h->d_vext, gbytes, cudaMemcpyDeviceToDevice));
+  CK(cudaMalloc((void **)&h->d_vhxc, gbytes));
+  CK(cudaMemset(h->d_vhxc, 0, gbytes));
+  CK(cudaMalloc((void **)&h->d_vloc32, (size_t)grid_off * sizeof(float)));
+  CK(cudaMalloc((void **)&h->d_rho_in, gbytes));
+  CK(cudaMalloc((void **)&h->d_rho_out, gbytes));
+  CK(cudaMalloc((void **)&h->d_exc, gbytes));
+  CK(cudaMalloc((void **)&h->d_vxc, gbytes));
+  CK(cudaMalloc((void **)&h->d_cgrid, (size_t)grid_off * sizeof(double2)));
+  CK(cudaMalloc((void **)&h->d_partial, (size_t)std::max<long long>(part_off, 1) * sizeof(double)));
+  const size_t pbytes = (size_t)h->total_psi * h->elem_size();
+  CK(cudaMalloc(&h->d_X, pbytes));
+  CK(cudaMalloc(&h->d_Y, pbytes));
+  CK(cudaMalloc(&h->d_Yp, pbytes));
+  CK(cudaMalloc(&h->d_HX, pbytes));
+  CK(cudaMemset(h->d_X, 0, pbytes));
+  CK(cudaMemset(h->d_Y, 0, pbytes));
+  CK(cudaMemset(h->d_Yp, 0, pbytes));
+  CK(cudaMemset(h->d_HX, 0, pbytes));
+  CK(cudaMalloc(&h->d_planes, (size_t)std::max<long long>(h->total_planes, 1) * h->elem_size()));
+  CK(cudaMalloc((void **)&h->d_occw, (size_t)h->nitems * sizeof(double)));
+  CK(cudaMalloc((void **)&h->d_eig, (size_t)h->nitems * sizeof(double)));
+  CK(cudaMalloc((void **)&h->d_occ, (size_t)h->nitems * sizeof(double)));
+  CK(cudaMemset(h->d_eig, 0, (size_t)h->nitems * sizeof(double)));
+  CK(cudaMemset(h->d_occ, 0, (size_t)h->nitems * sizeof(double)));
+  CK(cudaMalloc((void **)&h->d_coef, (size_t)h->nks * sizeof(Axpby)));
+
+  h->tab.sys = h->d_sys;
+  h->tab.ks = h->d_ks;
+  h->tab.item_ks = h->d_item_ks;
+  h->tab.item_band = h->d_item_band;
+  h->tab.pidx = h->d_pidx;
+  h->tab.kin64 = h->d_kin64;
+  h->tab.kin32 = h->d_kin32;
+  h->tab.xstart = h->d_xstart;
+  h->tab.rowstart = h->d_rowstart;
+  h->tab.rows = h->d_rows;
+  h->tab.tw64 = h->d_tw64;
+  h->tab.tw32 = h->d_tw32;
+  if (refresh_vloc32(h) != DEREK_OK) FAIL(DEREK_ERR_CUDA, h->last_error);
+  int st = derek_scf_alloc(h);
+  if (st != DEREK_OK) FAIL(st, h->last_error);
+  CK(cudaStreamSynchronize(h->stream));
+  *out = h;
+  return DEREK_OK;
+}
+
+static int check_sys(derek_gpu_t *h, int s) { return h && s >= 0 && s < h->nsys; }
+static int ks_index(derek_gpu_t *h, int s, int k) {
+  if (!check_sys(h, s) || k < 0 || k >= h->sys[s].nk) return -1;
+  return h->sys[s].ks0 + k;
+}
+
+int derek_gpu_grid(derek_gpu_t *h, int s, int n_fine[3], int n_std[3]) {
+  if (!check_sys(h, s)) return DEREK_ERR_BAD_ARG;
+  for (int i = 0; i < 3; ++i) {
+    if (n_fine) n_fine[i] = h->sys[s].n[i];
+    if (n_std) n_std[i] = h->n_std[3 * s + i];
+  }
+  return DEREK_OK;
+}
+
+int derek_gpu_npw(derek_gpu_t *h, int s, int k, int *npw) {
+  int ki = ks_index(h, s, k);
+  if (ki < 0 || !npw) return DEREK_ERR_BAD_ARG;
+  *npw = h->ks[ki].npw;
+  return DEREK_OK;
+}
+
+int derek_gpu_gsphere(derek_gpu_t *h, int s, int k, int32_t *box_rows, int32_t *fft_index,
+                      double *kinetic) {
+  int ki = ks_index(h, s, k);
+  if (ki < 0) return DEREK_ERR_BAD_ARG;
+  const KSetDev &K = h->ks[ki];
+  for (int i = 0; i < K.npw; ++i) {
+    if (box_rows) box_rows[i] = h->box_rows[K.ent_off + i];
+    if (fft_index) fft_index[i] = h->fft_index[K.ent_off + i];
+    if (kinetic) kinetic[i] = h->kin64[K.ent_off + i];
+  }
+  return DEREK_OK;
+}
+
+int derek_gpu_fft3d(derek_gpu_t *h, int s, double *inout, int dir) {
+  if (!check_sys(h, s) || !inout || (dir != 1 && dir != -1)) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  double2 *g = h->d_cgrid + S.grid_off;
+  DEREK_CUDA(h, cudaMemcpyAsync(g, inout, (size_t)S.nr * sizeof(double2), cudaMemcpyHostToDevice,
+                                h->stream));
+  // dir = +1 is the forward transform, exponent -i
+  launch_fft3d_grid(h->tab, s, 1, h->max_nmax, h->d_cgrid, dir == 1 ? -1 : +1, h->stream);
+  DEREK_CUDA(h, cudaGetLastError());
+  DEREK_CUDA(h, cudaMemcpyAsync(inout, g, (size_t)S.nr * sizeof(double2), cudaMemcpyDeviceToHost,
+                                h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int derek_gpu_set_vloc(derek_gpu_t *h, int s, const double *v) {
+  if (!check_sys(h, s) || !v) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_vloc + S.grid_off, v, (size_t)S.nr * sizeof(double),
+                                cudaMemcpyHostToDevice, h->stream));
+  int st = refresh_vloc32(h);
+  if (st) return st;
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int derek_gpu_get_vloc(derek_gpu_t *h, int s, double *v) {
+  if (!check_sys(h, s) || !v) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  DEREK_CUDA(h, cudaMemcpyAsync(v, h->d_vloc + S.grid_off, (size_t)S.nr * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+// copy between a host complex128 [nb][npw] slice and a padded device buffer
+static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool to_dev) {
+  const KSetDev &K = h->ks[ki];
+  const size_t es = h->elem_size();
+  char *dev = (char *)dev_base + (size_t)K.psi_off * es;
+  const size_t n = (size_t)K.nb * K.npw_pad;
+  if (h->prec == DEREK_PREC_FP64) {
+    DEREK_CUDA(h, cudaMemcpy2DAsync(to_dev ? (void *)dev : (void *)host,
+                                    to_dev ? K.npw_pad * 16 : K.npw * 16,
+                                    to_dev ? (const void *)host : (const void *)dev,
+                                    to_dev ? K.npw * 16 : K.npw_pad * 16, K.npw * 16, K.nb,
+                                    to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                                    h->stream));
+    if (to_dev) {
+      // zero the padding
+      for (int b = 0; b < K.nb && K.npw_pad > K.npw; ++b)
+        DEREK_CUDA(h, cudaMemsetAsync(dev + ((size_t)b * K.npw_pad + K.npw) * es, 0,
+                                      (size_t)(K.npw_pad - K.npw) * es, h->stream));
+    }
+    DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DEREK_OK;
+  }
+  std::vector<float> tmp(2 * n, 0.0f);
+  if (to_dev) {
+    for (int b = 0; b < K.nb; ++b)
+      for (int g = 0; g < K.npw; ++g) {
+        tmp[2 * ((size_t)b * K.npw_pad + g)] = (float)host[2 * ((size_t)b * K.npw + g)];
+        tmp[2 * ((size_t)b * K.npw_pad + g) + 1] = (float)host[2 * ((size_t)b * K.npw + g) + 1];
+      }
+    DEREK_CUDA(h, cudaMemcpyAsync(dev, tmp.data(), n * es, cudaMemcpyHostToDevice, h->stream));
+    DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  } else {
+    DEREK_CUDA(h, cudaMemcpyAsync(tmp.data(), dev, n * es, cudaMemcpyDeviceToHost, h->stream));
+    DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (int b = 0; b < K.nb; ++b)
+      for (int g = 0; g < K.npw; ++g) {
+        host[2 * ((size_t)b * K.npw + g)] = tmp[2 * ((size_t)b * K.npw_pad + g)];
+        host[2 * ((size_t)b * K.npw + g) + 1] = tmp[2 * ((size_t)b * K.npw_pad + g) + 1];
+      }
+  }
+  return DEREK_OK;
+}
+
+int derek_gpu_set_wfn(derek_gpu_t *h, int s, int k, const double *psi) {
+  int ki = ks_index(h, s, k);
+  if (ki < 0 || !psi) return DEREK_ERR_BAD_ARG;
+  return copy_slice(h, ki, h->d_X, const_cast<double *>(psi), true);
+}
+
+int derek_gpu_get_wfn(derek_gpu_t *h, int s, int k, double *psi) {
+  int ki = ks_index(h, s, k);
+  if (ki < 0 || !psi) return DEREK_ERR_BAD_ARG;
+  return copy_slice(h, ki, h->d_X, psi, false);
+}
+
+int derek_gpu_apply_h(derek_gpu_t *h, int s, int k, double *hpsi) {
+  int ki = ks_index(h, s, k);
+  if (ki < 0 || !hpsi) return DEREK_ERR_BAD_ARG;
+  const KSetDev &K = h->ks[ki];
+  int st = apply_h_items(h, K.item0, K.nb, h->d_X, nullptr, h->d_HX, nullptr);
+  if (st) return st;
+  return copy_slice(h, ki, h->d_HX, hpsi, false);
+}
+
+int derek_gpu_density(derek_gpu_t *h, int s, const double *occ, double *rho) {
+  if (!check_sys(h, s) || !occ || !rho) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  // per-item weights w_k f / Omega for this system, zero elsewhere
+  std::vector<double> w(h->nitems, 0.0);
+  for (int k = 0; k < S.nk; ++k) {
+    const KSetDev &K = h->ks[S.ks0 + k];
+    for (int b = 0; b < K.nb; ++b) w[K.item0 + b] = K.wk * occ[(size_t)k * S.nb + b] / S.volume;
+  }
+  // other systems are masked off for the duration of the call
+  std::vector<SysDev> masked = h->sys;
+  for (int i = 0; i < h->nsys; ++i) masked[i].active = (i == s) && h->sys[i].active;
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, masked.data(), masked.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_occw, w.data(), w.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, h->stream));
+  int st = density_items(h, h->d_X, h->d_rho_out);
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
+  if (st) return st;
+  DEREK_CUDA(h, cudaMemcpyAsync(rho, h->d_rho_out + S.grid_off, (size_t)S.nr * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int derek_gpu_xc_lda(derek_gpu_t *h, long n, const double *rho, double *exc, double *vxc) {
+  if (!h || n <= 0 || !rho || (!exc && !vxc)) return DEREK_ERR_BAD_ARG;
+  double *d = nullptr;
+  DEREK_CUDA(h, cudaMalloc((void **)&d, 3 * (size_t)n * sizeof(double)));
+  cudaMemcpyAsync(d, rho, n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  launch_lda(n, d, d + n, d + 2 * n, h->stream);
+  if (exc) cudaMemcpyAsync(exc, d + n, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (vxc) cudaMemcpyAsync(vxc, d + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_status(e, h, "xc_lda");
+  return DEREK_OK;
+}
+
+int derek_host_prime_fact(int n) { return n > 0 ? prime_fact_round(n) : -1; }
+
+int derek_host_grid_sizes(const double cell[9], double ecut, double g_fine_scale, int policy,
+                          int n_std[3], int n_fine[3]) {
+  if (!cell || !n_std || !n_fine || !(ecut > 0)) return DEREK_ERR_BAD_ARG;
+  grid_sizes(cell, ecut, g_fine_scale > 0 ? g_fine_scale : 2.0, policy, n_std, n_fine);
+  return DEREK_OK;
+}
+
+int derek_host_gsphere(const double inv_cell[9], double ecut, const double kfrac[3],
+                       const int n_std[3], int capacity, int32_t *box_rows, int *npw) {
+  if (!inv_cell || !kfrac || !n_std || !npw || !(ecut > 0)) return DEREK_ERR_BAD_ARG;
+  Sphere sp;
+  build_sphere(inv_cell, ecut, kfrac, n_std, sp);
+  *npw = (int)sp.box_row.size();
+  if (box_rows)
+    for (int i = 0; i < *npw && i < capacity; ++i) box_rows[i] = sp.box_row[i];
+  return DEREK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// Shared types and helpers for the DEReK GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <type_traits>
+
+#include "derek_gpu.h"
+
+namespace derek {
+
+// Complex element type per precision: float2 (FP32 path) or double2 (FP64).
+template <typename R> struct CT;
+template <> struct CT<float>  { using T = float2; };
+template <> struct CT<double> { using T = double2; };
+template <typename R> using cplx = typename CT<R>::T;
+
+template <typename R> __host__ __device__ __forceinline__ cplx<R> mk(R x, R y) {
+  cplx<R> c; c.x = x; c.y = y; return c;
+}
+template <typename R> __host__ __device__ __forceinline__ cplx<R> cadd(cplx<R> a, cplx<R> b) {
+  return mk<R>(a.x + b.x, a.y + b.y);
+}
+template <typename R> __host__ __device__ __forceinline__ cplx<R> csub(cplx<R> a, cplx<R> b) {
+  return mk<R>(a.x - b.x, a.y - b.y);
+}
+template <typename R> __host__ __device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
+  return mk<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) * b
+template <typename R> __host__ __device__ __forceinline__ cplx<R> cmulc(cplx<R> a, cplx<R> b) {
+  return mk<R>(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+template <typename R> __host__ __device__ __forceinline__ cplx<R> cscale(cplx<R> a, R s) {
+  return mk<R>(a.x * s, a.y * s);
+}
+
+constexpr int kMaxRadices = 8;
+constexpr int kMaxDim = 128;       // largest FFT length along one axis
+
+// Radix plan of one FFT length (product of radices == n).
+struct FftPlan {
+  int n;
+  int nstages;
+  int radix[kMaxRadices];
+  long long tw_off;   // offset of this length's twiddle table (n entries)
+};
+
+// One independent Kohn-Sham system of a batch.
+struct SysDev {
+  int n[3];
+  int nr;
+  int nk;
+  int nb;
+  int ks0;                 // first k-set index of this system
+  int active;              // 0 once converged (work items exit early)
+  double volume;
+  double B[9];             // inv_cell, row-major: G_i = sum_j B[i*3+j] m_j
+  double ecut;
+  double nelec;
+  double kT;
+  long long grid_off;      // offset of this system's grids (nr entries)
+  FftPlan plan[3];
+};
+
+// One (system, k-point) pair: its plane-wave sphere and buffers.
+struct KSetDev {
+  int sys;
+  int kidx;
+  int npw;
+  int npw_pad;
+  int nb;
+  int nxr;                 // number of x-planes spanned by the sphere
+  int mx_min;              // Miller x of plane 0
+  int item0;               // first (k-set, band) item of this k-set
+  long long psi_off;       // element offset of band 0 in psi-shaped buffers
+  long long ent_off;       // offset into per-sphere-entry tables
+  long long plane_off;     // offset into per-plane tables (nxr + 1 entries)
+  long long row_off;       // offset into active-row lists
+  long long t_off;         // element offset of this k-set in the plane buffer
+  double wk;
+  double kfrac[3];
+};
+
+// Error codes mirrored from the C ABI.
+enum Status : int {
+  OK = DEREK_OK,
+  BAD_ARG = DEREK_ERR_BAD_ARG,
+  OOM = DEREK_ERR_OOM,
+  CUDA = DEREK_ERR_CUDA,
+  NOT_CONVERGED = DEREK_ERR_NOT_CONVERGED,
+  CHOLESKY = DEREK_ERR_CHOLESKY,
+  NAN_DETECTED = DEREK_ERR_NAN,
+  TIMEOUT = DEREK_ERR_TIMEOUT,
+  UNSUPPORTED = DEREK_ERR_UNSUPPORTED,
+};
+
+}  // namespace derek

@@ -1,0 +1,89 @@
+// The handle behind derek_gpu_t: host copies of the batch description and
+// the device arrays, laid out once at creation.
+#pragma once
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+struct derek_gpu {
+  // ---- configuration
+  derek_scf_opts opts;
+  int prec = DEREK_PREC_FP64;
+  int nsys = 0;
+  int nks = 0;
+  int nitems = 0;
+  int max_n[3] = {0, 0, 0};
+  int max_nmax = 0;        // max over all axes and systems
+  int max_nxr = 0;
+  int max_plane_yz = 0;    // max n2*n3
+  int max_nb = 0;
+  long long total_psi = 0; // elements per psi-shaped buffer
+  long long total_planes = 0;
+  long long total_grid = 0;
+
+  // ---- host copies
+  std::vector<derek::SysDev> sys;
+  std::vector<derek::KSetDev> ks;
+  std::vector<int> n_std;          // 3 per system
+  std::vector<int> item_ks, item_band;
+  std::vector<int32_t> box_rows, fft_index;  // per sphere entry (parity hooks)
+  std::vector<double> kin64;
+  std::vector<double> vext_host;   // per system grid, concatenated
+
+  // ---- device tables
+  derek::Tables tab{};
+  derek::SysDev *d_sys = nullptr;
+  derek::KSetDev *d_ks = nullptr;
+  int *d_item_ks = nullptr, *d_item_band = nullptr;
+  int *d_pidx = nullptr, *d_xstart = nullptr, *d_rowstart = nullptr;
+  short *d_rows = nullptr;
+  double *d_kin64 = nullptr;
+  float *d_kin32 = nullptr;
+  double2 *d_tw64 = nullptr;
+  float2 *d_tw32 = nullptr;
+
+  // ---- device grids (FP64, grid_off per system)
+  double *d_vext = nullptr, *d_vloc = nullptr, *d_vhxc = nullptr;
+  float *d_vloc32 = nullptr;
+  double *d_rho_in = nullptr, *d_rho_out = nullptr;
+  double *d_exc = nullptr, *d_vxc = nullptr;
+  double2 *d_cgrid = nullptr;      // complex work grid
+  double *d_partial = nullptr;     // per-k-set density partials
+  long long *d_partial_off = nullptr;
+
+  // ---- device psi-shaped buffers (element type by precision)
+  void *d_X = nullptr, *d_Y = nullptr, *d_Yp = nullptr, *d_HX = nullptr;
+  void *d_planes = nullptr;
+  double *d_occw = nullptr;        // per item: w_k f / Omega (density weights)
+  double *d_eig = nullptr;         // per item
+  double *d_occ = nullptr;         // per item: f in [0, 2]
+  derek::Axpby *d_coef = nullptr;  // per k-set filter coefficients
+
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+
+  size_t elem_size() const { return prec == DEREK_PREC_FP64 ? sizeof(double2) : sizeof(float2); }
+};
+
+namespace derek {
+
+int cuda_status(cudaError_t e, derek_gpu *h, const char *what);
+#define DEREK_CUDA(h, call)                                   \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return derek::cuda_status(_e, h, #call); \
+  } while (0)
+
+// Runs H.psi for items [item_begin, item_begin+nitems) on `in`, writing
+// `out` = alpha H in + beta in + gamma prev with per-k-set coefficients
+// (coef = nullptr: plain H in).
+int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
+                  void *out, const Axpby *coef);
+// Density of every active system from psi buffer `psi` and per-item weights
+// h->d_occw into rho (FP64 grids).
+int density_items(derek_gpu *h, const void *psi, double *rho);
+
+}  // namespace derek

@@ -1,0 +1,190 @@
+/*
+ * derek_gpu.h -- C ABI of the GB300 plane-wave Kohn-Sham hot path.
+ *
+ * The DEReK Fortran driver binds these through iso_c_binding, the same way
+ * Source/fft.f90:57-132 binds FFTW: opaque handle as type(c_ptr), scalars by
+ * value, arrays as assumed-size C_DOUBLE / C_DOUBLE_COMPLEX buffers.  Every
+ * entry point returns an int status (0 = DEREK_OK); derek_gpu_strerror maps a
+ * status to text for io_errors (Source/io.f90:885-930).
+ *
+ * Conventions
+ *   units       Hartree atomic units (Ha, bohr), as after io_convert_all
+ *               (Source/io.f90:324-358).
+ *   cell        column-major like the Fortran cell(3,3): cell[3*j + i] is
+ *               cell(i+1, j+1); column j is lattice vector j
+ *               (r = cell . frac, Source/basis.f90:166-167).
+ *   inv_cell    transpose(2 pi cell^-1) as Source/io.f90:1954, same storage.
+ *   grids       flat z-fastest order, index (ix*ny + iy)*nz + iz
+ *               (Source/fft.f90:260,273).
+ *   G order     the reference's centred standard-box order, x outermost and
+ *               z innermost (Source/basis.f90:125-135); a k-point's sphere is
+ *               the ordered subsequence with 1/2|k+G|^2 <= ecut.
+ *   psi         [band][npw] interleaved complex, G fastest (the reference's
+ *               coeff(gvec, kpt, band, spinor) slice for one k, nspinor = 1).
+ *   ownership   host arrays stay owned by the caller and are copied; device
+ *               memory belongs to the handle.
+ *   threading   one host thread per handle; all work runs on the handle's
+ *               own CUDA stream.
+ */
+#ifndef DEREK_GPU_H
+#define DEREK_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define DEREK_OK                 0
+#define DEREK_ERR_BAD_ARG        1
+#define DEREK_ERR_OOM            2
+#define DEREK_ERR_CUDA           3
+#define DEREK_ERR_NOT_CONVERGED  4
+#define DEREK_ERR_CHOLESKY       5
+#define DEREK_ERR_NAN            6
+#define DEREK_ERR_TIMEOUT        7
+#define DEREK_ERR_UNSUPPORTED    8
+
+/* precision modes */
+#define DEREK_PREC_FP64   0   /* complex128 psi, FP64 FFTs and contractions */
+#define DEREK_PREC_MIXED  1   /* complex64 psi, FP32 FFTs and H.psi, BF16x3
+                                 tensor-core contractions; FP64 Cholesky,
+                                 Jacobi, occupations, densities, energies */
+
+/* grid policies for n_fine = 0 */
+#define DEREK_GRID_REFERENCE 0  /* basis_prime_fact: {2,3,5,7,11,13}-smooth */
+#define DEREK_GRID_SMOOTH23  1  /* {2,3}-smooth */
+
+typedef struct derek_gpu derek_gpu_t;
+
+/* One independent system.  Mirrors the fields of current_structure /
+ * current_params the hot path reads (Source/io.f90:63-114,171-194). */
+typedef struct {
+  double cell[9];          /* bohr, column-major cell(3,3) */
+  double inv_cell[9];      /* transpose(2 pi cell^-1); all zero = derive */
+  double ecut;             /* cut_off_energy, Ha */
+  double g_fine_scale;     /* Source/io.f90:73 default 2.0 */
+  int    n_fine[3];        /* fine FFT grid; zeros = derive (grid_policy) */
+  int    grid_policy;      /* DEREK_GRID_* */
+  int    nk;               /* number of k-points */
+  const double *kpts;      /* nk*3 fractional (reciprocal basis) */
+  const double *wk;        /* nk weights summing to 1; NULL = uniform */
+  int    nbands;           /* n_electrons + conduction_bands (io.f90:316) */
+  int    nspinor;          /* 1 (2 = non-collinear, not supported yet) */
+  double nelec;            /* n_electrons */
+  double kT;               /* electronic_temp converted to Ha, > 0 */
+  const double *vext;      /* nr FP64 values, or NULL to build from wells */
+  int    nwells;           /* Gaussian wells: jellium + sum of wells */
+  const double *wells;     /* nwells*5: cx cy cz (fractional) depth width */
+} derek_sys_desc;
+
+/* SCF options (keys the reference lacks; defaults in derek_gpu_default_opts). */
+typedef struct {
+  int    precision;        /* DEREK_PREC_* */
+  double mix_alpha;        /* Pulay/linear mixing amplitude */
+  double kerker_q0;        /* Kerker wavevector (1/bohr); 0 = no Kerker */
+  int    pulay_history;    /* stored (n_in, residual) pairs, <= 16 */
+  int    cheb_degree;      /* Chebyshev filter degree per SCF iteration */
+  int    first_passes;     /* filter passes in the first SCF iteration */
+  int    first_degree;     /* filter degree of those passes */
+  uint64_t seed;           /* start-vector hash seed */
+  int    use_graph;        /* capture each SCF iteration in a CUDA graph */
+  int    use_tensor_cores; /* mixed mode: tcgen05 BF16x3 contractions */
+} derek_scf_opts;
+
+/* Per-system SCF report (Source/electronic.f90:143-146 table row). */
+typedef struct {
+  double energy;           /* Kohn-Sham total energy of the output density */
+  double free_energy;      /* energy - kT * entropy (the converged quantity) */
+  double delta;            /* |F - F_prev| of the last iteration */
+  double efermi;           /* Fermi level */
+  double entropy;
+  double e_band, e_hartree, e_xc, e_dc;
+  int    iterations;
+  int    converged;
+} derek_scf_report;
+
+void derek_gpu_default_opts(derek_scf_opts *opts);
+const char *derek_gpu_strerror(int status);
+/* Detail text of the last failure on h (h = NULL: the last failed create). */
+const char *derek_gpu_last_error(derek_gpu_t *h);
+
+/* Create a handle over nsys independent systems.  Replaces the set-up the
+ * reference spreads over basis_init (Source/basis.f90:65-241), fft_init
+ * (Source/fft.f90:139-219), state_init (Source/state.f90:59-168) and
+ * pot_external_pot (Source/pot.f90:104-190). */
+int derek_gpu_create(derek_gpu_t **h, const derek_sys_desc *sys, int nsys,
+                     const derek_scf_opts *opts);
+int derek_gpu_destroy(derek_gpu_t *h);
+
+/* Sizes: fine grid, standard box and sphere size of (sys, k). */
+int derek_gpu_grid(derek_gpu_t *h, int sys, int n_fine[3], int n_std[3]);
+int derek_gpu_npw(derek_gpu_t *h, int sys, int k, int *npw);
+
+/* Sphere of (sys, k): 0-based row numbers into the standard-box G list
+ * (basis.f90:125-135) and the flat fine-grid FFT index of each entry.
+ * Parity hook for the G tables (Source/basis.f90:125-149). */
+int derek_gpu_gsphere(derek_gpu_t *h, int sys, int k, int32_t *box_rows,
+                      int32_t *fft_index, double *kinetic);
+
+/* In-place unnormalised 3D c2c FFT of one fine-grid array of system sys.
+ * dir = +1 forward (exponent -i), -1 backward (+i).  Replaces fft_3d with
+ * grid='FINE' (Source/fft.f90:222-303). */
+int derek_gpu_fft3d(derek_gpu_t *h, int sys, double *inout_interleaved, int dir);
+
+/* Local potential used by H.psi: V_ext + V_H + v_xc on the fine grid (FP64). */
+int derek_gpu_set_vloc(derek_gpu_t *h, int sys, const double *vloc);
+int derek_gpu_get_vloc(derek_gpu_t *h, int sys, double *vloc);
+
+/* Wavefunction slice of (sys, k): nb bands x npw interleaved complex128. */
+int derek_gpu_set_wfn(derek_gpu_t *h, int sys, int k, const double *psi);
+int derek_gpu_get_wfn(derek_gpu_t *h, int sys, int k, double *psi);
+
+/* H.psi on the handle's stored wavefunctions of (sys, k) with the current
+ * local potential; result copied to hpsi (nb x npw complex128).
+ * Replaces pot_apply_wfn (Source/pot.f90:344-382) plus the kinetic term. */
+int derek_gpu_apply_h(derek_gpu_t *h, int sys, int k, double *hpsi);
+
+/* n(r) = sum_k w_k sum_b occ[k][b] |psi_kb(r)|^2 / Omega from the stored
+ * wavefunctions.  Replaces density_calculate (Source/density.f90:101-130);
+ * occ is occ(nbands, nk) as state_data%occ (Source/state.f90:43). */
+int derek_gpu_density(derek_gpu_t *h, int sys, const double *occ, double *rho);
+
+/* LDA (Slater exchange + Perdew-Wang 92 correlation, libxc ids 1 + 12),
+ * spin-unpolarised: exc = energy per particle, vxc = potential. */
+int derek_gpu_xc_lda(derek_gpu_t *h, long n, const double *rho, double *exc,
+                     double *vxc);
+
+/* Overlap S = psi^H psi of the stored wavefunctions of (sys, k):
+ * nb x nb complex128, row-major S[i*nb + j] = <psi_i|psi_j>.
+ * The reference's wave_dot_* (Source/wave.f90:929-1036), as a full matrix. */
+int derek_gpu_overlap(derek_gpu_t *h, int sys, int k, double *s);
+
+/* Self-consistent field.  scf_iterate runs one iteration on every active
+ * system; scf_run iterates until |dF| < etol or max_scf iterations
+ * (Source/electronic.f90:86-175).  rep has one entry per system. */
+int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep);
+int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol,
+                      derek_scf_report *rep);
+
+/* Results of the last SCF iteration. */
+int derek_gpu_get_eigenvalues(derek_gpu_t *h, int sys, double *eig /* nk*nb */);
+int derek_gpu_get_occupations(derek_gpu_t *h, int sys, double *occ /* nk*nb */);
+int derek_gpu_get_density(derek_gpu_t *h, int sys, double *rho /* nr */);
+
+/* Host-only helpers (no GPU needed): the grid and sphere rules the handle
+ * uses, exposed so drivers and tests can check them on any machine. */
+int derek_host_prime_fact(int n);  /* Source/basis.f90:257-309 */
+int derek_host_grid_sizes(const double cell[9], double ecut, double g_fine_scale,
+                          int grid_policy, int n_std[3], int n_fine[3]);
+/* Sphere of one k-point; writes at most `capacity` rows, returns the count
+ * in *npw (call with capacity 0 to size). */
+int derek_host_gsphere(const double inv_cell[9], double ecut, const double kfrac[3],
+                       const int n_std[3], int capacity, int32_t *box_rows, int *npw);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DEREK_GPU_H */

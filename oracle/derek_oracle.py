@@ -1,0 +1,598 @@
+"""CPU FP64 oracle for the DEReK plane-wave Kohn-Sham hot path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker the GPU library is
+compared against; nothing in the shipped library imports it.  Only the tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may use it.
+
+What it restates, and from where (paths are inside the DEReK source tree):
+
+* FFT grid sizing          Source/basis.f90:87-95 (k_cut, std and fine sizes)
+* smooth-size rounding     Source/basis.f90:257-309 (basis_prime_fact, 13-smooth)
+* reciprocal cell          Source/io.f90:1954 (inv_cell = transpose(2 pi cell^-1))
+* lattice lengths          Source/io.f90:1956-1966 (norms of the columns of cell)
+* centred G enumeration    Source/basis.f90:125-149 (x outer, z inner)
+* real-space grid          Source/basis.f90:156-188 (frac = i/n, i = 1..n)
+* Monkhorst-Pack k-points  Source/io.f90:2016-2031 (k = n d - (1 + d)/2)
+* FFT sign / layout        Source/fft.f90:204-212, 260-291 (dir=+1 forward e^{-i},
+                           dir=-1 backward e^{+i}, neither normalised, flat
+                           index (ix*ny + iy)*nz + iz)
+* jellium potential        Source/pot.f90:131-136 (diag = 0.5 Ne / N_fine;
+                           V = (V11 + V22)/2 as in Source/xsf.f90:44-45)
+* nbands                   Source/io.f90:316 (n_electrons + conduction_bands)
+* LDA exchange/correlation libxc 6.2.2 vendored in ExLib/libxc:
+                           maple/util.mpl:39-97 (LDA_X_FACTOR, RS_FACTOR),
+                           maple/lda_exc/lda_c_pw.mpl:18-45 (PW92, id 12),
+                           src/lda_c_pw.c:41-50 (parameters),
+                           src/work_lda_inc.c:50-56 (density threshold 1e-15)
+
+Everything the reference never implemented (its SCF loop, density, V.psi and
+overlap routines are stubs: Source/electronic.f90:135-167,
+Source/density.f90:101-130, Source/pot.f90:344-382, Source/wave.f90:929-1036)
+is textbook plane-wave DFT, written out below: kinetic 1/2|k+G|^2, Hartree
+4 pi n(G)/|G|^2 with G=0 dropped, Fermi-Dirac occupations with bisection for
+the Fermi level, Pulay (DIIS) density mixing with optional Kerker
+preconditioning, and the Kohn-Sham total and free energies.
+
+Units are Hartree atomic units throughout.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+TWO_PI = 2.0 * math.pi
+FOUR_PI = 4.0 * math.pi
+DENS_THRESHOLD = 1e-15  # libxc lda_x.c:63 / lda_c_pw.c:130
+
+
+# --------------------------------------------------------------------------
+# Grid sizing and reciprocal-space tables
+# --------------------------------------------------------------------------
+
+def prime_fact_round(n: int, primes=(2, 3, 5, 7, 11, 13), max_cycles: int = 100) -> int:
+    """Smallest m >= n whose prime factors all lie in ``primes``.
+
+    Restates basis_prime_fact (Source/basis.f90:257-309): strip every listed
+    prime from N repeatedly; if nothing else remains N is accepted, otherwise
+    N is incremented (at most ``max_cycles`` times).
+    """
+    for _ in range(max_cycles):
+        m = n
+        changed = True
+        while changed:
+            changed = False
+            for p in primes:
+                if m % p == 0:
+                    m //= p
+                    changed = True
+        if m == 1:
+            return n
+        n += 1
+    return n
+
+
+def smooth23_round(n: int) -> int:
+    """Smallest m >= n of the form 2^a 3^b (the {2,3}-smooth grid policy)."""
+    return prime_fact_round(n, primes=(2, 3), max_cycles=1 << 20)
+
+
+def lattice_lengths(cell: np.ndarray) -> np.ndarray:
+    """|a|,|b|,|c| as the norms of the columns of cell (Source/io.f90:1956-1966)."""
+    cell = np.asarray(cell, dtype=np.float64)
+    return np.sqrt((cell ** 2).sum(axis=0))
+
+
+def inv_cell(cell: np.ndarray) -> np.ndarray:
+    """transpose(2 pi * inverse(cell)) (Source/io.f90:1954).
+
+    G = inv_cell @ (i, j, k) for integer Miller indices (Source/basis.f90:130-131).
+    """
+    return np.ascontiguousarray((TWO_PI * np.linalg.inv(np.asarray(cell, dtype=np.float64))).T)
+
+
+def cell_volume(cell: np.ndarray) -> float:
+    return float(abs(np.linalg.det(np.asarray(cell, dtype=np.float64))))
+
+
+def grid_sizes(cell, ecut: float, g_fine_scale: float = 2.0, policy: str = "reference"):
+    """Standard and fine FFT grid sizes (Source/basis.f90:87-105).
+
+    policy "reference": round the fine grid to {2,3,5,7,11,13}-smooth sizes as
+    the reference; policy "smooth23": round it to {2,3}-smooth sizes.  The
+    standard box is always rounded by the reference rule.
+    Returns (n_std[3], n_fine[3]) as int tuples.
+    """
+    k_cut = math.sqrt(2.0 * ecut)
+    lengths = lattice_lengths(cell)
+    std = [math.ceil(k_cut * L / math.pi) for L in lengths]
+    fine = [math.ceil(g_fine_scale * k_cut * L / math.pi) for L in lengths]
+    rnd = prime_fact_round if policy == "reference" else smooth23_round
+    # the standard box defines the G list, so it always follows the reference rule
+    return tuple(prime_fact_round(n) for n in std), tuple(rnd(n) for n in fine)
+
+
+def centred_range(n: int) -> np.ndarray:
+    """Miller range -n/2 .. n - n/2 - 1 with Fortran integer division (basis.f90:126)."""
+    return np.arange(-(n // 2), n - n // 2, dtype=np.int64)
+
+
+def miller_box(n_std) -> np.ndarray:
+    """Centred Miller indices of the standard box, x outermost, z innermost
+    (Source/basis.f90:125-135).  Row ig-1 holds grid_points(ig,:) / inv_cell."""
+    rx, ry, rz = (centred_range(n) for n in n_std)
+    mx, my, mz = np.meshgrid(rx, ry, rz, indexing="ij")
+    return np.stack([mx.ravel(), my.ravel(), mz.ravel()], axis=1)
+
+
+def mp_kpoints(grid) -> np.ndarray:
+    """Monkhorst-Pack list in fractional reciprocal coordinates
+    (Source/io.f90:2016-2031): k_i = n d - (1 + d)/2, d = 1/N_i, n = 1..N_i,
+    x outermost, z innermost."""
+    out = []
+    d = [1.0 / g for g in grid]
+    for a in range(1, grid[0] + 1):
+        for b in range(1, grid[1] + 1):
+            for c in range(1, grid[2] + 1):
+                out.append([a * d[0] - (1.0 + d[0]) / 2,
+                            b * d[1] - (1.0 + d[1]) / 2,
+                            c * d[2] - (1.0 + d[2]) / 2])
+    return np.array(out, dtype=np.float64)
+
+
+def gsphere(cell, ecut: float, kfrac, n_std, inv_cell_given=None):
+    """Plane-wave sphere for one k-point.
+
+    The sphere is the ordered subsequence of the reference's standard-box
+    G list (Source/basis.f90:125-135) with 1/2 |k+G|^2 <= ecut.  Returns
+    (box_rows, miller, kinetic): 0-based row numbers into the box list, the
+    Miller indices (Npw,3) and 1/2|k+G|^2 (Npw,).
+    """
+    B = inv_cell(cell) if inv_cell_given is None else np.asarray(inv_cell_given, dtype=np.float64)
+    m = miller_box(n_std)
+    kq = m.astype(np.float64) + np.asarray(kfrac, dtype=np.float64)[None, :]
+    # G_i = inv_cell(i,1) q1 + inv_cell(i,2) q2 + inv_cell(i,3) q3, summed left to
+    # right without fused multiply-adds (the order of Fortran's matmul loop)
+    g = [(B[i, 0] * kq[:, 0] + B[i, 1] * kq[:, 1]) + B[i, 2] * kq[:, 2] for i in range(3)]
+    kin = 0.5 * ((g[0] * g[0] + g[1] * g[1]) + g[2] * g[2])
+    rows = np.nonzero(kin <= ecut)[0]
+    return rows.astype(np.int64), m[rows], kin[rows]
+
+
+def fft_flat_index(miller: np.ndarray, n_fine) -> np.ndarray:
+    """Flat z-fastest index (ix*ny + iy)*nz + iz of Miller indices wrapped
+    into the fine FFT box (Source/fft.f90:260,273 layout)."""
+    n1, n2, n3 = n_fine
+    ix = np.mod(miller[:, 0], n1)
+    iy = np.mod(miller[:, 1], n2)
+    iz = np.mod(miller[:, 2], n3)
+    return (ix * n2 + iy) * n3 + iz
+
+
+def fft_miller(n: int) -> np.ndarray:
+    """Miller index of each FFT index 0..n-1 under the reference's centred
+    convention: i for i < n - n/2, else i - n (basis.f90:126 range)."""
+    i = np.arange(n, dtype=np.int64)
+    return np.where(i < n - n // 2, i, i - n)
+
+
+def gvec_sq_grid(cell, n_fine) -> np.ndarray:
+    """|G|^2 on the fine FFT box (n1,n2,n3)."""
+    B = inv_cell(cell)
+    m1, m2, m3 = (fft_miller(n) for n in n_fine)
+    M = np.stack(np.meshgrid(m1, m2, m3, indexing="ij"), axis=-1).astype(np.float64)
+    G = M @ B.T
+    return (G * G).sum(axis=-1)
+
+
+def real_frac_points(n_fine) -> np.ndarray:
+    """Fractional coordinates of the reference's real grid, frac = i/n with
+    i = 1..n (Source/basis.f90:156-188), z-fastest flat order, shape (N,3)."""
+    f = [np.arange(1, n + 1, dtype=np.float64) / n for n in n_fine]
+    fx, fy, fz = np.meshgrid(*f, indexing="ij")
+    return np.stack([fx.ravel(), fy.ravel(), fz.ravel()], axis=1)
+
+
+# --------------------------------------------------------------------------
+# External potential
+# --------------------------------------------------------------------------
+
+def vext_jellium_wells(cell, n_fine, n_electrons: float, wells) -> np.ndarray:
+    """Jellium constant plus attractive Gaussian wells on the fine grid.
+
+    The constant follows the reference's 'jelly' case (Source/pot.f90:133-134:
+    each diagonal entry 0.5 Ne / N_fine, so V = (V11+V22)/2 = 0.5 Ne / N_fine).
+    Each well i (fractional centre c_i, depth U_i > 0, width w_i) subtracts
+    U_i exp(-|r - R_i|^2 / (2 w_i^2)) using the minimum-image distance.  The
+    reference parses such wells (Source/io.f90:1888-1922) but sets them to
+    zero (Source/pot.f90:165-166); this is the intended form.
+    Points are sampled at the reference's real grid (frac = i/n, i = 1..n).
+    Returns V(r) as a flat float64 array in z-fastest order.
+    """
+    cell = np.asarray(cell, dtype=np.float64)
+    N = int(np.prod(n_fine))
+    frac = real_frac_points(n_fine)
+    v = np.full(N, 0.5 * n_electrons / N, dtype=np.float64)
+    for (cx, cy, cz, depth, width) in np.asarray(wells, dtype=np.float64).reshape(-1, 5):
+        d = frac - np.array([cx, cy, cz])[None, :]
+        d -= np.rint(d)
+        r = d @ cell.T
+        r2 = (r * r).sum(axis=1)
+        v -= depth * np.exp(-r2 / (2.0 * width * width))
+    return v
+
+
+def random_wells(rng: np.random.Generator, count: int,
+                 depth=(1.0, 3.0), width=(0.8, 1.5)) -> np.ndarray:
+    """Seeded wells: rows (cx, cy, cz, depth, width), centres fractional U[0,1)."""
+    c = rng.random((count, 3))
+    d = rng.uniform(depth[0], depth[1], count)
+    w = rng.uniform(width[0], width[1], count)
+    return np.concatenate([c, d[:, None], w[:, None]], axis=1)
+
+
+# --------------------------------------------------------------------------
+# FFT with the reference's conventions
+# --------------------------------------------------------------------------
+
+def fft3d(flat: np.ndarray, n_fine, direction: int) -> np.ndarray:
+    """3D c2c DFT of a z-fastest flat array, unnormalised both ways.
+
+    direction=+1 is FFTW_FORWARD (exponent -i), direction=-1 FFTW_BACKWARD
+    (exponent +i), Source/fft.f90:264-284.  numpy.fft stands in for FFTW.
+    """
+    a = np.asarray(flat, dtype=np.complex128).reshape(n_fine)
+    if direction == 1:
+        out = np.fft.fftn(a)
+    elif direction == -1:
+        out = np.fft.ifftn(a) * a.size
+    else:
+        raise ValueError("direction must be +1 or -1")
+    return out.ravel()
+
+
+# --------------------------------------------------------------------------
+# LDA exchange-correlation (Slater + Perdew-Wang 92), spin-unpolarised
+# --------------------------------------------------------------------------
+
+PW92 = dict(a=0.031091, alpha1=0.21370, beta1=7.5957, beta2=3.5876,
+            beta3=1.6382, beta4=0.49294, p=1.0)
+
+
+def lda_x_c(rho: np.ndarray):
+    """(eps_x, v_x, eps_c, v_c) for spin-unpolarised densities.
+
+    Exchange: eps_x = -(3/4)(3/pi)^{1/3} n^{1/3} (maple/util.mpl:58,86-94 with
+    zeta=0), v_x = 4/3 eps_x.  Correlation: PW92 G(rs) of
+    maple/lda_exc/lda_c_pw.mpl:34-37 with the first parameter column of
+    src/lda_c_pw.c:41-50 (zeta = 0 kills the spin-stiffness terms),
+    v_c = eps_c - rs/3 d eps_c/d rs.  rs = (3/(4 pi n))^{1/3}.
+    Densities below 1e-15 give zeros (src/work_lda_inc.c:50); exchange is also
+    screened when n/2 <= 1e-15 (maple/util.mpl:102).
+    """
+    rho = np.asarray(rho, dtype=np.float64)
+    out = [np.zeros_like(rho) for _ in range(4)]
+    mask = rho >= DENS_THRESHOLD
+    n = np.maximum(rho[mask], DENS_THRESHOLD)
+    ex = -0.75 * (3.0 / math.pi) ** (1.0 / 3.0) * np.cbrt(n)
+    xmask = (0.5 * n) > DENS_THRESHOLD
+    ex = np.where(xmask, ex, 0.0)
+    vx = 4.0 / 3.0 * ex
+    rs = (3.0 / (FOUR_PI * n)) ** (1.0 / 3.0)
+    P = PW92
+    srs = np.sqrt(rs)
+    q0 = -2.0 * P["a"] * (1.0 + P["alpha1"] * rs)
+    q1 = 2.0 * P["a"] * (P["beta1"] * srs + P["beta2"] * rs + P["beta3"] * rs * srs
+                         + P["beta4"] * rs ** (P["p"] + 1.0))
+    dq1 = P["a"] * (P["beta1"] / srs + 2.0 * P["beta2"] + 3.0 * P["beta3"] * srs
+                    + 2.0 * (P["p"] + 1.0) * P["beta4"] * rs ** P["p"])
+    lg = np.log(1.0 + 1.0 / q1)  # libxc evaluates log(1 + x), not log1p
+    ec = q0 * lg
+    dec = -2.0 * P["a"] * P["alpha1"] * lg - q0 * dq1 / (q1 * q1 + q1)
+    vc = ec - rs / 3.0 * dec
+    for o, v in zip(out, (ex, vx, ec, vc)):
+        o[mask] = v
+    return tuple(out)
+
+
+def lda_exc_vxc(rho: np.ndarray):
+    ex, vx, ec, vc = lda_x_c(rho)
+    return ex + ec, vx + vc
+
+
+# --------------------------------------------------------------------------
+# Deterministic start vectors (same hash as the GPU library)
+# --------------------------------------------------------------------------
+
+MASK64 = (1 << 64) - 1
+
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    x = (x + np.uint64(0x9E3779B97F4A7C15)) & np.uint64(MASK64)
+    z = x
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & np.uint64(MASK64)
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & np.uint64(MASK64)
+    return z ^ (z >> np.uint64(31))
+
+
+def start_wavefunctions(seed: int, sys_index: int, k_index: int, nbands: int, npw: int) -> np.ndarray:
+    """Real start coefficients r - 0.5 per (band, G) like wave_initialise_wfn
+    (Source/wave.f90:873-886), drawn from a counter hash instead of the
+    Fortran generator so every implementation produces the same numbers.
+    Returns (nbands, npw) complex128."""
+    with np.errstate(over="ignore"):
+        b = np.arange(nbands, dtype=np.uint64)[:, None]
+        g = np.arange(npw, dtype=np.uint64)[None, :]
+        key = (np.uint64(seed) * np.uint64(0x100000001B3)
+               ^ (np.uint64(sys_index) << np.uint64(40))
+               ^ (np.uint64(k_index) << np.uint64(24)))
+        ctr = (key + b * np.uint64(1 << 20) + g) & np.uint64(MASK64)
+        h = splitmix64(ctr)
+    u = (h >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    return (u - 0.5).astype(np.complex128)
+
+
+# --------------------------------------------------------------------------
+# System description
+# --------------------------------------------------------------------------
+
+@dataclass
+class System:
+    cell: np.ndarray
+    ecut: float
+    n_fine: tuple
+    n_std: tuple
+    kpts: np.ndarray            # (nk,3) fractional
+    wk: np.ndarray              # (nk,) weights summing to 1
+    nbands: int
+    nelec: float
+    kT: float
+    vext: np.ndarray            # flat (N,)
+    wells: np.ndarray = field(default_factory=lambda: np.zeros((0, 5)))
+
+    @property
+    def nr(self) -> int:
+        return int(np.prod(self.n_fine))
+
+    @property
+    def volume(self) -> float:
+        return cell_volume(self.cell)
+
+
+def make_system(L: float, ecut: float, nelec: float, nbands: int, wells,
+                kgrid=(1, 1, 1), kpts=None, kT: float = 0.01,
+                policy: str = "smooth23", g_fine_scale: float = 2.0) -> System:
+    """Cubic-cell system with the jellium + wells potential."""
+    cell = np.eye(3) * float(L)
+    n_std, n_fine = grid_sizes(cell, ecut, g_fine_scale, policy)
+    if kpts is None:
+        kpts = mp_kpoints(kgrid)
+    kpts = np.asarray(kpts, dtype=np.float64).reshape(-1, 3)
+    wk = np.full(len(kpts), 1.0 / len(kpts))
+    wells = np.asarray(wells, dtype=np.float64).reshape(-1, 5)
+    vext = vext_jellium_wells(cell, n_fine, nelec, wells)
+    return System(cell, ecut, tuple(n_fine), tuple(n_std), kpts, wk, nbands,
+                  float(nelec), float(kT), vext, wells)
+
+
+# --------------------------------------------------------------------------
+# Hamiltonian pieces
+# --------------------------------------------------------------------------
+
+class KBasis:
+    """Sphere data of one k-point: Miller indices, FFT indices, kinetic."""
+
+    def __init__(self, sys: System, ik: int):
+        rows, mil, kin = gsphere(sys.cell, sys.ecut, sys.kpts[ik], sys.n_std)
+        self.rows = rows
+        self.miller = mil
+        self.kinetic = kin
+        self.fidx = fft_flat_index(mil, sys.n_fine)
+        self.npw = len(rows)
+
+
+def apply_h(sys: System, kb: KBasis, vloc: np.ndarray, psi: np.ndarray) -> np.ndarray:
+    """H psi for psi of shape (nb, npw): 1/2|k+G|^2 psi + (1/N) F[V F^-1 psi].
+
+    F^-1 is the reference's unnormalised backward transform (dir=-1) and F the
+    forward one (dir=+1); the 1/N restores the DFT normalisation.
+    """
+    N = sys.nr
+    out = np.empty_like(psi)
+    box = np.zeros(N, dtype=np.complex128)
+    for b in range(psi.shape[0]):
+        box[:] = 0
+        box[kb.fidx] = psi[b]
+        r = fft3d(box, sys.n_fine, -1)
+        r *= vloc
+        g = fft3d(r, sys.n_fine, 1)
+        out[b] = kb.kinetic * psi[b] + g[kb.fidx] / N
+    return out
+
+
+def dense_h(sys: System, kb: KBasis, vloc: np.ndarray) -> np.ndarray:
+    """Dense Npw x Npw Hamiltonian: T + V(G - G') with V(G) = F[V]/N."""
+    vG = fft3d(vloc.astype(np.complex128), sys.n_fine, 1).reshape(sys.n_fine) / sys.nr
+    d = kb.miller[:, None, :] - kb.miller[None, :, :]
+    n1, n2, n3 = sys.n_fine
+    H = vG[np.mod(d[..., 0], n1), np.mod(d[..., 1], n2), np.mod(d[..., 2], n3)]
+    H[np.diag_indices_from(H)] += kb.kinetic
+    return H
+
+
+def band_density(sys: System, kb: KBasis, psi: np.ndarray, weights: np.ndarray) -> np.ndarray:
+    """sum_b weights[b] |psi_b(r)|^2 / Omega with psi_b(r) = F^-1[c_b]."""
+    N = sys.nr
+    rho = np.zeros(N, dtype=np.float64)
+    box = np.zeros(N, dtype=np.complex128)
+    for b in range(psi.shape[0]):
+        if weights[b] == 0.0:
+            continue
+        box[:] = 0
+        box[kb.fidx] = psi[b]
+        r = fft3d(box, sys.n_fine, -1)
+        rho += weights[b] * (r.real ** 2 + r.imag ** 2)
+    return rho / sys.volume
+
+
+def hartree(sys: System, rho: np.ndarray):
+    """(V_H(r), E_H): V_H(G) = 4 pi n(G)/|G|^2 with G = 0 dropped,
+    n(G) = F[n]/N, E_H = Omega/2 sum_G 4 pi |n(G)|^2/|G|^2."""
+    g2 = gvec_sq_grid(sys.cell, sys.n_fine).ravel()
+    nG = fft3d(rho.astype(np.complex128), sys.n_fine, 1) / sys.nr
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kern = np.where(g2 > 0, FOUR_PI / np.where(g2 > 0, g2, 1.0), 0.0)
+    vG = kern * nG
+    eh = 0.5 * sys.volume * float(np.sum(kern * (nG.real ** 2 + nG.imag ** 2)))
+    vh = fft3d(vG, sys.n_fine, -1).real
+    return vh, eh
+
+
+def fermi_occupations(eigs: np.ndarray, wk: np.ndarray, nelec: float, kT: float, tol: float = 1e-14):
+    """Fermi-Dirac occupations f in [0,2] (spin-unpolarised) with the Fermi
+    level found by bisection so that sum_k w_k sum_n f_nk = Ne.
+    Returns (f, mu, entropy) where entropy S = -2 sum w f~ ln f~ + (1-f~) ln(1-f~),
+    f~ = f/2, so that the free energy is E - kT S."""
+    lo = float(eigs.min()) - 50.0 * kT - 1.0
+    hi = float(eigs.max()) + 50.0 * kT + 1.0
+
+    def count(mu):
+        x = np.clip((eigs - mu) / kT, -200.0, 200.0)
+        f = 2.0 / (1.0 + np.exp(x))
+        return float((wk[:, None] * f).sum())
+
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if count(mid) < nelec:
+            lo = mid
+        else:
+            hi = mid
+        if hi - lo < tol:
+            break
+    mu = 0.5 * (lo + hi)
+    x = np.clip((eigs - mu) / kT, -200.0, 200.0)
+    ft = 1.0 / (1.0 + np.exp(x))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = np.where((ft > 0) & (ft < 1), ft * np.log(ft) + (1 - ft) * np.log1p(-ft), 0.0)
+    entropy = -2.0 * float((wk[:, None] * s).sum())
+    return 2.0 * ft, mu, entropy
+
+
+class PulayMixer:
+    """Pulay (DIIS) density mixing with optional Kerker preconditioning.
+
+    Residual R = n_out - n_in.  Coefficients c minimise |sum c_i R_i|^2 (plain
+    r-space dot) subject to sum c_i = 1; the next input density is
+    sum c_i n_in_i + P[sum c_i R_i] with P = alpha (q0 = 0) or
+    alpha G^2/(G^2 + q0^2) applied in reciprocal space (Kerker).
+    """
+
+    def __init__(self, sys: System, alpha: float = 0.3, history: int = 8, q0: float = 0.0):
+        self.sys = sys
+        self.alpha = alpha
+        self.history = history
+        self.q0 = q0
+        self.nin: list = []
+        self.res: list = []
+        if q0 > 0:
+            g2 = gvec_sq_grid(sys.cell, sys.n_fine).ravel()
+            self.kerker = g2 / (g2 + q0 * q0)
+        else:
+            self.kerker = None
+
+    def precondition(self, r: np.ndarray) -> np.ndarray:
+        if self.kerker is None:
+            return self.alpha * r
+        rG = fft3d(r.astype(np.complex128), self.sys.n_fine, 1)
+        rG *= self.alpha * self.kerker
+        return fft3d(rG, self.sys.n_fine, -1).real / self.sys.nr
+
+    def mix(self, nin: np.ndarray, nout: np.ndarray) -> np.ndarray:
+        self.nin.append(nin.copy())
+        self.res.append(nout - nin)
+        if len(self.nin) > self.history:
+            self.nin.pop(0)
+            self.res.pop(0)
+        m = len(self.res)
+        A = np.empty((m + 1, m + 1))
+        for i in range(m):
+            for j in range(m):
+                A[i, j] = float(np.dot(self.res[i], self.res[j]))
+        A[m, :m] = 1.0
+        A[:m, m] = 1.0
+        A[m, m] = 0.0
+        rhs = np.zeros(m + 1)
+        rhs[m] = 1.0
+        c = np.linalg.lstsq(A, rhs, rcond=None)[0][:m]
+        n_opt = sum(ci * ni for ci, ni in zip(c, self.nin))
+        r_opt = sum(ci * ri for ci, ri in zip(c, self.res))
+        return n_opt + self.precondition(r_opt)
+
+
+@dataclass
+class ScfResult:
+    converged: bool
+    iterations: int
+    energy: float           # Kohn-Sham total energy of the output density
+    free_energy: float      # energy - kT * entropy
+    efermi: float
+    eigenvalues: np.ndarray  # (nk, nb)
+    occupations: np.ndarray  # (nk, nb)
+    density: np.ndarray      # output density of the last iteration, flat
+    history: list
+
+
+def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3,
+        history: int = 8, q0: float = 0.0, solver: str = "dense", verbose: bool = False) -> ScfResult:
+    """Self-consistent field loop (the intended electronic_scf,
+    Source/electronic.f90:86-175: iterate until |E - E_prev| < etol).
+
+    Each iteration diagonalises H[n_in] exactly ("dense", scipy eigh of the
+    Npw x Npw matrix), fills bands with Fermi-Dirac occupations, forms n_out,
+    evaluates the energies of n_out and mixes.  Start density: uniform Ne/Omega.
+    """
+    import scipy.linalg as sla
+
+    kbs = [KBasis(sys, ik) for ik in range(len(sys.kpts))]
+    omega = sys.volume
+    N = sys.nr
+    dv = omega / N
+    nin = np.full(N, sys.nelec / omega)
+    mixer = PulayMixer(sys, alpha=alpha, history=history, q0=q0)
+    e_prev = None
+    hist = []
+    result = None
+    for it in range(1, max_scf + 1):
+        vh, _ = hartree(sys, nin)
+        _, vxc = lda_exc_vxc(nin)
+        vhxc = vh + vxc
+        vloc = sys.vext + vhxc
+        eigs = np.zeros((len(kbs), sys.nbands))
+        vecs = []
+        for ik, kb in enumerate(kbs):
+            H = dense_h(sys, kb, vloc)
+            w, v = sla.eigh(H, subset_by_index=[0, sys.nbands - 1], driver="evr")
+            eigs[ik] = w
+            vecs.append(v.T.copy())
+        f, mu, ent = fermi_occupations(eigs, sys.wk, sys.nelec, sys.kT)
+        nout = np.zeros(N)
+        for ik, kb in enumerate(kbs):
+            nout += sys.wk[ik] * band_density(sys, kb, vecs[ik], f[ik])
+        eband = float((sys.wk[:, None] * f * eigs).sum())
+        _, eh = hartree(sys, nout)
+        exc_eps, _ = lda_exc_vxc(nout)
+        exc = dv * float(np.dot(nout, exc_eps))
+        e_dc = dv * float(np.dot(vhxc, nout))
+        energy = eband - e_dc + eh + exc
+        free = energy - sys.kT * ent
+        hist.append((it, energy, free, mu))
+        if verbose:
+            print(f"scf {it:3d} E={energy:.12f} F={free:.12f} mu={mu:.8f}")
+        result = ScfResult(False, it, energy, free, mu, eigs, f, nout, hist)
+        if e_prev is not None and abs(free - e_prev) < etol:
+            result.converged = True
+            break
+        e_prev = free
+        nin = mixer.mix(nin, nout)
+    return result

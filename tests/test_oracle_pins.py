@@ -1,0 +1,158 @@
+"""Pins the CPU oracle against the reference's own data and formulas.
+
+* LDA exchange/correlation against libxc 6.2.2's golden vectors (the only
+  golden data in the reference tree that fixes hot-path arithmetic).
+* FFT sign/normalisation against a direct DFT (Source/fft.f90:204-212).
+* Grid rule, G order and Monkhorst-Pack formula against hand-derived values of
+  Source/basis.f90:87-149,257-309 and Source/io.f90:2016-2031.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_lda_matches_libxc_golden(oracle):
+    with open(os.path.join(GOLDEN, "libxc_lda_unpol.json")) as f:
+        data = json.load(f)["systems"]
+    for name, d in data.items():
+        rho = np.array(d["rho"])
+        ex, vx, ec, vc = oracle.lda_x_c(rho)
+        for got, key in ((ex, "zk_x"), (vx, "vrho_x"), (ec, "zk_c"), (vc, "vrho_c")):
+            ref = np.array(d[key])
+            rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+            assert rel.max() < 5e-13, (name, key, rel.max())
+
+
+def test_lda_matches_compiled_libxc(oracle):
+    path = os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "libxc_lda.so")
+    if not os.path.exists(path):
+        pytest.skip("libxc checker not built (needs the reference tree)")
+    import ctypes
+    lib = ctypes.CDLL(path)
+    rng = np.random.default_rng(3)
+    rho = np.concatenate([10 ** rng.uniform(-14, 3, 4000), [0.0, 1e-15, 2e-15, 1e-16, -1.0]])
+    n = len(rho)
+    outs = [np.zeros(n) for _ in range(4)]
+    p = [a.ctypes.data_as(ctypes.c_void_p) for a in [rho] + outs]
+    assert lib.ref_lda_unpol(ctypes.c_long(n), *p) == 0
+    mine = oracle.lda_x_c(rho)
+    for a, b in zip(mine, outs):
+        assert np.allclose(a, b, rtol=1e-12, atol=1e-300)
+
+
+def test_fft_convention_direct_dft(oracle):
+    n = (4, 6, 5)
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal(np.prod(n)) + 1j * rng.standard_normal(np.prod(n))
+    idx = np.array(np.meshgrid(*[np.arange(m) for m in n], indexing="ij")).reshape(3, -1).T
+    ph = (idx[:, None, :] * idx[None, :, :] / np.array(n)).sum(-1)
+    fwd = np.exp(-2j * np.pi * ph) @ a
+    bwd = np.exp(2j * np.pi * ph) @ a
+    assert np.allclose(oracle.fft3d(a, n, 1), fwd, atol=1e-10)
+    assert np.allclose(oracle.fft3d(a, n, -1), bwd, atol=1e-10)
+    # a plane wave exp(i G0 r) transforms to N delta_{G,G0} (unnormalised)
+    g0 = (1, 2, 3)
+    pw = np.exp(2j * np.pi * (idx * np.array(g0) / np.array(n)).sum(1))
+    out = oracle.fft3d(pw, n, 1)
+    k = (g0[0] * n[1] + g0[1]) * n[2] + g0[2]
+    assert abs(out[k] - np.prod(n)) < 1e-9
+    assert np.abs(np.delete(out, k)).max() < 1e-9
+
+
+@pytest.mark.parametrize("L,ecut,std,ref_fine,s23_fine", [
+    (10.0, 10.0, 15, 30, 32),   # 8 electrons, Gamma
+    (16.0, 20.0, 33, 65, 72),   # 64 k-points
+    (12.0, 15.0, 21, 42, 48),   # adjoint workload
+])
+def test_grid_rules(oracle, L, ecut, std, ref_fine, s23_fine):
+    cell = np.eye(3) * L
+    ns, nf = oracle.grid_sizes(cell, ecut, 2.0, "reference")
+    assert ns == (std,) * 3 and nf == (ref_fine,) * 3
+    _, nf2 = oracle.grid_sizes(cell, ecut, 2.0, "smooth23")
+    assert nf2 == (s23_fine,) * 3
+
+
+def test_prime_fact_rule(oracle):
+    smooth = [n for n in range(1, 200) if oracle.prime_fact_round(n) == n]
+    for n in smooth:
+        m = n
+        for p in (2, 3, 5, 7, 11, 13):
+            while m % p == 0:
+                m //= p
+        assert m == 1
+    assert oracle.prime_fact_round(17) == 18
+    assert oracle.prime_fact_round(19) == 20
+    assert oracle.prime_fact_round(29) == 30
+    assert oracle.prime_fact_round(61) == 63
+    assert oracle.smooth23_round(65) == 72
+    assert oracle.smooth23_round(42) == 48
+
+
+def test_centred_box_order(oracle):
+    m = oracle.miller_box((3, 4, 2))
+    # x outermost, z innermost; range -n/2 .. n-n/2-1
+    assert m[0].tolist() == [-1, -2, -1]
+    assert m[1].tolist() == [-1, -2, 0]
+    assert m[2].tolist() == [-1, -1, -1]
+    assert m[-1].tolist() == [1, 1, 0]
+    assert len(m) == 24
+
+
+def test_mp_kpoints(oracle):
+    k = oracle.mp_kpoints((4, 4, 4))
+    assert len(k) == 64
+    assert np.allclose(sorted(set(np.round(k[:, 0], 12))), [-0.375, -0.125, 0.125, 0.375])
+    assert np.allclose(k[0], [-0.375, -0.375, -0.375]) and np.allclose(k[1], [-0.375, -0.375, -0.125])
+    assert np.allclose(oracle.mp_kpoints((1, 1, 1)), [[0, 0, 0]])
+    assert np.allclose(oracle.mp_kpoints((2, 2, 2))[0], [-0.25, -0.25, -0.25])
+
+
+def test_sphere_sizes(oracle):
+    cell = np.eye(3) * 10.0
+    ns, _ = oracle.grid_sizes(cell, 10.0)
+    rows, mil, kin = oracle.gsphere(cell, 10.0, [0, 0, 0], ns)
+    assert len(rows) == 1503
+    assert np.all(kin <= 10.0)
+    assert np.all(np.diff(rows) > 0)
+    cell = np.eye(3) * 16.0
+    ns, _ = oracle.grid_sizes(cell, 20.0)
+    sizes = {len(oracle.gsphere(cell, 20.0, k, ns)[0]) for k in oracle.mp_kpoints((4, 4, 4))}
+    assert min(sizes) >= 17470 and max(sizes) <= 17529
+
+
+def test_jellium_constant(oracle):
+    n = (8, 8, 8)
+    v = oracle.vext_jellium_wells(np.eye(3) * 5.0, n, 8.0, np.zeros((0, 5)))
+    assert np.allclose(v, 0.5 * 8.0 / 512)
+
+
+def test_free_electron_eigenvalues(oracle):
+    """V = 0: eigenvalues are 1/2|k+G|^2 exactly (analytic known answer)."""
+    s = oracle.make_system(6.0, 4.0, 2, 4, np.zeros((0, 5)), kpts=[[0.1, 0.2, -0.3]])
+    kb = oracle.KBasis(s, 0)
+    H = oracle.dense_h(s, kb, np.zeros(s.nr))
+    w = np.linalg.eigvalsh(H)
+    assert np.allclose(np.sort(w), np.sort(kb.kinetic), atol=1e-12)
+
+
+def test_cosine_potential_gap(oracle):
+    """V(x) = 2 V0 cos(2 pi x / L) separates: the lowest states (G_y = G_z = 0)
+    are those of the 1D Mathieu matrix 1/2 (k + m G)^2 + V0 (|dm| = 1), and
+    the first zone-boundary gap is 2|V0| to first order."""
+    L, v0 = 8.0, 0.05
+    s = oracle.make_system(L, 3.0, 2, 4, np.zeros((0, 5)), kpts=[[0.5, 0.0, 0.0]])
+    frac = np.arange(s.n_fine[0]) / s.n_fine[0]
+    vx = 2 * v0 * np.cos(2 * np.pi * frac)
+    v = np.broadcast_to(vx[:, None, None], s.n_fine).ravel().copy()
+    kb = oracle.KBasis(s, 0)
+    w = np.linalg.eigvalsh(oracle.dense_h(s, kb, v))
+    G = 2 * np.pi / L
+    m = np.array(sorted(kb.miller[(kb.miller[:, 1] == 0) & (kb.miller[:, 2] == 0), 0]))
+    H1 = np.diag(0.5 * ((0.5 + m) * G) ** 2) + v0 * (np.abs(m[:, None] - m[None, :]) == 1)
+    w1 = np.linalg.eigvalsh(H1)
+    assert np.allclose(w[:2], w1[:2], atol=1e-12)
+    assert abs((w[1] - w[0]) - 2 * v0) < 2e-3
