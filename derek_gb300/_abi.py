@@ -49,6 +49,7 @@ class ScfOpts(ctypes.Structure):
         ("precision", _i), ("mix_alpha", _d), ("kerker_q0", _d), ("pulay_history", _i),
         ("cheb_degree", _i), ("first_passes", _i), ("first_degree", _i),
         ("seed", ctypes.c_uint64), ("use_graph", _i), ("use_tensor_cores", _i),
+        ("density_tol", _d),
     ]
 
 
@@ -56,7 +57,7 @@ class ScfReport(ctypes.Structure):
     _fields_ = [
         ("energy", _d), ("free_energy", _d), ("delta", _d), ("efermi", _d), ("entropy", _d),
         ("e_band", _d), ("e_hartree", _d), ("e_xc", _d), ("e_dc", _d),
-        ("iterations", _i), ("converged", _i),
+        ("residual", _d), ("iterations", _i), ("converged", _i),
     ]
 
 

@@ -536,20 +536,20 @@ static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool
 int derek_gpu_set_wfn(derek_gpu_t *h, int s, int k, const double *psi) {
   int ki = ks_index(h, s, k);
   if (ki < 0 || !psi) return DEREK_ERR_BAD_ARG;
-  return copy_slice(h, ki, h->d_X, const_cast<double *>(psi), true);
+  return copy_slice(h, ki, h->cur_psi(), const_cast<double *>(psi), true);
 }
 
 int derek_gpu_get_wfn(derek_gpu_t *h, int s, int k, double *psi) {
   int ki = ks_index(h, s, k);
   if (ki < 0 || !psi) return DEREK_ERR_BAD_ARG;
-  return copy_slice(h, ki, h->d_X, psi, false);
+  return copy_slice(h, ki, h->cur_psi(), psi, false);
 }
 
 int derek_gpu_apply_h(derek_gpu_t *h, int s, int k, double *hpsi) {
   int ki = ks_index(h, s, k);
   if (ki < 0 || !hpsi) return DEREK_ERR_BAD_ARG;
   const KSetDev &K = h->ks[ki];
-  int st = apply_h_items(h, K.item0, K.nb, h->d_X, nullptr, h->d_HX, nullptr);
+  int st = apply_h_items(h, K.item0, K.nb, h->cur_psi(), nullptr, h->d_HX, nullptr);
   if (st) return st;
   return copy_slice(h, ki, h->d_HX, hpsi, false);
 }
@@ -570,7 +570,7 @@ int derek_gpu_density(derek_gpu_t *h, int s, const double *occ, double *rho) {
                                 cudaMemcpyHostToDevice, h->stream));
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_occw, w.data(), w.size() * sizeof(double),
                                 cudaMemcpyHostToDevice, h->stream));
-  int st = density_items(h, h->d_X, h->d_rho_out);
+  int st = density_items(h, h->cur_psi(), h->d_rho_out);
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
                                 cudaMemcpyHostToDevice, h->stream));
   if (st) return st;

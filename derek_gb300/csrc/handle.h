@@ -6,7 +6,7 @@
 #include <string>
 #include <vector>
 
-#include "kernels.cuh"
+#include "subspace.cuh"
 
 struct derek_gpu {
   // ---- configuration
@@ -62,8 +62,30 @@ struct derek_gpu {
   double *d_occ = nullptr;         // per item: f in [0, 2]
   derek::Axpby *d_coef = nullptr;  // per k-set filter coefficients
 
+  // ---- SCF state (scf.cu)
+  derek::SysState *d_state = nullptr;
+  double2 *d_S = nullptr, *d_Hs = nullptr, *d_C = nullptr, *d_scratch = nullptr;
+  double2 *d_opart = nullptr;                  // overlap split-K partials
+  long long *d_mat_off = nullptr, *d_opart_off = nullptr, *d_hist_off = nullptr;
+  int *d_status = nullptr, *d_sweeps = nullptr;
+  derek::Axpby *d_coef_all = nullptr;
+  int max_degree = 0;
+  double *d_nin_hist = nullptr, *d_res_hist = nullptr;
+  double *d_epart = nullptr, *d_gpart = nullptr;
+  int hist = 8;
+  int max_npw = 0;
+  long long max_nr = 0;
+  int cur = 0;                                 // psi buffer holding the current subspace
+  bool scf_started = false;
+  std::vector<long long> mat_off;
+  cudaGraphExec_t graph_exec[3] = {nullptr, nullptr, nullptr};  // keyed by starting buffer
+  int graph_degree = -1;
+
   cudaStream_t stream = nullptr;
   std::string last_error;
+
+  void *buf(int i) const { return i == 0 ? d_X : (i == 1 ? d_Y : d_Yp); }
+  void *cur_psi() const { return buf(cur); }
 
   size_t elem_size() const { return prec == DEREK_PREC_FP64 ? sizeof(double2) : sizeof(float2); }
 };

@@ -1,14 +1,367 @@
-// SCF driver (placeholder entry points until the subspace solver lands).
-#include "handle.h"
+// SCF driver: Chebyshev-filtered subspace iteration inside a self-consistent
+// density loop, batched over every k-point and every system of the handle.
+//
+// The reference's electronic_scf (Source/electronic.f90:86-175) loops until
+// |E - E_prev| < energy_tol but never builds a Hamiltonian.  One iteration
+// here is
+//   filter    Y = p_m(H) X             (m fused H.psi applications)
+//   CholQR    S = Y^H Y = L L^H, X = Y L^-H
+//   RR        Hs = X^H H X = U diag(e) U^H (Jacobi), X <- X U
+//   occupations (Fermi-Dirac), n_out(r), energies of n_out, |dF| test
+//   Pulay (+Kerker) mixing -> n_in, V_loc = V_ext + V_H[n_in] + v_xc[n_in]
+// with every scalar kept on the device, so a steady-state iteration is one
+// CUDA graph launch followed by a small state read-back.
+#include <algorithm>
+#include <cstring>
 
-extern "C" int derek_scf_alloc(derek_gpu_t *) { return DEREK_OK; }
-extern "C" void derek_scf_free(derek_gpu_t *) {}
+#include "handle.h"
+#include "scf_kernels.cuh"
+
+using namespace derek;
+
+namespace {
+
+template <typename T> cudaError_t dalloc(T **p, size_t n) {
+  return cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T));
+}
+
+// -- pieces of an iteration -------------------------------------------------
+int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int hermitize) {
+  if (h->prec == DEREK_PREC_FP64)
+    launch_overlap<double>(h->tab, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit,
+                           (const double2 *)A, (const double2 *)B, h->d_opart, h->d_opart_off, out,
+                           h->d_mat_off, hermitize, h->stream);
+  else
+    launch_overlap<float>(h->tab, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit,
+                          (const float2 *)A, (const float2 *)B, h->d_opart, h->d_opart_off, out,
+                          h->d_mat_off, hermitize, h->stream);
+  return DEREK_OK;
+}
+
+int rotate_all(derek_gpu *h, void *X, const double2 *C) {
+  if (h->prec == DEREK_PREC_FP64)
+    launch_rotate<double>(h->tab, 0, h->nks, h->max_nb, h->max_npw, (double2 *)X, C, h->d_mat_off,
+                          h->stream);
+  else
+    launch_rotate<float>(h->tab, 0, h->nks, h->max_nb, h->max_npw, (float2 *)X, C, h->d_mat_off,
+                         h->stream);
+  return DEREK_OK;
+}
+
+// orthonormalise buf(cur) and do Rayleigh-Ritz; leaves Ritz values in d_eig
+int cholqr_rr(derek_gpu *h) {
+  void *X = h->cur_psi();
+  overlap_all(h, X, X, h->d_S, 1);
+  launch_cholesky_inv(h->tab, 0, h->nks, h->max_nb, h->d_S, h->d_C, h->d_mat_off, h->d_scratch,
+                      h->d_status, h->stream);
+  rotate_all(h, X, h->d_C);
+  int st = apply_h_items(h, 0, h->nitems, X, nullptr, h->d_HX, nullptr);
+  if (st) return st;
+  overlap_all(h, X, h->d_HX, h->d_Hs, 1);
+  launch_jacobi(h->tab, 0, h->nks, h->max_nb, h->d_Hs, h->d_C, h->d_mat_off, h->d_eig,
+                h->d_scratch, 30, 1e-14, h->d_sweeps, h->stream);
+  rotate_all(h, X, h->d_C);
+  return DEREK_OK;
+}
+
+int filter(derek_gpu *h, int m) {
+  launch_filter_coef(h->tab, h->nks, h->d_eig, h->d_state, h->d_coef_all, m, h->stream);
+  int in = h->cur, prev = -1;
+  for (int i = 0; i < m; ++i) {
+    const int out = prev < 0 ? (in + 1) % 3 : 3 - in - prev;
+    int st = apply_h_items(h, 0, h->nitems, h->buf(in), prev < 0 ? nullptr : h->buf(prev),
+                           h->buf(out), h->d_coef_all + (size_t)i * h->nks);
+    if (st) return st;
+    prev = in;
+    in = out;
+  }
+  h->cur = in;
+  return DEREK_OK;
+}
+
+int subspace_step(derek_gpu *h, int m) {
+  int st = filter(h, m);
+  if (st) return st;
+  return cholqr_rr(h);
+}
+
+int finish_iteration(derek_gpu *h) {
+  launch_occupations(h->tab, h->nsys, h->d_eig, h->d_occ, h->d_occw, h->d_state, h->stream);
+  int st = density_items(h, h->cur_psi(), h->d_rho_out);
+  if (st) return st;
+  launch_density_fft(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_out, h->d_cgrid,
+                     h->stream);
+  launch_energies(h->tab, h->nsys, h->d_vhxc, h->d_rho_in, h->d_rho_out, h->d_cgrid, h->d_epart, h->d_state,
+                  h->d_sys, h->d_status, h->stream);
+  launch_mix(h->tab, h->nsys, (int)h->max_nr, h->d_rho_in, h->d_rho_out, h->d_nin_hist,
+             h->d_res_hist, h->d_hist_off, h->d_state, h->hist, h->d_gpart, h->d_cgrid,
+             h->opts.mix_alpha, h->opts.kerker_q0, h->max_nmax, h->stream);
+  launch_potential(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_in, h->d_cgrid,
+                   h->d_vext, h->d_vhxc, h->d_vloc, h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vloc32,
+                   h->d_epart, h->d_state, 0, h->stream);
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+int scf_start(derek_gpu *h, double etol) {
+  // reset state: all systems active, uniform start density, start vectors
+  for (auto &s : h->sys) s.active = 1;
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
+  std::vector<SysState> st(h->nsys);
+  for (auto &x : st) {
+    std::memset(&x, 0, sizeof(x));
+    x.slot = -1;
+    x.etol = etol;
+    x.rtol = h->opts.density_tol;
+    x.free = 0.0;
+  }
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_state, st.data(), st.size() * sizeof(SysState),
+                                cudaMemcpyHostToDevice, h->stream));
+  DEREK_CUDA(h, cudaMemsetAsync(h->d_status, 0, h->nks * sizeof(int), h->stream));
+  launch_uniform_density(h->tab, h->nsys, (int)h->max_nr, h->d_rho_in, h->stream);
+  launch_potential(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_in, h->d_cgrid,
+                   h->d_vext, h->d_vhxc, h->d_vloc, h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vloc32,
+                   h->d_epart, h->d_state, 1, h->stream);
+  h->cur = 0;
+  if (h->prec == DEREK_PREC_FP64)
+    launch_init_psi<double>(h->tab, h->nitems, h->d_X, h->opts.seed, h->stream);
+  else
+    launch_init_psi<float>(h->tab, h->nitems, h->d_X, h->opts.seed, h->stream);
+  DEREK_CUDA(h, cudaGetLastError());
+  int s = cholqr_rr(h);
+  if (s) return s;
+  for (int p = 0; p < h->opts.first_passes; ++p) {
+    s = subspace_step(h, h->opts.first_degree);
+    if (s) return s;
+  }
+  h->scf_started = true;
+  return DEREK_OK;
+}
+
+int steady_iteration(derek_gpu *h) {
+  const int m = h->opts.cheb_degree;
+  if (!h->opts.use_graph) {
+    int s = subspace_step(h, m);
+    if (s) return s;
+    return finish_iteration(h);
+  }
+  if (h->graph_degree != m) {
+    for (auto &g : h->graph_exec)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    h->graph_degree = m;
+  }
+  const int start = h->cur;
+  if (!h->graph_exec[start]) {
+    cudaGraph_t g = nullptr;
+    DEREK_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int s = subspace_step(h, m);
+    if (!s) s = finish_iteration(h);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (s) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+    }
+    if (e != cudaSuccess) return cuda_status(e, h, "graph capture");
+    e = cudaGraphInstantiate(&h->graph_exec[start], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_status(e, h, "graph instantiate");
+  }
+  DEREK_CUDA(h, cudaGraphLaunch(h->graph_exec[start], h->stream));
+  h->cur = (start + m) % 3;
+  return DEREK_OK;
+}
+
+void fill_reports(derek_gpu *h, const std::vector<SysState> &st, derek_scf_report *rep) {
+  if (!rep) return;
+  for (int s = 0; s < h->nsys; ++s) {
+    const SysState &x = st[s];
+    derek_scf_report &r = rep[s];
+    r.energy = x.energy;
+    r.free_energy = x.free;
+    r.delta = x.delta;
+    r.efermi = x.mu;
+    r.entropy = x.entropy;
+    r.e_band = x.e_band;
+    r.e_hartree = x.e_h;
+    r.e_xc = x.e_xc;
+    r.e_dc = x.e_dc;
+    r.residual = x.resid;
+    r.iterations = x.iter;
+    r.converged = x.converged;
+  }
+}
+
+int read_state(derek_gpu *h, std::vector<SysState> &st) {
+  st.resize(h->nsys);
+  DEREK_CUDA(h, cudaMemcpyAsync(st.data(), h->d_state, st.size() * sizeof(SysState),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int one_iteration(derek_gpu *h, double etol) {
+  int s;
+  if (!h->scf_started) {
+    s = scf_start(h, etol);
+    if (s) return s;
+    s = finish_iteration(h);
+  } else {
+    s = steady_iteration(h);
+  }
+  return s;
+}
+
+}  // namespace
+
+extern "C" int derek_scf_alloc(derek_gpu_t *h) {
+  h->hist = std::max(1, std::min(h->opts.pulay_history, kMaxHist));
+  h->max_degree = std::max({h->opts.cheb_degree, h->opts.first_degree, 1});
+  if (h->max_nb > kMaxBands) {
+    h->last_error = "more than 128 bands per k-point";
+    return DEREK_ERR_UNSUPPORTED;
+  }
+  long long moff = 0, poff = 0;
+  std::vector<long long> opart_off;
+  for (const auto &K : h->ks) {
+    h->mat_off.push_back(moff);
+    moff += (long long)K.nb * K.nb;
+    opart_off.push_back(poff);
+    poff += (long long)((K.npw + kOverlapSplit - 1) / kOverlapSplit) * K.nb * K.nb;
+    h->max_npw = std::max(h->max_npw, K.npw);
+  }
+  std::vector<long long> hist_off;
+  long long hoff = 0;
+  for (const auto &S : h->sys) {
+    hist_off.push_back(hoff);
+    hoff += (long long)h->hist * S.nr;
+    h->max_nr = std::max<long long>(h->max_nr, S.nr);
+  }
+  cudaError_t e;
+#define A(call)                                                  \
+  if ((e = (call)) != cudaSuccess) return cuda_status(e, h, #call);
+  A(dalloc(&h->d_state, h->nsys));
+  A(dalloc(&h->d_S, moff));
+  A(dalloc(&h->d_Hs, moff));
+  A(dalloc(&h->d_C, moff));
+  A(dalloc(&h->d_scratch, 2 * moff));
+  A(dalloc(&h->d_opart, poff));
+  A(dalloc(&h->d_mat_off, h->mat_off.size()));
+  A(dalloc(&h->d_opart_off, opart_off.size()));
+  A(dalloc(&h->d_hist_off, hist_off.size()));
+  A(dalloc(&h->d_status, h->nks));
+  A(dalloc(&h->d_sweeps, h->nks));
+  A(dalloc(&h->d_coef_all, (size_t)h->max_degree * h->nks));
+  A(dalloc(&h->d_nin_hist, hoff));
+  A(dalloc(&h->d_res_hist, hoff));
+  A(dalloc(&h->d_epart, (size_t)h->nsys * 64 * 8));
+  A(dalloc(&h->d_gpart, (size_t)h->nsys * 64 * kMaxHist));
+  A(cudaMemcpy(h->d_mat_off, h->mat_off.data(), h->mat_off.size() * sizeof(long long),
+               cudaMemcpyHostToDevice));
+  A(cudaMemcpy(h->d_opart_off, opart_off.data(), opart_off.size() * sizeof(long long),
+               cudaMemcpyHostToDevice));
+  A(cudaMemcpy(h->d_hist_off, hist_off.data(), hist_off.size() * sizeof(long long),
+               cudaMemcpyHostToDevice));
+  A(cudaMemset(h->d_status, 0, h->nks * sizeof(int)));
+  A(cudaMemset(h->d_state, 0, h->nsys * sizeof(SysState)));
+#undef A
+  return DEREK_OK;
+}
+
+extern "C" void derek_scf_free(derek_gpu_t *h) {
+  for (auto &g : h->graph_exec)
+    if (g) cudaGraphExecDestroy(g);
+  void *ptrs[] = {h->d_state,  h->d_S,      h->d_Hs,       h->d_C,        h->d_scratch,
+                  h->d_opart,  h->d_mat_off, h->d_opart_off, h->d_hist_off, h->d_status,
+                  h->d_sweeps, h->d_coef_all, h->d_nin_hist, h->d_res_hist, h->d_epart,
+                  h->d_gpart};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+}
 
 extern "C" {
-int derek_gpu_overlap(derek_gpu_t *, int, int, double *) { return DEREK_ERR_UNSUPPORTED; }
-int derek_gpu_scf_iterate(derek_gpu_t *, derek_scf_report *) { return DEREK_ERR_UNSUPPORTED; }
-int derek_gpu_scf_run(derek_gpu_t *, int, double, derek_scf_report *) { return DEREK_ERR_UNSUPPORTED; }
-int derek_gpu_get_eigenvalues(derek_gpu_t *, int, double *) { return DEREK_ERR_UNSUPPORTED; }
-int derek_gpu_get_occupations(derek_gpu_t *, int, double *) { return DEREK_ERR_UNSUPPORTED; }
-int derek_gpu_get_density(derek_gpu_t *, int, double *) { return DEREK_ERR_UNSUPPORTED; }
+
+int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
+  if (!h || s < 0 || s >= h->nsys || k < 0 || k >= h->sys[s].nk || !out) return DEREK_ERR_BAD_ARG;
+  const int ki = h->sys[s].ks0 + k;
+  const KSetDev &K = h->ks[ki];
+  if (h->prec == DEREK_PREC_FP64)
+    launch_overlap<double>(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const double2 *)h->cur_psi(),
+                           (const double2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S,
+                           h->d_mat_off, 0, h->stream);
+  else
+    launch_overlap<float>(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const float2 *)h->cur_psi(),
+                          (const float2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S,
+                          h->d_mat_off, 0, h->stream);
+  DEREK_CUDA(h, cudaGetLastError());
+  DEREK_CUDA(h, cudaMemcpyAsync(out, h->d_S + h->mat_off[ki], (size_t)K.nb * K.nb * sizeof(double2),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
 }
+
+int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
+  if (!h) return DEREK_ERR_BAD_ARG;
+  int s = one_iteration(h, 0.0);
+  if (s) return s;
+  std::vector<SysState> st;
+  s = read_state(h, st);
+  if (s) return s;
+  fill_reports(h, st, rep);
+  for (const auto &x : st)
+    if (x.status) return x.status;
+  return DEREK_OK;
+}
+
+int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol, derek_scf_report *rep) {
+  if (!h || max_scf <= 0 || !(etol > 0)) return DEREK_ERR_BAD_ARG;
+  h->scf_started = false;
+  std::vector<SysState> st;
+  for (int it = 0; it < max_scf; ++it) {
+    int s = one_iteration(h, etol);
+    if (s) return s;
+    s = read_state(h, st);
+    if (s) return s;
+    bool all_done = true;
+    for (const auto &x : st) {
+      if (x.status) {
+        fill_reports(h, st, rep);
+        h->last_error = derek_gpu_strerror(x.status);
+        return x.status;
+      }
+      all_done &= x.converged != 0;
+    }
+    if (all_done) break;
+  }
+  fill_reports(h, st, rep);
+  for (const auto &x : st)
+    if (!x.converged) return DEREK_ERR_NOT_CONVERGED;
+  return DEREK_OK;
+}
+
+static int get_items(derek_gpu_t *h, int s, const double *src, double *out) {
+  if (!h || s < 0 || s >= h->nsys || !out) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  const KSetDev &K0 = h->ks[S.ks0];
+  DEREK_CUDA(h, cudaMemcpyAsync(out, src + K0.item0, (size_t)S.nk * S.nb * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int derek_gpu_get_eigenvalues(derek_gpu_t *h, int s, double *e) { return get_items(h, s, h ? h->d_eig : nullptr, e); }
+int derek_gpu_get_occupations(derek_gpu_t *h, int s, double *o) { return get_items(h, s, h ? h->d_occ : nullptr, o); }
+
+int derek_gpu_get_density(derek_gpu_t *h, int s, double *rho) {
+  if (!h || s < 0 || s >= h->nsys || !rho) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  DEREK_CUDA(h, cudaMemcpyAsync(rho, h->d_rho_out + S.grid_off, (size_t)S.nr * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,601 @@
+// Grid-level kernels of the SCF iteration: start vectors, Chebyshev filter
+// coefficients, Fermi-Dirac occupations, energies, Pulay/Kerker mixing and
+// the local potential V_ext + V_H + v_xc.  Every kernel is deterministic:
+// reductions use a fixed block count per system and a fixed summation order.
+//
+// The reference's SCF loop (Source/electronic.f90:86-175) is a stub; the
+// formulas here are textbook plane-wave Kohn-Sham DFT in Hartree units:
+//   f = 2 / (1 + exp((e - mu)/kT)),  sum_k w_k sum_n f_nk = N_e
+//   S = -2 sum_k w_k sum_n [f~ ln f~ + (1-f~) ln(1-f~)],  f~ = f/2
+//   n(G) = F[n]/N,  V_H(G) = 4 pi n(G)/|G|^2 (G = 0 dropped),
+//   E_H = Omega/2 sum_G 4 pi |n(G)|^2/|G|^2
+//   E = E_band - int V_Hxc[n_in] n_out + E_H[n_out] + E_xc[n_out],  F = E - kT S
+#include "scf_kernels.cuh"
+#include "xc.cuh"
+
+namespace derek {
+
+constexpr int RB = 64;  // reduction blocks per system
+constexpr int EP = 8;   // partial slots per block: 0-2 energies, 3 residual, 4 V max
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double gsq(const SysDev &S, long long r) {
+  const int n1 = S.n[0], n2 = S.n[1], n3 = S.n[2];
+  const int iz = (int)(r % n3);
+  const int iy = (int)((r / n3) % n2);
+  const int ix = (int)(r / ((long long)n2 * n3));
+  const double m0 = ix < n1 - n1 / 2 ? ix : ix - n1;
+  const double m1 = iy < n2 - n2 / 2 ? iy : iy - n2;
+  const double m2 = iz < n3 - n3 / 2 ? iz : iz - n3;
+  double g2 = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    const double g = S.B[3 * i] * m0 + S.B[3 * i + 1] * m1 + S.B[3 * i + 2] * m2;
+    g2 += g * g;
+  }
+  return g2;
+}
+
+// ---- start vectors: real r - 0.5 per (band, G) like wave_initialise_wfn
+// (Source/wave.f90:873-886), from a splitmix64 counter hash
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ULL;
+  unsigned long long z = x;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+template <typename R>
+__global__ void k_init_psi(const Tables t, cplx<R> *__restrict__ X, unsigned long long seed) {
+  const int item = blockIdx.x;
+  const int ksi = t.item_ks[item];
+  const KSetDev &K = t.ks[ksi];
+  const int b = t.item_band[item];
+  const unsigned long long key = (seed * 0x100000001B3ULL) ^ ((unsigned long long)K.sys << 40) ^
+                                 ((unsigned long long)K.kidx << 24);
+  cplx<R> *dst = X + K.psi_off + (long long)b * K.npw_pad;
+  for (int g = threadIdx.x; g < K.npw_pad; g += blockDim.x) {
+    R v = 0;
+    if (g < K.npw) {
+      const unsigned long long h = splitmix64(key + (unsigned long long)b * (1ULL << 20) + g);
+      v = (R)((double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5);
+    }
+    dst[g] = mk<R>(v, 0);
+  }
+}
+
+// ---- Chebyshev filter coefficients (scaled filter of Zhou, Saad, Tiago and
+// Chelikowsky, J. Comput. Phys. 219 (2006) 172): damp [a, b], scale at a0.
+__global__ void k_filter_coef(const Tables t, int nks, const double *__restrict__ eig,
+                              const SysState *__restrict__ st, Axpby *__restrict__ coef, int m) {
+  const int ksi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ksi >= nks) return;
+  const KSetDev &K = t.ks[ksi];
+  const SysDev &S = t.sys[K.sys];
+  double a0 = eig[K.item0];
+  double a = eig[K.item0 + K.nb - 1];
+  const double b = S.ecut + st[K.sys].vmax + 0.01 * fabs(S.ecut);
+  if (!(a < b)) a = b - 0.1 * fabs(b - a0) - 1e-3;
+  if (!(a0 < a)) a0 = a - 1e-3;
+  const double e = 0.5 * (b - a), c = 0.5 * (b + a);
+  const double sigma1 = e / (a0 - c);
+  double sigma = sigma1;
+  coef[ksi] = Axpby{sigma1 / e, -c * sigma1 / e, 0.0};
+  for (int i = 1; i < m; ++i) {
+    const double sn = 1.0 / (2.0 / sigma1 - sigma);
+    const double al = 2.0 * sn / e;
+    coef[(long long)i * nks + ksi] = Axpby{al, -c * al, -sigma * sn};
+    sigma = sn;
+  }
+}
+
+// ---- Fermi-Dirac occupations, one block per system
+__global__ void __launch_bounds__(1024) k_occupations(const Tables t, const double *__restrict__ eig,
+                                                      double *__restrict__ occ,
+                                                      double *__restrict__ occw,
+                                                      SysState *__restrict__ st) {
+  __shared__ double red[1024];
+  __shared__ double s_lo, s_hi, s_mu;
+  __shared__ int s_done;
+  const int s = blockIdx.x;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const int nb = S.nb, nk = S.nk;
+  const int ntot = nb * nk;
+  const double kT = S.kT, ne = S.nelec;
+  // bracket
+  double lo = 1e300, hi = -1e300;
+  for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
+    const KSetDev &K = t.ks[S.ks0 + i / nb];
+    const double e = eig[K.item0 + i % nb];
+    lo = fmin(lo, e);
+    hi = fmax(hi, e);
+  }
+  red[threadIdx.x] = lo;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmin(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) s_lo = red[0] - 40.0 * kT - 1.0;
+  __syncthreads();
+  red[threadIdx.x] = hi;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    s_hi = red[0] + 40.0 * kT + 1.0;
+    s_mu = 0.5 * (s_lo + s_hi);
+    s_done = 0;
+  }
+  __syncthreads();
+  // safeguarded Newton on N(mu) - Ne
+  for (int it = 0; it < 200; ++it) {
+    const double mu = s_mu;
+    double cnt = 0, der = 0;
+    for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
+      const KSetDev &K = t.ks[S.ks0 + i / nb];
+      const double x = fmin(fmax((eig[K.item0 + i % nb] - mu) / kT, -200.0), 200.0);
+      const double f = 1.0 / (1.0 + exp(x));
+      cnt += K.wk * 2.0 * f;
+      der += K.wk * 2.0 * f * (1.0 - f) / kT;
+    }
+    cnt = block_sum(cnt, red);
+    der = block_sum(der, red);
+    if (threadIdx.x == 0) {
+      const double r = cnt - ne;
+      if (r < 0)
+        s_lo = mu;
+      else
+        s_hi = mu;
+      double nmu = der > 0 ? mu - r / der : 0.5 * (s_lo + s_hi);
+      if (!(nmu > s_lo && nmu < s_hi)) nmu = 0.5 * (s_lo + s_hi);
+      if (fabs(r) <= 1e-14 * ne || (s_hi - s_lo) <= 1e-15 * fmax(1.0, fabs(mu))) s_done = 1;
+      s_mu = s_done ? mu : nmu;
+    }
+    __syncthreads();
+    if (s_done) break;
+  }
+  const double mu = s_mu;
+  double ent = 0, eb = 0;
+  for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
+    const KSetDev &K = t.ks[S.ks0 + i / nb];
+    const int item = K.item0 + i % nb;
+    const double e = eig[item];
+    const double x = fmin(fmax((e - mu) / kT, -200.0), 200.0);
+    const double f = 1.0 / (1.0 + exp(x));
+    occ[item] = 2.0 * f;
+    occw[item] = K.wk * 2.0 * f / S.volume;
+    if (f > 0.0 && f < 1.0) ent += K.wk * (f * log(f) + (1.0 - f) * log1p(-f));
+    eb += K.wk * 2.0 * f * e;
+  }
+  ent = block_sum(ent, red);
+  eb = block_sum(eb, red);
+  if (threadIdx.x == 0) {
+    st[s].mu = mu;
+    st[s].entropy = -2.0 * ent;
+    st[s].e_band = eb;
+  }
+}
+
+// ---- energies of the output density.  cgrid holds F[n_out] (unnormalised).
+__global__ void __launch_bounds__(256) k_energy_partials(const Tables t, const double *__restrict__ vhxc,
+                                                         const double *__restrict__ rho_in,
+                                                         const double *__restrict__ rho_out,
+                                                         const double2 *__restrict__ cgrid,
+                                                         double *__restrict__ part) {
+  __shared__ double red[256];
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const long long n = S.nr;
+  const long long chunk = (n + RB - 1) / RB;
+  const long long r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+  double q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+  for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const double nr = rho_out[S.grid_off + r];
+    q3 = fmax(q3, fabs(nr - rho_in[S.grid_off + r]));
+    q0 += vhxc[S.grid_off + r] * nr;
+    double e, v;
+    lda_point(nr, e, v);
+    q1 += nr * e;
+    const double g2 = gsq(S, r);
+    if (g2 > 0) {
+      const double2 c = cgrid[S.grid_off + r];
+      q2 += (c.x * c.x + c.y * c.y) / g2;
+    }
+  }
+  q0 = block_sum(q0, red);
+  q1 = block_sum(q1, red);
+  q2 = block_sum(q2, red);
+  red[threadIdx.x] = q3;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double *p = part + ((long long)s * RB + blockIdx.x) * EP;
+    p[0] = q0;
+    p[1] = q1;
+    p[2] = q2;
+    p[3] = red[0];
+  }
+}
+
+__global__ void k_energy_final(const Tables t, int nsys, const double *__restrict__ part,
+                               SysState *__restrict__ st, SysDev *__restrict__ sys_rw,
+                               const int *__restrict__ ks_status) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  double q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+  for (int b = 0; b < RB; ++b) {
+    const double *p = part + ((long long)s * RB + b) * EP;
+    q0 += p[0];
+    q1 += p[1];
+    q2 += p[2];
+    q3 = fmax(q3, p[3]);
+  }
+  const double dv = S.volume / S.nr;
+  const double four_pi = 12.566370614359172953850573533118;
+  SysState &X = st[s];
+  X.resid = q3;
+  X.e_dc = dv * q0;
+  X.e_xc = dv * q1;
+  X.e_h = 0.5 * S.volume * four_pi * q2 / ((double)S.nr * (double)S.nr);
+  X.energy = X.e_band - X.e_dc + X.e_h + X.e_xc;
+  const double F = X.energy - S.kT * X.entropy;
+  X.iter += 1;
+  X.delta = X.iter > 1 ? fabs(F - X.free) : 1e300;
+  X.free_prev = X.free;
+  X.free = F;
+  int status = 0;
+  for (int k = 0; k < S.nk; ++k)
+    if (ks_status[S.ks0 + k]) status = ks_status[S.ks0 + k];
+  if (!(F == F)) status = DEREK_ERR_NAN;
+  X.status = status;
+  if (X.iter > 1 && X.delta < X.etol && (X.rtol <= 0.0 || X.resid < X.rtol)) X.converged = 1;
+  if (X.converged || status) sys_rw[s].active = 0;
+}
+
+// ---- Pulay mixing with optional Kerker preconditioning
+__global__ void __launch_bounds__(256) k_mix_store(const Tables t, const double *__restrict__ rho_in,
+                                                   const double *__restrict__ rho_out,
+                                                   double *__restrict__ nin_hist,
+                                                   double *__restrict__ res_hist,
+                                                   const long long *__restrict__ hist_off,
+                                                   const SysState *__restrict__ st, int H) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const int slot = (st[s].slot + 1) % H;
+  double *ni = nin_hist + hist_off[s] + (long long)slot * S.nr;
+  double *re = res_hist + hist_off[s] + (long long)slot * S.nr;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < S.nr;
+       r += (long long)gridDim.x * blockDim.x) {
+    const double a = rho_in[S.grid_off + r];
+    ni[r] = a;
+    re[r] = rho_out[S.grid_off + r] - a;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mix_gram_partials(const Tables t, const double *__restrict__ res_hist,
+                                                           const long long *__restrict__ hist_off,
+                                                           const SysState *__restrict__ st, int H,
+                                                           double *__restrict__ part) {
+  __shared__ double red[256];
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const int slot = (st[s].slot + 1) % H;
+  const int m = min(st[s].nhist + 1, H);
+  const long long n = S.nr;
+  const long long chunk = (n + RB - 1) / RB;
+  const long long r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+  const double *rs = res_hist + hist_off[s] + (long long)slot * n;
+  for (int j = 0; j < m; ++j) {
+    const double *rj = res_hist + hist_off[s] + (long long)j * n;
+    double q = 0;
+    for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) q += rs[r] * rj[r];
+    q = block_sum(q, red);
+    if (threadIdx.x == 0) part[((long long)s * RB + blockIdx.x) * kMaxHist + j] = q;
+  }
+}
+
+__global__ void k_mix_solve(const Tables t, int nsys, const double *__restrict__ part,
+                            SysState *__restrict__ st, int H) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  SysState &X = st[s];
+  const int slot = (X.slot + 1) % H;
+  const int m = min(X.nhist + 1, H);
+  for (int j = 0; j < m; ++j) {
+    double q = 0;
+    for (int b = 0; b < RB; ++b) q += part[((long long)s * RB + b) * kMaxHist + j];
+    X.gram[slot * kMaxHist + j] = q;
+    X.gram[j * kMaxHist + slot] = q;
+  }
+  X.slot = slot;
+  X.nhist = m;
+  // [G 1; 1^T 0] [c; lambda] = [0; 1], G scaled by its largest diagonal
+  double A[(kMaxHist + 1) * (kMaxHist + 1)];
+  double rhs[kMaxHist + 1];
+  const int N = m + 1;
+  double gmax = 0;
+  for (int j = 0; j < m; ++j) gmax = fmax(gmax, X.gram[j * kMaxHist + j]);
+  if (!(gmax > 0)) gmax = 1;
+  for (int i = 0; i < m; ++i) {
+    for (int j = 0; j < m; ++j) A[i * N + j] = X.gram[i * kMaxHist + j] / gmax;
+    A[i * N + m] = 1.0;
+    A[m * N + i] = 1.0;
+    rhs[i] = 0.0;
+  }
+  A[m * N + m] = 0.0;
+  rhs[m] = 1.0;
+  bool ok = true;
+  for (int c = 0; c < N && ok; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < N; ++r)
+      if (fabs(A[r * N + c]) > fabs(A[piv * N + c])) piv = r;
+    if (!(fabs(A[piv * N + c]) > 1e-14)) {
+      ok = false;
+      break;
+    }
+    if (piv != c) {
+      for (int j = 0; j < N; ++j) {
+        const double tmp = A[c * N + j];
+        A[c * N + j] = A[piv * N + j];
+        A[piv * N + j] = tmp;
+      }
+      const double tmp = rhs[c];
+      rhs[c] = rhs[piv];
+      rhs[piv] = tmp;
+    }
+    for (int r = c + 1; r < N; ++r) {
+      const double f = A[r * N + c] / A[c * N + c];
+      for (int j = c; j < N; ++j) A[r * N + j] -= f * A[c * N + j];
+      rhs[r] -= f * rhs[c];
+    }
+  }
+  double x[kMaxHist + 1];
+  if (ok) {
+    for (int r = N - 1; r >= 0; --r) {
+      double v = rhs[r];
+      for (int j = r + 1; j < N; ++j) v -= A[r * N + j] * x[j];
+      x[r] = v / A[r * N + r];
+    }
+  }
+  for (int j = 0; j < kMaxHist; ++j) X.coef[j] = 0.0;
+  if (ok) {
+    for (int j = 0; j < m; ++j) X.coef[j] = x[j];
+  } else {
+    X.coef[slot] = 1.0;
+  }
+}
+
+// rho_in <- sum c_j nin_j + (kerker ? 0 : alpha sum c_j R_j); cgrid <- sum c_j R_j
+__global__ void __launch_bounds__(256) k_mix_combine(const Tables t, double *__restrict__ rho_in,
+                                                     const double *__restrict__ nin_hist,
+                                                     const double *__restrict__ res_hist,
+                                                     const long long *__restrict__ hist_off,
+                                                     const SysState *__restrict__ st,
+                                                     double2 *__restrict__ cgrid, double alpha,
+                                                     int kerker) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const int m = st[s].nhist;
+  double c[kMaxHist];
+  for (int j = 0; j < kMaxHist; ++j) c[j] = j < m ? st[s].coef[j] : 0.0;
+  const long long n = S.nr;
+  const double *ni = nin_hist + hist_off[s];
+  const double *re = res_hist + hist_off[s];
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
+       r += (long long)gridDim.x * blockDim.x) {
+    double a = 0, b = 0;
+    for (int j = 0; j < m; ++j) {
+      a += c[j] * ni[(long long)j * n + r];
+      b += c[j] * re[(long long)j * n + r];
+    }
+    if (kerker) {
+      rho_in[S.grid_off + r] = a;
+      cgrid[S.grid_off + r] = make_double2(b, 0.0);
+    } else {
+      rho_in[S.grid_off + r] = a + alpha * b;
+    }
+  }
+}
+
+// cgrid <- alpha G^2/(G^2 + q0^2) cgrid / N (the /N undoes the unnormalised pair)
+__global__ void __launch_bounds__(256) k_kerker_scale(const Tables t, double2 *__restrict__ cgrid,
+                                                      double alpha, double q0) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const double invn = 1.0 / S.nr;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < S.nr;
+       r += (long long)gridDim.x * blockDim.x) {
+    const double g2 = gsq(S, r);
+    const double f = alpha * g2 / (g2 + q0 * q0) * invn;
+    double2 &c = cgrid[S.grid_off + r];
+    c.x *= f;
+    c.y *= f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_add_real(const Tables t, double *__restrict__ rho,
+                                                  const double2 *__restrict__ cgrid) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < S.nr;
+       r += (long long)gridDim.x * blockDim.x)
+    rho[S.grid_off + r] += cgrid[S.grid_off + r].x;
+}
+
+// ---- potential
+__global__ void __launch_bounds__(256) k_real_to_complex(const Tables t, const double *__restrict__ a,
+                                                         double2 *__restrict__ c, int all) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!all && !S.active) return;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < S.nr;
+       r += (long long)gridDim.x * blockDim.x)
+    c[S.grid_off + r] = make_double2(a[S.grid_off + r], 0.0);
+}
+
+__global__ void __launch_bounds__(256) k_hartree_scale(const Tables t, double2 *__restrict__ c, int all) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!all && !S.active) return;
+  const double four_pi = 12.566370614359172953850573533118;
+  const double invn = 1.0 / S.nr;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < S.nr;
+       r += (long long)gridDim.x * blockDim.x) {
+    const double g2 = gsq(S, r);
+    const double f = g2 > 0 ? four_pi / g2 * invn : 0.0;
+    double2 &v = c[S.grid_off + r];
+    v.x *= f;
+    v.y *= f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_build_vloc(const Tables t, const double *__restrict__ rho_in,
+                                                    const double2 *__restrict__ vh,
+                                                    const double *__restrict__ vext,
+                                                    double *__restrict__ vhxc,
+                                                    double *__restrict__ vloc,
+                                                    float *__restrict__ vloc32,
+                                                    double *__restrict__ part, int all) {
+  __shared__ double red[256];
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!all && !S.active) return;
+  const long long n = S.nr;
+  const long long chunk = (n + RB - 1) / RB;
+  const long long r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+  double vm = -1e300;
+  for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const long long i = S.grid_off + r;
+    double e, v;
+    lda_point(rho_in[i], e, v);
+    const double hx = vh[i].x + v;
+    vhxc[i] = hx;
+    const double vl = vext[i] + hx;
+    vloc[i] = vl;
+    if (vloc32) vloc32[i] = (float)vl;
+    vm = fmax(vm, vl);
+  }
+  red[threadIdx.x] = vm;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[((long long)s * RB + blockIdx.x) * EP + 4] = red[0];
+}
+
+__global__ void k_vmax_final(const Tables t, int nsys, const double *__restrict__ part,
+                             SysState *__restrict__ st, int all) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  if (!all && !t.sys[s].active) return;
+  double vm = -1e300;
+  for (int b = 0; b < RB; ++b) vm = fmax(vm, part[((long long)s * RB + b) * EP + 4]);
+  st[s].vmax = vm;
+}
+
+__global__ void __launch_bounds__(256) k_uniform_density(const Tables t, double *__restrict__ rho) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  const double v = S.nelec / S.volume;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < S.nr;
+       r += (long long)gridDim.x * blockDim.x)
+    rho[S.grid_off + r] = v;
+}
+
+// ---------------------------------------------------------------------------
+template <typename R>
+void launch_init_psi(const Tables &t, int nitems, void *X, unsigned long long seed, cudaStream_t st) {
+  k_init_psi<R><<<nitems, 256, 0, st>>>(t, (cplx<R> *)X, seed);
+}
+template void launch_init_psi<float>(const Tables &, int, void *, unsigned long long, cudaStream_t);
+template void launch_init_psi<double>(const Tables &, int, void *, unsigned long long, cudaStream_t);
+
+void launch_filter_coef(const Tables &t, int nks, const double *eig, const SysState *st, Axpby *coef,
+                        int m, cudaStream_t s) {
+  k_filter_coef<<<(nks + 127) / 128, 128, 0, s>>>(t, nks, eig, st, coef, m);
+}
+
+void launch_occupations(const Tables &t, int nsys, const double *eig, double *occ, double *occw,
+                        SysState *st, cudaStream_t s) {
+  k_occupations<<<nsys, 1024, 0, s>>>(t, eig, occ, occw, st);
+}
+
+void launch_energies(const Tables &t, int nsys, const double *vhxc, const double *rho_in,
+                     const double *rho_out, const double2 *cgrid, double *part, SysState *st,
+                     SysDev *sys_rw, const int *ks_status, cudaStream_t s) {
+  k_energy_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, vhxc, rho_in, rho_out, cgrid, part);
+  k_energy_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, sys_rw, ks_status);
+}
+
+void launch_mix(const Tables &t, int nsys, int max_nr, double *rho_in, const double *rho_out,
+                double *nin_hist, double *res_hist, const long long *hist_off, SysState *st, int H,
+                double *part, double2 *cgrid, double alpha, double q0, int max_n, cudaStream_t s) {
+  const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
+  k_mix_store<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, rho_out, nin_hist, res_hist, hist_off, st, H);
+  k_mix_gram_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, res_hist, hist_off, st, H, part);
+  k_mix_solve<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, H);
+  const int kerker = q0 > 0;
+  k_mix_combine<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, nin_hist, res_hist, hist_off, st, cgrid,
+                                               alpha, kerker);
+  if (kerker) {
+    launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
+    k_kerker_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, alpha, q0);
+    launch_fft3d_grid(t, 0, nsys, max_n, cgrid, +1, s);
+    k_add_real<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, cgrid);
+  }
+}
+
+void launch_potential(const Tables &t, int nsys, int max_nr, int max_n, const double *rho_in,
+                      double2 *cgrid, const double *vext, double *vhxc, double *vloc, float *vloc32,
+                      double *part, SysState *st, int all, cudaStream_t s) {
+  const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
+  k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, cgrid, all);
+  launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
+  k_hartree_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, all);
+  launch_fft3d_grid(t, 0, nsys, max_n, cgrid, +1, s);
+  k_build_vloc<<<dim3(RB, nsys), 256, 0, s>>>(t, rho_in, cgrid, vext, vhxc, vloc, vloc32, part, all);
+  k_vmax_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, all);
+}
+
+void launch_density_fft(const Tables &t, int nsys, int max_nr, int max_n, const double *rho,
+                        double2 *cgrid, cudaStream_t s) {
+  const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
+  k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho, cgrid, 0);
+  launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
+}
+
+void launch_uniform_density(const Tables &t, int nsys, int max_nr, double *rho, cudaStream_t s) {
+  const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
+  k_uniform_density<<<dim3(gx, nsys), 256, 0, s>>>(t, rho);
+}
+
+}  // namespace derek

@@ -1,0 +1,29 @@
+// Launchers of the grid-level SCF kernels (scf_kernels.cu).
+#pragma once
+
+#include <algorithm>
+
+#include "subspace.cuh"
+
+namespace derek {
+
+template <typename R>
+void launch_init_psi(const Tables &t, int nitems, void *X, unsigned long long seed, cudaStream_t st);
+void launch_filter_coef(const Tables &t, int nks, const double *eig, const SysState *st, Axpby *coef,
+                        int m, cudaStream_t s);
+void launch_occupations(const Tables &t, int nsys, const double *eig, double *occ, double *occw,
+                        SysState *st, cudaStream_t s);
+void launch_energies(const Tables &t, int nsys, const double *vhxc, const double *rho_in,
+                     const double *rho_out, const double2 *cgrid, double *part, SysState *st,
+                     SysDev *sys_rw, const int *ks_status, cudaStream_t s);
+void launch_mix(const Tables &t, int nsys, int max_nr, double *rho_in, const double *rho_out,
+                double *nin_hist, double *res_hist, const long long *hist_off, SysState *st, int H,
+                double *part, double2 *cgrid, double alpha, double q0, int max_n, cudaStream_t s);
+void launch_potential(const Tables &t, int nsys, int max_nr, int max_n, const double *rho_in,
+                      double2 *cgrid, const double *vext, double *vhxc, double *vloc, float *vloc32,
+                      double *part, SysState *st, int all, cudaStream_t s);
+void launch_density_fft(const Tables &t, int nsys, int max_nr, int max_n, const double *rho,
+                        double2 *cgrid, cudaStream_t s);
+void launch_uniform_density(const Tables &t, int nsys, int max_nr, double *rho, cudaStream_t s);
+
+}  // namespace derek

@@ -1,0 +1,461 @@
+// Subspace kernels of the Chebyshev-filtered subspace iteration:
+//   overlaps  A^H B (split-K, batched over k-sets)        -> FP64 matrices
+//   rotation  X <- X C (in place, batched over k-sets)
+//   Cholesky of the overlap and the inverse factor C = L^-H (FP64)
+//   Hermitian Jacobi eigensolver of the projected Hamiltonian (FP64)
+// These replace the empty wave_dot_* routines (Source/wave.f90:929-1036)
+// with the full matrices a Rayleigh-Ritz step needs.
+#include <cstdio>
+
+#include "subspace.cuh"
+
+namespace derek {
+
+// ---------------------------------------------------------------------------
+// Overlap: part[ks][split] = sum_{G in split} conj(A_i(G)) B_j(G)
+// ---------------------------------------------------------------------------
+constexpr int OT = 16;   // output tile
+constexpr int OKC = 32;  // K chunk staged in shared memory
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_overlap_partial(const Tables t, int ks_begin,
+                                                         const cplx<R> *__restrict__ A,
+                                                         const cplx<R> *__restrict__ B,
+                                                         double2 *__restrict__ part,
+                                                         const long long *__restrict__ part_off,
+                                                         int ksplit) {
+  __shared__ cplx<R> As[OT][OKC + 1];
+  __shared__ cplx<R> Bs[OT][OKC + 1];
+  const int ksi = ks_begin + blockIdx.z;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;
+  const int nb = K.nb;
+  const int nt = (nb + OT - 1) / OT;
+  const int ti = blockIdx.x / nt, tj = blockIdx.x - (blockIdx.x / nt) * nt;
+  if (ti >= nt) return;
+  const int split = blockIdx.y;
+  const int g0 = split * ksplit;
+  if (g0 >= K.npw) return;
+  const int g1 = min(K.npw, g0 + ksplit);
+  const int ty = threadIdx.x / OT, tx = threadIdx.x % OT;
+  const int i0 = ti * OT, j0 = tj * OT;
+  const cplx<R> *Ab = A + K.psi_off;
+  const cplx<R> *Bb = B + K.psi_off;
+  R ar = 0, ai = 0;
+  for (int k0 = g0; k0 < g1; k0 += OKC) {
+    for (int e = threadIdx.x; e < OT * OKC; e += blockDim.x) {
+      const int r = e / OKC, c = e % OKC;
+      const int g = k0 + c;
+      const int ia = i0 + r, jb = j0 + r;
+      As[r][c] = (ia < nb && g < g1) ? Ab[(long long)ia * K.npw_pad + g] : mk<R>(0, 0);
+      Bs[r][c] = (jb < nb && g < g1) ? Bb[(long long)jb * K.npw_pad + g] : mk<R>(0, 0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < OKC; ++c) {
+      const cplx<R> a = As[ty][c], b = Bs[tx][c];
+      ar += a.x * b.x + a.y * b.y;
+      ai += a.x * b.y - a.y * b.x;
+    }
+    __syncthreads();
+  }
+  const int i = i0 + ty, j = j0 + tx;
+  if (i < nb && j < nb)
+    part[part_off[ksi] + ((long long)split * nb + i) * nb + j] = make_double2((double)ar, (double)ai);
+}
+
+__global__ void k_overlap_reduce(const Tables t, int ks_begin, const double2 *__restrict__ part,
+                                 const long long *__restrict__ part_off, int ksplit,
+                                 double2 *__restrict__ out, const long long *__restrict__ mat_off,
+                                 int hermitize) {
+  const int ksi = ks_begin + blockIdx.x;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;
+  const int nb = K.nb;
+  const int nsplit = (K.npw + ksplit - 1) / ksplit;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    double x = 0, y = 0;
+    for (int s = 0; s < nsplit; ++s) {
+      const double2 v = part[part_off[ksi] + (long long)s * nb * nb + e];
+      x += v.x;
+      y += v.y;
+    }
+    out[mat_off[ksi] + e] = make_double2(x, y);
+  }
+  if (hermitize) {
+    __syncthreads();
+    double2 *M = out + mat_off[ksi];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      const int i = e / nb, j = e % nb;
+      if (i < j) {
+        const double2 a = M[i * nb + j], b = M[j * nb + i];
+        const double2 h = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+        M[i * nb + j] = h;
+        M[j * nb + i] = make_double2(h.x, -h.y);
+      } else if (i == j) {
+        M[e].y = 0.0;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Rotation: X[:, j] <- sum_i X[:, i] C[i][j], in place per G tile
+// ---------------------------------------------------------------------------
+constexpr int RG = 32;   // G columns per block
+constexpr int RI = 32;   // rows of C staged per chunk
+constexpr int RJ = 16;   // max output bands per thread (nb <= 8 * RJ = 128)
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_rotate(const Tables t, int ks_begin, cplx<R> *__restrict__ X,
+                                                const double2 *__restrict__ C,
+                                                const long long *__restrict__ mat_off) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ksi = ks_begin + blockIdx.y;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;
+  const int g0 = blockIdx.x * RG;
+  if (g0 >= K.npw) return;
+  const int nb = K.nb;
+  cplx<R> *Xs = reinterpret_cast<cplx<R> *>(smem_raw);   // [RI][RG]
+  cplx<R> *Cs = Xs + RI * RG;                            // [RI][nb]
+  const int g = threadIdx.x % RG, jg = threadIdx.x / RG;  // 8 j-groups
+  cplx<R> acc[RJ];
+#pragma unroll
+  for (int q = 0; q < RJ; ++q) acc[q] = mk<R>(0, 0);
+  cplx<R> *Xb = X + K.psi_off;
+  const double2 *Cb = C + mat_off[ksi];
+  for (int i0 = 0; i0 < nb; i0 += RI) {
+    const int ni = min(RI, nb - i0);
+    for (int e = threadIdx.x; e < RI * RG; e += blockDim.x) {
+      const int r = e / RG, c = e % RG;
+      const int gg = g0 + c;
+      Xs[e] = (r < ni && gg < K.npw) ? Xb[(long long)(i0 + r) * K.npw_pad + gg] : mk<R>(0, 0);
+    }
+    for (int e = threadIdx.x; e < ni * nb; e += blockDim.x) {
+      const int r = e / nb, c = e % nb;
+      const double2 v = Cb[(long long)(i0 + r) * nb + c];
+      Cs[r * nb + c] = mk<R>((R)v.x, (R)v.y);
+    }
+    __syncthreads();
+    for (int r = 0; r < ni; ++r) {
+      const cplx<R> x = Xs[r * RG + g];
+#pragma unroll
+      for (int q = 0; q < RJ; ++q) {
+        const int j = jg + 8 * q;
+        if (j < nb) {
+          const cplx<R> c = Cs[r * nb + j];
+          acc[q].x += x.x * c.x - x.y * c.y;
+          acc[q].y += x.x * c.y + x.y * c.x;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  const int gg = g0 + g;
+  if (gg < K.npw) {
+#pragma unroll
+    for (int q = 0; q < RJ; ++q) {
+      const int j = jg + 8 * q;
+      if (j < nb) Xb[(long long)j * K.npw_pad + gg] = acc[q];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky S = L L^H and C = L^-H (upper triangular), one block per k-set.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 zmulc(double2 a, double2 b) {  // a * conj(b)
+  return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+__global__ void __launch_bounds__(256) k_cholesky_inv(const Tables t, int ks_begin,
+                                                      const double2 *__restrict__ S,
+                                                      double2 *__restrict__ Cout,
+                                                      const long long *__restrict__ mat_off,
+                                                      double2 *__restrict__ scratch,
+                                                      int *__restrict__ status, int use_smem) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ksi = ks_begin + blockIdx.x;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;
+  const int n = K.nb;
+  double2 *M = use_smem ? reinterpret_cast<double2 *>(smem_raw) : scratch + 2 * mat_off[ksi];
+  double2 *Li = M + n * n;
+  __shared__ double s_diag;
+  __shared__ int s_fail;
+  const double2 *Sb = S + mat_off[ksi];
+  double dmax = 0.0;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    M[e] = Sb[e];
+    Li[e] = make_double2(0, 0);
+  }
+  if (threadIdx.x == 0) s_fail = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) dmax = fmax(dmax, M[i * n + i].x);
+    s_diag = dmax;
+  }
+  __syncthreads();
+  const double thr = 1e-13 * s_diag;
+  for (int j = 0; j < n; ++j) {
+    if (threadIdx.x == 0) {
+      const double d = M[j * n + j].x;
+      if (!(d > thr)) s_fail = 1;
+      M[j * n + j] = make_double2(sqrt(fmax(d, thr)), 0.0);
+    }
+    __syncthreads();
+    const double inv = 1.0 / M[j * n + j].x;
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) {
+      M[i * n + j].x *= inv;
+      M[i * n + j].y *= inv;
+    }
+    __syncthreads();
+    // trailing update of the lower triangle: M[i][k] -= L[i][j] conj(L[k][j]), j < k <= i
+    const int m = n - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = j + 1 + e / m, k = j + 1 + e % m;
+      if (k <= i) {
+        const double2 p = zmulc(M[i * n + j], M[k * n + j]);
+        M[i * n + k].x -= p.x;
+        M[i * n + k].y -= p.y;
+      }
+    }
+    __syncthreads();
+  }
+  // inverse of L: column c solves L x = e_c (forward substitution), one thread per column
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    for (int i = c; i < n; ++i) {
+      double2 acc = make_double2(i == c ? 1.0 : 0.0, 0.0);
+      for (int p = c; p < i; ++p) {
+        const double2 q = zmul(M[i * n + p], Li[p * n + c]);
+        acc.x -= q.x;
+        acc.y -= q.y;
+      }
+      const double d = 1.0 / M[i * n + i].x;
+      Li[i * n + c] = make_double2(acc.x * d, acc.y * d);
+    }
+  }
+  __syncthreads();
+  // C[i][j] = conj(Linv[j][i])
+  double2 *Cb = Cout + mat_off[ksi];
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    const double2 v = Li[j * n + i];
+    Cb[e] = make_double2(v.x, -v.y);
+  }
+  if (threadIdx.x == 0 && s_fail) status[ksi] = DEREK_ERR_CHOLESKY;
+}
+
+// ---------------------------------------------------------------------------
+// Hermitian Jacobi eigensolver (parallel cyclic, round-robin pair ordering).
+// A <- U^H A U with U = diag(1, e^{-i phi}) [[c, s], [-s, c]] on each pair.
+// Eigenvalues ascending go to eig[item0 + j]; eigenvectors (columns) to C.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
+                                                const double2 *__restrict__ Hs,
+                                                double2 *__restrict__ Cout,
+                                                const long long *__restrict__ mat_off,
+                                                double *__restrict__ eig,
+                                                double2 *__restrict__ scratch, int max_sweeps,
+                                                double tol, int v_in_smem,
+                                                int *__restrict__ sweeps_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ksi = ks_begin + blockIdx.x;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;
+  const int n = K.nb;
+  const int ne = n + (n & 1);  // even count for the tournament
+  const int np = ne / 2;
+  double2 *A = reinterpret_cast<double2 *>(smem_raw);
+  double2 *V = v_in_smem ? A + n * n : scratch + 2 * mat_off[ksi];
+  double *rc = reinterpret_cast<double *>(A + n * n + (v_in_smem ? n * n : 0));  // [np]
+  double *rs = rc + np;
+  double2 *rph = reinterpret_cast<double2 *>(rs + np);  // [np]
+  int *pp = reinterpret_cast<int *>(rph + np);           // [np]
+  int *pq = pp + np;                                    // [np]
+  int *idx = pq + np;                                   // [ne]
+  __shared__ double red[256];
+  __shared__ double red2[256];
+  const double2 *Hb = Hs + mat_off[ksi];
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    A[e] = Hb[e];
+    const int i = e / n, j = e % n;
+    V[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) idx[i] = i;
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    // convergence: sum of |offdiag|^2 vs sum of |A|^2, both summed directly
+    double off = 0, tot = 0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const double m2 = A[e].x * A[e].x + A[e].y * A[e].y;
+      tot += m2;
+      if (e / n != e % n) off += m2;
+    }
+    red[threadIdx.x] = off;
+    red2[threadIdx.x] = tot;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        red[threadIdx.x] += red[threadIdx.x + s];
+        red2[threadIdx.x] += red2[threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    const bool done = red[0] <= tol * tol * red2[0];
+    __syncthreads();
+    if (done) break;
+    for (int round = 0; round < ne - 1; ++round) {
+      for (int k = threadIdx.x; k < np; k += blockDim.x) {
+        int p = idx[k], q = idx[ne - 1 - k];
+        if (p > q) {
+          const int tmp = p;
+          p = q;
+          q = tmp;
+        }
+        pp[k] = p;
+        pq[k] = q;
+        double c = 1.0, s = 0.0;
+        double2 ph = make_double2(1.0, 0.0);
+        if (q < n) {
+          const double a = A[p * n + p].x, d = A[q * n + q].x;
+          const double2 b = A[p * n + q];
+          const double e = hypot(b.x, b.y);
+          if (e > 0.0) {
+            ph = make_double2(b.x / e, b.y / e);
+            const double tau = (d - a) / (2.0 * e);
+            const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + tt * tt);
+            s = tt * c;
+          }
+        }
+        rc[k] = c;
+        rs[k] = s;
+        rph[k] = ph;
+      }
+      __syncthreads();
+      // rows: new p = c A_p - s ph A_q ; new q = s A_p + c ph A_q
+      for (int w = threadIdx.x; w < np * n; w += blockDim.x) {
+        const int k = w / n, col = w % n;
+        const int p = pp[k], q = pq[k];
+        if (q >= n || rs[k] == 0.0) continue;
+        const double c = rc[k], s = rs[k];
+        const double2 ph = rph[k];
+        const double2 ap = A[p * n + col], aq = A[q * n + col];
+        const double2 phq = zmul(ph, aq);
+        A[p * n + col] = make_double2(c * ap.x - s * phq.x, c * ap.y - s * phq.y);
+        A[q * n + col] = make_double2(s * ap.x + c * phq.x, s * ap.y + c * phq.y);
+      }
+      __syncthreads();
+      // columns of A and V: new p = c X_p - s conj(ph) X_q ; new q = s X_p + c conj(ph) X_q
+      for (int w = threadIdx.x; w < np * n; w += blockDim.x) {
+        const int k = w / n, row = w % n;
+        const int p = pp[k], q = pq[k];
+        if (q >= n || rs[k] == 0.0) continue;
+        const double c = rc[k], s = rs[k];
+        const double2 phc = make_double2(rph[k].x, -rph[k].y);
+        {
+          const double2 xp = A[row * n + p], xq = A[row * n + q];
+          const double2 t2 = zmul(phc, xq);
+          A[row * n + p] = make_double2(c * xp.x - s * t2.x, c * xp.y - s * t2.y);
+          A[row * n + q] = make_double2(s * xp.x + c * t2.x, s * xp.y + c * t2.y);
+        }
+        {
+          const double2 xp = V[row * n + p], xq = V[row * n + q];
+          const double2 t2 = zmul(phc, xq);
+          V[row * n + p] = make_double2(c * xp.x - s * t2.x, c * xp.y - s * t2.y);
+          V[row * n + q] = make_double2(s * xp.x + c * t2.x, s * xp.y + c * t2.y);
+        }
+      }
+      __syncthreads();
+      // next tournament round: keep idx[0], rotate the rest by one
+      if (threadIdx.x == 0) {
+        const int last = idx[ne - 1];
+        for (int i = ne - 1; i > 1; --i) idx[i] = idx[i - 1];
+        idx[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0 && sweeps_out) sweeps_out[ksi] = sweep;
+  // sort eigenvalues ascending (selection by rank; ties broken by index)
+  double *ev = rc;  // reuse: n entries needed, np*2 >= n available
+  for (int i = threadIdx.x; i < n; i += blockDim.x) ev[i] = A[i * n + i].x;
+  __syncthreads();
+  double2 *Cb = Cout + mat_off[ksi];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double vi = ev[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) rank += (ev[j] < vi) || (ev[j] == vi && j < i);
+    eig[K.item0 + rank] = vi;
+    for (int r = 0; r < n; ++r) Cb[r * n + rank] = V[r * n + i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename R>
+void launch_overlap(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, int ksplit,
+                    const cplx<R> *A, const cplx<R> *B, double2 *part, const long long *part_off,
+                    double2 *out, const long long *mat_off, int hermitize, cudaStream_t st) {
+  if (nks <= 0) return;
+  const int nt = (max_nb + OT - 1) / OT;
+  dim3 grid(nt * nt, (max_npw + ksplit - 1) / ksplit, nks);
+  k_overlap_partial<R><<<grid, 256, 0, st>>>(t, ks_begin, A, B, part, part_off, ksplit);
+  k_overlap_reduce<<<nks, 256, 0, st>>>(t, ks_begin, part, part_off, ksplit, out, mat_off, hermitize);
+}
+
+template <typename R>
+void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, cplx<R> *X,
+                   const double2 *C, const long long *mat_off, cudaStream_t st) {
+  if (nks <= 0) return;
+  const size_t sm = (RI * RG + (size_t)RI * max_nb) * sizeof(cplx<R>);
+  cudaFuncSetAttribute(k_rotate<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((max_npw + RG - 1) / RG, nks);
+  k_rotate<R><<<grid, 256, sm, st>>>(t, ks_begin, X, C, mat_off);
+}
+
+bool cholesky_fits_smem(int max_nb) { return 2 * (size_t)max_nb * max_nb * 16 <= 200 * 1024; }
+bool jacobi_v_fits_smem(int max_nb) { return 2 * (size_t)max_nb * max_nb * 16 + 64 * max_nb + 256 <= 210 * 1024; }
+
+void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *S,
+                         double2 *C, const long long *mat_off, double2 *scratch, int *status,
+                         cudaStream_t st) {
+  if (nks <= 0) return;
+  const int use_smem = cholesky_fits_smem(max_nb);
+  const size_t sm = use_smem ? 2 * (size_t)max_nb * max_nb * sizeof(double2) : 0;
+  cudaFuncSetAttribute(k_cholesky_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_cholesky_inv<<<nks, 256, sm, st>>>(t, ks_begin, S, C, mat_off, scratch, status, use_smem);
+}
+
+void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
+                   double2 *C, const long long *mat_off, double *eig, double2 *scratch,
+                   int max_sweeps, double tol, int *sweeps_out, cudaStream_t st) {
+  if (nks <= 0) return;
+  const int v_smem = jacobi_v_fits_smem(max_nb);
+  const int ne = max_nb + 1;
+  const size_t sm = (size_t)max_nb * max_nb * sizeof(double2) * (v_smem ? 2 : 1) +
+                    (size_t)ne / 2 * (2 * sizeof(double) + sizeof(double2) + 2 * sizeof(int)) +
+                    (size_t)(ne + 1) * sizeof(int) + 64;
+  cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_jacobi<<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps, tol,
+                                 v_smem, sweeps_out);
+}
+
+#define DEREK_INST(R)                                                                          \
+  template void launch_overlap<R>(const Tables &, int, int, int, int, int, const cplx<R> *,    \
+                                  const cplx<R> *, double2 *, const long long *, double2 *,   \
+                                  const long long *, int, cudaStream_t);                      \
+  template void launch_rotate<R>(const Tables &, int, int, int, int, cplx<R> *,               \
+                                 const double2 *, const long long *, cudaStream_t);
+DEREK_INST(float)
+DEREK_INST(double)
+#undef DEREK_INST
+
+}  // namespace derek

@@ -1,0 +1,46 @@
+// Launchers of the subspace kernels (subspace.cu) and the SCF grid kernels
+// (scf_kernels.cu).
+#pragma once
+
+#include "kernels.cuh"
+
+namespace derek {
+
+constexpr int kMaxBands = 128;   // per k-set (rotation kernel register tile)
+constexpr int kOverlapSplit = 2048;
+
+template <typename R>
+void launch_overlap(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, int ksplit,
+                    const cplx<R> *A, const cplx<R> *B, double2 *part, const long long *part_off,
+                    double2 *out, const long long *mat_off, int hermitize, cudaStream_t st);
+template <typename R>
+void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, cplx<R> *X,
+                   const double2 *C, const long long *mat_off, cudaStream_t st);
+bool cholesky_fits_smem(int max_nb);
+bool jacobi_v_fits_smem(int max_nb);
+void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *S,
+                         double2 *C, const long long *mat_off, double2 *scratch, int *status,
+                         cudaStream_t st);
+void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
+                   double2 *C, const long long *mat_off, double *eig, double2 *scratch,
+                   int max_sweeps, double tol, int *sweeps_out, cudaStream_t st);
+
+// Per-system SCF scalars kept on the device.
+constexpr int kMaxHist = 16;
+struct SysState {
+  double mu, entropy, e_band, e_dc, e_h, e_xc, energy, free, free_prev, delta;
+  double vmax;             // max V_loc (filter upper bound)
+  double etol;
+  double rtol;             // density residual tolerance (0 = off)
+  double resid;            // max|n_out - n_in|
+  int iter;
+  int converged;
+  int status;
+  int nhist;               // stored mixing pairs
+  int slot;                // slot of the newest pair
+  int pad;
+  double gram[kMaxHist * kMaxHist];
+  double coef[kMaxHist];
+};
+
+}  // namespace derek

@@ -91,6 +91,8 @@ typedef struct {
   uint64_t seed;           /* start-vector hash seed */
   int    use_graph;        /* capture each SCF iteration in a CUDA graph */
   int    use_tensor_cores; /* mixed mode: tcgen05 BF16x3 contractions */
+  double density_tol;      /* also require max|n_out - n_in| < density_tol
+                              (0 = energy criterion only, as the reference) */
 } derek_scf_opts;
 
 /* Per-system SCF report (Source/electronic.f90:143-146 table row). */
@@ -101,6 +103,7 @@ typedef struct {
   double efermi;           /* Fermi level */
   double entropy;
   double e_band, e_hartree, e_xc, e_dc;
+  double residual;         /* max|n_out - n_in| of the last iteration */
   int    iterations;
   int    converged;
 } derek_scf_report;

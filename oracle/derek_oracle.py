@@ -544,13 +544,15 @@ class ScfResult:
 
 
 def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3,
-        history: int = 8, q0: float = 0.0, solver: str = "dense", verbose: bool = False) -> ScfResult:
+        history: int = 8, q0: float = 0.0, solver: str = "dense", verbose: bool = False,
+        rtol: float = None) -> ScfResult:
     """Self-consistent field loop (the intended electronic_scf,
     Source/electronic.f90:86-175: iterate until |E - E_prev| < etol).
 
     Each iteration diagonalises H[n_in] exactly ("dense", scipy eigh of the
     Npw x Npw matrix), fills bands with Fermi-Dirac occupations, forms n_out,
     evaluates the energies of n_out and mixes.  Start density: uniform Ne/Omega.
+    With rtol set, convergence also needs max|n_out - n_in| < rtol.
     """
     import scipy.linalg as sla
 
@@ -586,11 +588,12 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
         e_dc = dv * float(np.dot(vhxc, nout))
         energy = eband - e_dc + eh + exc
         free = energy - sys.kT * ent
-        hist.append((it, energy, free, mu))
+        resid = float(np.max(np.abs(nout - nin)))
+        hist.append((it, energy, free, mu, resid))
         if verbose:
-            print(f"scf {it:3d} E={energy:.12f} F={free:.12f} mu={mu:.8f}")
+            print(f"scf {it:3d} E={energy:.12f} F={free:.12f} mu={mu:.8f} |R|={resid:.2e}")
         result = ScfResult(False, it, energy, free, mu, eigs, f, nout, hist)
-        if e_prev is not None and abs(free - e_prev) < etol:
+        if e_prev is not None and abs(free - e_prev) < etol and (rtol is None or resid < rtol):
             result.converged = True
             break
         e_prev = free

@@ -1,0 +1,114 @@
+"""GPU SCF parity against the FP64 oracle's converged fixtures
+(tests/golden/make_scf_golden.py).
+
+FP64 path: free energy, energy, Fermi level and eigenvalues within 1e-8 Ha,
+output density within 1e-7 (relative L2).  Mixed path: |dF| / N_e < 1e-6 Ha
+per electron, the headline accuracy target; eigenvalue and density errors are
+bounded loosely and reported.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def make_handle(oracle, d, precision=0, **opts):
+    import derek_gb300 as dg
+    cell = d["cell"]
+    nf = tuple(int(x) for x in d["n_fine"])
+    vext = oracle.vext_jellium_wells(cell, nf, float(d["nelec"]), d["wells"])
+    spec = dg.SystemSpec(cell, float(d["ecut"]), d["kpts"], int(d["nbands"]), float(d["nelec"]),
+                         kT=float(d["kT"]), wk=d["wk"], vext=vext, n_fine=nf,
+                         inv_cell=oracle.inv_cell(cell))
+    kw = dict(mix_alpha=0.3, kerker_q0=float(d["q0"]), pulay_history=8, density_tol=1e-10)
+    kw.update(opts)
+    return dg.Handle(spec, precision=precision, **kw)
+
+
+@pytest.mark.parametrize("name", ["scf_c1", "scf_kpts"])
+def test_scf_fp64_matches_oracle(oracle, name):
+    d = load(name)
+    with make_handle(oracle, d) as h:
+        rep = h.electronic_scf(max_scf=300, etol=1e-12)[0]
+        eig = h.eigenvalues()
+        rho = h.density()
+        occ = h.occupations()
+    assert rep["converged"], rep
+    assert abs(rep["free_energy"] - d["free_energy"]) < 1e-8, (rep["free_energy"], d["free_energy"])
+    assert abs(rep["energy"] - d["energy"]) < 1e-8
+    assert abs(rep["efermi"] - d["efermi"]) < 1e-8
+    assert np.max(np.abs(eig - d["eig"])) < 1e-8, np.max(np.abs(eig - d["eig"]))
+    assert np.max(np.abs(occ - d["occ"])) < 1e-6
+    rel = np.linalg.norm(rho - d["density"]) / np.linalg.norm(d["density"])
+    assert rel < 1e-7, rel
+
+
+def test_scf_mixed_precision_accuracy(oracle):
+    d = load("scf_c1")
+    with make_handle(oracle, d, precision=1, density_tol=0.0) as h:
+        rep = h.electronic_scf(max_scf=200, etol=1e-7)[0]
+        eig = h.eigenvalues()
+        rho = h.density()
+    assert rep["converged"], rep
+    per_electron = abs(rep["free_energy"] - d["free_energy"]) / float(d["nelec"])
+    assert per_electron < 1e-6, per_electron
+    assert np.max(np.abs(eig - d["eig"])) < 1e-4
+    rel = np.linalg.norm(rho - d["density"]) / np.linalg.norm(d["density"])
+    assert rel < 1e-3, rel
+
+
+def test_scf_graph_matches_eager(oracle):
+    d = load("scf_kpts")
+    out = []
+    for g in (0, 1):
+        with make_handle(oracle, d, use_graph=g) as h:
+            rep = h.electronic_scf(max_scf=60, etol=1e-9)[0]
+            out.append((rep["free_energy"], rep["iterations"], h.eigenvalues()))
+    assert out[0][1] == out[1][1]
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][2], out[1][2])
+
+
+def test_scf_deterministic_rerun(oracle):
+    d = load("scf_kpts")
+    with make_handle(oracle, d) as h:
+        a = h.electronic_scf(max_scf=40, etol=1e-9)[0]
+        rho_a = h.density()
+        b = h.electronic_scf(max_scf=40, etol=1e-9)[0]
+        rho_b = h.density()
+    assert a["free_energy"] == b["free_energy"] and a["iterations"] == b["iterations"]
+    assert np.array_equal(rho_a, rho_b)
+
+
+def test_scf_not_converged_status(oracle):
+    import derek_gb300 as dg
+    d = load("scf_kpts")
+    with make_handle(oracle, d) as h:
+        rep = h.electronic_scf(max_scf=2, etol=1e-12)[0]
+        assert not rep["converged"] and rep["iterations"] == 2
+        # the handle stays usable
+        rep = h.electronic_scf(max_scf=100, etol=1e-8)[0]
+        assert rep["converged"]
+
+
+def test_nan_in_potential_is_reported(oracle):
+    import derek_gb300 as dg
+    d = load("scf_kpts")
+    d = dict(d)
+    cell = d["cell"]
+    nf = tuple(int(x) for x in d["n_fine"])
+    vext = oracle.vext_jellium_wells(cell, nf, float(d["nelec"]), d["wells"])
+    vext[17] = np.nan
+    spec = dg.SystemSpec(cell, float(d["ecut"]), d["kpts"], int(d["nbands"]), float(d["nelec"]),
+                         kT=float(d["kT"]), vext=vext, n_fine=nf)
+    with dg.Handle(spec) as h:
+        with pytest.raises(dg.DerekError) as e:
+            h.electronic_scf(max_scf=5, etol=1e-8)
+        assert e.value.status in (dg._abi.DEREK_ERR_NAN, dg._abi.DEREK_ERR_CHOLESKY)
