@@ -1,0 +1,326 @@
+#!/usr/bin/env python3
+"""Benchmark: converged ground states per second on the 64-k-point workload.
+
+Workload (synthetic, seeded): cubic cell L=16 bohr, Ecut=20 Ha, FFT grid
+72^3, 4x4x4 Monkhorst-Pack k-points (64), 64 electrons in 80 bands, jellium +
+16 Gaussian wells, LDA, Kerker + Pulay mixing, kT = 0.01 Ha.
+
+One step = one self-consistent ground state from the uniform start density to
+|dF| < etol, on the mixed-precision path (complex64 FFT / H.psi, FP64
+Cholesky, Jacobi, occupations and energies).  Before timing, the same
+workload is solved once on the all-FP64 path and the mixed result must agree
+to |dF| / N_e < 1e-6 Ha per electron (the line records the error).
+
+value  : ground states/s with inputs resident on the device (handle reused,
+         SCF restarted each step), timed with CUDA events on the library's
+         stream.
+e2e    : the same through the C ABI with host buffers: each step uploads the
+         external potential from pinned host memory, runs the SCF and copies
+         eigenvalues, occupations and density back.
+roofline: the fused H.psi (three stage kernels over all 64 x 80 bands),
+         algorithmic bytes = psi in + H psi out (8 B per complex64 coefficient)
+         + the sphere index map (4 B per plane wave) + V(r) (4 B per point),
+         divided by its CUDA-event time, against MEASURED_PEAKS.json hbm_gbs.
+The working set (planes buffer ~7 GB) is far larger than L2, so no flush is
+needed between steps.
+
+--impl reference times the FP64 numpy oracle (the reference's SCF is a stub
+and its Fortran build is unavailable) on all host cores on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "converged ground states/sec at |dE|<1e-6 Ha/e vs FP64 path"
+UNIT = "ground_states/s"
+WORKLOAD = "kpts64: L=16 bohr, Ecut=20 Ha, 72^3 grid, 4x4x4 MP (64 k), 64 e / 80 bands, 16 wells"
+ETOL = 1e-6          # Ha, |F - F_prev| per iteration
+FP64_TOL = 1e-6      # Ha per electron vs the FP64 path
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="kpts64")
+    p.add_argument("--skip-fp64", action="store_true", help="skip the FP64 accuracy gate (debug)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons (200 ms)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax.append(float(c[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, c[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def hpsi_bytes(h, specs, elem=8, real=4):
+    """Algorithmic bytes of one H.psi over every band (buffer bands included)
+    of every k-point."""
+    total = 0
+    for si, s in enumerate(specs):
+        nf, _ = h.grid(si)
+        nbi = h.bands(si)[1]
+        total += real * nf[0] * nf[1] * nf[2]
+        for k in range(len(s.kpts)):
+            npw = h.npw(si, k)
+            total += 2 * elem * npw * nbi + 4 * npw
+    return total
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import derek_gb300 as dg
+    from derek_gb300 import workloads
+
+    specs, mix = workloads.WORKLOADS[args.workload]()
+    nelec = sum(s.nelec for s in specs)
+    scf_opts = dict(cheb_degree=8, first_passes=4, first_degree=10, **mix)
+    out = {"metric": METRIC, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "complex64 (FP32 FFT/H.psi) + FP64 subspace",
+           "data": "synthetic (seeded)"}
+
+    # ---- accuracy gate: FP64 path once, untimed
+    f64 = None
+    if not args.skip_fp64:
+        with dg.Handle(specs, precision=dg.DEREK_PREC_FP64, **scf_opts) as h64:
+            t = time.time()
+            rep64 = h64.electronic_scf(max_scf=100, etol=ETOL * 1e-2)
+            f64 = [r["free_energy"] for r in rep64]
+            fp64_seconds = time.time() - t
+
+    h = dg.Handle(specs, precision=dg.DEREK_PREC_MIXED, **scf_opts)
+    ext = torch.cuda.ExternalStream(h.stream())
+    for _ in range(args.warmup):
+        h.electronic_scf(max_scf=100, etol=ETOL)
+
+    clocks = Clocks()
+    l0 = dg.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = []
+    with clocks:
+        torch.cuda.synchronize()
+        ev0.record(ext)
+        for _ in range(args.steps):
+            reps.append(h.electronic_scf(max_scf=100, etol=ETOL))
+        ev1.record(ext)
+        torch.cuda.synchronize()
+    launches = dg.launch_count() - l0
+    ms = ev0.elapsed_time(ev1)
+    converged = sum(int(r["converged"]) for rep in reps for r in rep)
+    value = converged / (ms / 1e3)
+    iters = [r["iterations"] for r in reps[-1]]
+
+    err = None
+    if f64 is not None:
+        err = max(abs(r["free_energy"] - f) for r, f in zip(reps[-1], f64)) / max(nelec, 1)
+        if err >= FP64_TOL:
+            print(json.dumps({"error": f"mixed vs FP64 |dF|/Ne = {err:.3e} >= {FP64_TOL}"}),
+                  file=sys.stderr)
+
+    # ---- end to end through the C ABI with host buffers
+    vext_host = []
+    for si in range(len(specs)):
+        v = torch.from_numpy(h.get_vext(si)).pin_memory()
+        vext_host.append(v)
+    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h2d = sum(v.numel() * 8 for v in vext_host)
+    d2h = 0
+    torch.cuda.synchronize()
+    ev2.record(ext)
+    for _ in range(args.steps):
+        for si in range(len(specs)):
+            h.set_vext(vext_host[si].numpy(), si)
+        h.electronic_scf(max_scf=100, etol=ETOL)
+        d2h = 0
+        for si in range(len(specs)):
+            d2h += h.eigenvalues(si).nbytes + h.occupations(si).nbytes + h.density(si).nbytes
+    ev3.record(ext)
+    torch.cuda.synchronize()
+    e2e_ms = ev2.elapsed_time(ev3)
+    e2e = {"value": round(len(specs) * args.steps / (e2e_ms / 1e3), 4), "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    # ---- roofline of the fused H.psi
+    t_apply, stages = h.time_apply_h(nrep=5)
+    nbytes = hpsi_bytes(h, specs)
+    peak, src = measured_peaks()
+    achieved = nbytes / (t_apply / 1e3) / 1e9
+    stage_names = ["inv_yz (scatter + backward z,y)", "vmul_x (backward x, V(r), forward x)",
+                   "fwd_yz (forward y,z + gather + kinetic)"]
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None,
+                "kernel": "fused H.psi, 3 stage kernels over 64 k x 80 bands",
+                "bytes_per_launch": nbytes, "ms_per_launch": round(t_apply, 4),
+                "stage_ms": {n: round(x, 4) for n, x in zip(stage_names, stages)},
+                "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)"}
+    bands_per_gs = _hpsi_band_applications(specs, reps[-1], scf_opts)
+
+    out.update({
+        "value": round(value, 4),
+        "ms_per_step": round(ms / args.steps, 2),
+        "config": {"workload": WORKLOAD, "precision": "mixed", "etol_Ha": ETOL,
+                   "iterations": iters, "chebyshev_degree": scf_opts["cheb_degree"],
+                   "l2": "inputs larger than L2 (planes buffer ~7 GB), no flush",
+                   "parallelism": f"replicas x{args.gpus}"},
+        "accuracy": {"mixed_vs_fp64_dF_per_electron_Ha": err,
+                     "fp64_path_seconds": round(fp64_seconds, 2) if f64 else None,
+                     "fp64_free_energy": f64},
+        "e2e": e2e,
+        "roofline": roofline,
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "hpsi_band_applications_per_ground_state": bands_per_gs,
+    })
+    h.close()
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(specs, scf_opts, bands_per_gs, workers=1)
+    return out
+
+
+def _hpsi_band_applications(specs, rep, o):
+    """Band H.psi applications of one ground state: the first iteration does
+    one Rayleigh-Ritz H.psi plus first_passes x (first_degree + 1); every
+    later one cheb_degree + 1."""
+    total = 0
+    for s, r in zip(specs, rep):
+        per_iter = o["cheb_degree"] + 1
+        first = 1 + o["first_passes"] * (o["first_degree"] + 1) + 0
+        n = first + max(r["iterations"] - 1, 0) * per_iter
+        total += n * len(s.kpts) * s.nbands
+    return total
+
+
+def _spec_dict(s):
+    return {"cell": s.cell.tolist(), "ecut": s.ecut, "kpts": s.kpts.tolist(), "nbands": s.nbands,
+            "nelec": s.nelec, "kT": s.kT, "wells": s.wells.tolist()}
+
+
+def cpu_baseline(specs, scf_opts, bands_per_gs, workers=1, kpoints=1):
+    from oracle import cpu_baseline as cb
+    spec = _spec_dict(specs[0])
+    deg = scf_opts["cheb_degree"]
+    r = cb.sample(spec, deg, kpoints=kpoints, workers=workers)
+    # seconds per band H.psi in the sample (degree + 1 block applications)
+    per_band = r["per_k_iteration_s"] / ((deg + 1) * specs[0].nbands)
+    if workers > 1:
+        per_band = r["wall_s"] / (kpoints * (deg + 1) * specs[0].nbands)
+    gs_rate = 1.0 / (per_band * bands_per_gs)
+    return {"value": gs_rate, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": (f"{kpoints} k-point subspace iteration(s) of the same workload on the FP64 numpy "
+                       f"oracle ({deg} filtered H.psi + 1 Rayleigh-Ritz H.psi on 80 bands, CholQR, "
+                       f"eigh) = {r['wall_s']:.1f} s; scaled by {bands_per_gs} band H.psi "
+                       f"applications per ground state")}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    import numpy as np
+    from derek_gb300 import workloads  # noqa: F401  (inputs only; no GPU use)
+    specs, mix = workloads.WORKLOADS[args.workload]()
+    scf_opts = dict(cheb_degree=8, first_passes=4, first_degree=10, **mix)
+    from oracle import cpu_baseline as cb
+    ncores = cb.cores()
+    # work per ground state as the GPU solver's typical 20-iteration SCF
+    rep = [{"iterations": 20} for _ in specs]
+    bands_per_gs = _hpsi_band_applications(specs, rep, scf_opts)
+    samples = []
+    for i in range(args.warmup + args.steps):
+        c = cpu_baseline(specs, scf_opts, bands_per_gs, workers=ncores, kpoints=ncores)
+        if i >= args.warmup:
+            samples.append(c)
+    value = float(np.mean([c["value"] for c in samples]))
+    out = {"impl": "reference", "metric": METRIC, "unit": UNIT, "value": value, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+           "config": {"workload": WORKLOAD, "assumed_scf_iterations": 20},
+           "ms_per_step": 1e3 / value if value > 0 else None,
+           "cpu_baseline": dict(samples[-1], value=value),
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": ("DEReK's own SCF is a stub (Source/electronic.f90:135-167) and its Fortran/"
+                    "FFTW/MPI build is unavailable here; the FP64 numpy oracle port stands in")}
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        out = run_reference(args)
+    else:
+        out = run_ours(args)
+    if out is not None and int(os.environ.get("RANK", "0")) == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

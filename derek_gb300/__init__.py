@@ -134,6 +134,12 @@ class Handle:
         _check(lib.derek_gpu_grid(self._h, sys, nf, ns), self._h, "grid")
         return tuple(nf), tuple(ns)
 
+    def bands(self, sys=0):
+        """(requested bands, bands carried internally including the buffer)."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _check(lib.derek_gpu_bands(self._h, sys, ctypes.byref(a), ctypes.byref(b)), self._h, "bands")
+        return a.value, b.value
+
     def npw(self, sys=0, k=0):
         n = ctypes.c_int()
         _check(lib.derek_gpu_npw(self._h, sys, k, ctypes.byref(n)), self._h, "npw")
@@ -238,11 +244,39 @@ class Handle:
         _check(lib.derek_gpu_get_occupations(self._h, sys, _dptr(e)), self._h, "occupations")
         return e
 
+    def set_vext(self, v, sys=0):
+        v = np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+        _check(lib.derek_gpu_set_vext(self._h, sys, _dptr(v)), self._h, "set_vext")
+
+    def get_vext(self, sys=0):
+        nf, _ = self.grid(sys)
+        v = np.zeros(int(np.prod(nf)))
+        _check(lib.derek_gpu_get_vext(self._h, sys, _dptr(v)), self._h, "get_vext")
+        return v
+
+    def stream(self):
+        """The handle's cudaStream_t as an integer (for external event timing)."""
+        return int(lib.derek_gpu_stream(self._h) or 0)
+
+    def time_apply_h(self, nrep=5):
+        """Mean device ms of one H.psi over every band and k-point, and of its
+        three stage kernels."""
+        tot = ctypes.c_double()
+        stage = (ctypes.c_double * 3)()
+        _check(lib.derek_gpu_time_apply_h(self._h, int(nrep), ctypes.byref(tot), stage), self._h,
+               "time_apply_h")
+        return tot.value, list(stage)
+
     def density(self, sys=0):
         nf, _ = self.grid(sys)
         rho = np.zeros(int(np.prod(nf)))
         _check(lib.derek_gpu_get_density(self._h, sys, _dptr(rho)), self._h, "density")
         return rho
+
+
+def launch_count() -> int:
+    """Kernels launched by the library in this process (graph replays included)."""
+    return int(lib.derek_gpu_launch_count())
 
 
 def host_prime_fact(n: int) -> int:

@@ -49,7 +49,7 @@ class ScfOpts(ctypes.Structure):
         ("precision", _i), ("mix_alpha", _d), ("kerker_q0", _d), ("pulay_history", _i),
         ("cheb_degree", _i), ("first_passes", _i), ("first_degree", _i),
         ("seed", ctypes.c_uint64), ("use_graph", _i), ("use_tensor_cores", _i),
-        ("density_tol", _d),
+        ("density_tol", _d), ("buffer_bands", _i),
     ]
 
 
@@ -75,6 +75,7 @@ SIGNATURES = {
     "derek_gpu_destroy": (_i, [_vp]),
     "derek_gpu_grid": (_i, [_vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "derek_gpu_npw": (_i, [_vp, _i, _i, ctypes.POINTER(_i)]),
+    "derek_gpu_bands": (_i, [_vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "derek_gpu_gsphere": (_i, [_vp, _i, _i, _vp, _vp, _pd]),
     "derek_gpu_fft3d": (_i, [_vp, _i, _pd, _i]),
     "derek_gpu_set_vloc": (_i, [_vp, _i, _pd]),
@@ -90,6 +91,11 @@ SIGNATURES = {
     "derek_gpu_get_eigenvalues": (_i, [_vp, _i, _pd]),
     "derek_gpu_get_occupations": (_i, [_vp, _i, _pd]),
     "derek_gpu_get_density": (_i, [_vp, _i, _pd]),
+    "derek_gpu_set_vext": (_i, [_vp, _i, _pd]),
+    "derek_gpu_get_vext": (_i, [_vp, _i, _pd]),
+    "derek_gpu_stream": (_vp, [_vp]),
+    "derek_gpu_launch_count": (ctypes.c_ulonglong, []),
+    "derek_gpu_time_apply_h": (_i, [_vp, _i, _pd, _pd]),
     "derek_host_prime_fact": (_i, [_i]),
     "derek_host_grid_sizes": (_i, [ctypes.POINTER(_d), _d, _d, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "derek_host_gsphere": (_i, [ctypes.POINTER(_d), _d, ctypes.POINTER(_d), ctypes.POINTER(_i), _i, _vp,

@@ -1,6 +1,7 @@
 // Handle creation and the primitive C-ABI entry points (tables, FFT, H.psi,
 // density, XC).  The SCF entry points live in scf.cu.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -13,6 +14,10 @@ using derek::KSetDev;
 using derek::SysDev;
 
 namespace derek {
+
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch(long long n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+unsigned long long launch_total() { return g_launches.load(std::memory_order_relaxed); }
 
 int cuda_status(cudaError_t e, derek_gpu *h, const char *what) {
   if (h) h->last_error = std::string(what) + ": " + cudaGetErrorString(e);
@@ -76,7 +81,7 @@ int density_items(derek_gpu *h, const void *psi, double *rho) {
                             h->d_partial_off, h->stream);
   }
   for (int s = 0; s < h->nsys; ++s)
-    k_reduce_partials<<<152, 256, 0, h->stream>>>(h->d_sys, h->d_ks, s, h->d_partial,
+    derek::note_launch(), k_reduce_partials<<<152, 256, 0, h->stream>>>(h->d_sys, h->d_ks, s, h->d_partial,
                                                   h->d_partial_off, rho);
   DEREK_CUDA(h, cudaGetLastError());
   return DEREK_OK;
@@ -84,7 +89,7 @@ int density_items(derek_gpu *h, const void *psi, double *rho) {
 
 int refresh_vloc32(derek_gpu *h) {
   if (h->prec != DEREK_PREC_FP64)
-    k_to_float<<<152 * 4, 256, 0, h->stream>>>(h->total_grid, h->d_vloc, h->d_vloc32);
+    derek::note_launch(), k_to_float<<<152 * 4, 256, 0, h->stream>>>(h->total_grid, h->d_vloc, h->d_vloc32);
   DEREK_CUDA(h, cudaGetLastError());
   return DEREK_OK;
 }
@@ -121,6 +126,8 @@ void derek_gpu_default_opts(derek_scf_opts *o) {
   o->seed = 20240101ULL;
   o->use_graph = 1;
   o->use_tensor_cores = 1;
+  o->density_tol = 0.0;
+  o->buffer_bands = -1;
 }
 
 const char *derek_gpu_strerror(int s) {
@@ -252,7 +259,10 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     h->max_plane_yz = std::max(h->max_plane_yz, nfine[1] * nfine[2]);
     S.nr = nfine[0] * nfine[1] * nfine[2];
     S.nk = d.nk;
-    S.nb = d.nbands;
+    const int nbuf = h->opts.buffer_bands >= 0 ? h->opts.buffer_bands : std::max(4, (d.nbands + 9) / 10);
+    const int nbi = d.nbands + nbuf;
+    S.nb = nbi;
+    S.nbr = d.nbands;
     S.ks0 = (int)h->ks.size();
     S.active = 1;
     S.volume = cell_volume(d.cell);
@@ -261,7 +271,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     S.kT = d.kT;
     S.grid_off = grid_off;
     grid_off += S.nr;
-    h->max_nb = std::max(h->max_nb, d.nbands);
+    h->max_nb = std::max(h->max_nb, nbi);
 
     std::vector<double> v;
     if (d.vext)
@@ -274,13 +284,14 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       Sphere sp;
       build_sphere(inv, d.ecut, d.kpts + 3 * k, nstd, sp);
       const int npw = (int)sp.box_row.size();
-      if (npw < d.nbands) FAIL(DEREK_ERR_BAD_ARG, "fewer plane waves than bands");
+      if (npw < nbi) FAIL(DEREK_ERR_BAD_ARG, "fewer plane waves than bands");
       KSetDev K{};
       K.sys = s;
       K.kidx = k;
       K.npw = npw;
       K.npw_pad = (npw + 31) / 32 * 32;
-      K.nb = d.nbands;
+      K.nb = nbi;
+      K.nbr = d.nbands;
       K.wk = d.wk ? d.wk[k] : 1.0 / d.nk;
       for (int i = 0; i < 3; ++i) K.kfrac[i] = d.kpts[3 * k + i];
       const int mxmin = sp.mx.front(), mxmax = sp.mx.back();
@@ -329,15 +340,15 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       ent_off += npw;
       plane_off += K.nxr + 1;
       row_off = (long long)rows.size();
-      psi_off += (long long)d.nbands * K.npw_pad;
-      t_off += (long long)d.nbands * K.nxr * nfine[1] * nfine[2];
+      psi_off += (long long)nbi * K.npw_pad;
+      t_off += (long long)nbi * K.nxr * nfine[1] * nfine[2];
       partial_off.push_back(part_off);
       part_off += S.nr;
-      for (int b = 0; b < d.nbands; ++b) {
+      for (int b = 0; b < nbi; ++b) {
         h->item_ks.push_back((int)h->ks.size());
         h->item_band.push_back(b);
       }
-      h->nitems += d.nbands;
+      h->nitems += nbi;
       h->ks.push_back(K);
     }
     h->sys.push_back(S);
@@ -435,6 +446,13 @@ int derek_gpu_grid(derek_gpu_t *h, int s, int n_fine[3], int n_std[3]) {
   return DEREK_OK;
 }
 
+int derek_gpu_bands(derek_gpu_t *h, int s, int *nb, int *nbi) {
+  if (!check_sys(h, s)) return DEREK_ERR_BAD_ARG;
+  if (nb) *nb = h->sys[s].nbr;
+  if (nbi) *nbi = h->sys[s].nb;
+  return DEREK_OK;
+}
+
 int derek_gpu_npw(derek_gpu_t *h, int s, int k, int *npw) {
   int ki = ks_index(h, s, k);
   if (ki < 0 || !npw) return DEREK_ERR_BAD_ARG;
@@ -490,22 +508,23 @@ int derek_gpu_get_vloc(derek_gpu_t *h, int s, double *v) {
   return DEREK_OK;
 }
 
-// copy between a host complex128 [nb][npw] slice and a padded device buffer
+// copy between a host complex128 [nbr][npw] slice and a padded device buffer
+// (only the requested bands; buffer bands stay on the device)
 static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool to_dev) {
   const KSetDev &K = h->ks[ki];
   const size_t es = h->elem_size();
   char *dev = (char *)dev_base + (size_t)K.psi_off * es;
-  const size_t n = (size_t)K.nb * K.npw_pad;
+  const int nb = K.nbr;
+  const size_t n = (size_t)nb * K.npw_pad;
   if (h->prec == DEREK_PREC_FP64) {
     DEREK_CUDA(h, cudaMemcpy2DAsync(to_dev ? (void *)dev : (void *)host,
                                     to_dev ? K.npw_pad * 16 : K.npw * 16,
                                     to_dev ? (const void *)host : (const void *)dev,
-                                    to_dev ? K.npw * 16 : K.npw_pad * 16, K.npw * 16, K.nb,
+                                    to_dev ? K.npw * 16 : K.npw_pad * 16, K.npw * 16, nb,
                                     to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
                                     h->stream));
     if (to_dev) {
-      // zero the padding
-      for (int b = 0; b < K.nb && K.npw_pad > K.npw; ++b)
+      for (int b = 0; b < nb && K.npw_pad > K.npw; ++b)
         DEREK_CUDA(h, cudaMemsetAsync(dev + ((size_t)b * K.npw_pad + K.npw) * es, 0,
                                       (size_t)(K.npw_pad - K.npw) * es, h->stream));
     }
@@ -514,7 +533,7 @@ static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool
   }
   std::vector<float> tmp(2 * n, 0.0f);
   if (to_dev) {
-    for (int b = 0; b < K.nb; ++b)
+    for (int b = 0; b < nb; ++b)
       for (int g = 0; g < K.npw; ++g) {
         tmp[2 * ((size_t)b * K.npw_pad + g)] = (float)host[2 * ((size_t)b * K.npw + g)];
         tmp[2 * ((size_t)b * K.npw_pad + g) + 1] = (float)host[2 * ((size_t)b * K.npw + g) + 1];
@@ -524,7 +543,7 @@ static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool
   } else {
     DEREK_CUDA(h, cudaMemcpyAsync(tmp.data(), dev, n * es, cudaMemcpyDeviceToHost, h->stream));
     DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
-    for (int b = 0; b < K.nb; ++b)
+    for (int b = 0; b < nb; ++b)
       for (int g = 0; g < K.npw; ++g) {
         host[2 * ((size_t)b * K.npw + g)] = tmp[2 * ((size_t)b * K.npw_pad + g)];
         host[2 * ((size_t)b * K.npw + g) + 1] = tmp[2 * ((size_t)b * K.npw_pad + g) + 1];
@@ -561,7 +580,7 @@ int derek_gpu_density(derek_gpu_t *h, int s, const double *occ, double *rho) {
   std::vector<double> w(h->nitems, 0.0);
   for (int k = 0; k < S.nk; ++k) {
     const KSetDev &K = h->ks[S.ks0 + k];
-    for (int b = 0; b < K.nb; ++b) w[K.item0 + b] = K.wk * occ[(size_t)k * S.nb + b] / S.volume;
+    for (int b = 0; b < K.nbr; ++b) w[K.item0 + b] = K.wk * occ[(size_t)k * S.nbr + b] / S.volume;
   }
   // other systems are masked off for the duration of the call
   std::vector<SysDev> masked = h->sys;
@@ -611,6 +630,72 @@ int derek_host_gsphere(const double inv_cell[9], double ecut, const double kfrac
   *npw = (int)sp.box_row.size();
   if (box_rows)
     for (int i = 0; i < *npw && i < capacity; ++i) box_rows[i] = sp.box_row[i];
+  return DEREK_OK;
+}
+
+int derek_gpu_set_vext(derek_gpu_t *h, int s, const double *v) {
+  if (!check_sys(h, s) || !v) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_vext + S.grid_off, v, (size_t)S.nr * sizeof(double),
+                                cudaMemcpyHostToDevice, h->stream));
+  std::copy(v, v + S.nr, h->vext_host.begin() + S.grid_off);
+  h->scf_started = false;
+  return DEREK_OK;
+}
+
+int derek_gpu_get_vext(derek_gpu_t *h, int s, double *v) {
+  if (!check_sys(h, s) || !v) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  std::copy(h->vext_host.begin() + S.grid_off, h->vext_host.begin() + S.grid_off + S.nr, v);
+  return DEREK_OK;
+}
+
+void *derek_gpu_stream(derek_gpu_t *h) { return h ? (void *)h->stream : nullptr; }
+
+unsigned long long derek_gpu_launch_count(void) { return launch_total(); }
+
+int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage) {
+  if (!h || nrep <= 0) return DEREK_ERR_BAD_ARG;
+  cudaEvent_t ev[4];
+  for (auto &e : ev) DEREK_CUDA(h, cudaEventCreate(&e));
+  double tot[3] = {0, 0, 0};
+  const void *in = h->cur_psi();
+  for (int r = 0; r < nrep; ++r) {
+    cudaEventRecord(ev[0], h->stream);
+    if (h->prec == DEREK_PREC_FP64) {
+      launch_inv_yz<double>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const double2 *)in,
+                            (double2 *)h->d_planes, nullptr, h->stream);
+      cudaEventRecord(ev[1], h->stream);
+      launch_vmul_x<double>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
+                            (double2 *)h->d_planes, h->d_vloc, h->stream);
+      cudaEventRecord(ev[2], h->stream);
+      launch_fwd_yz<double>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz,
+                            (const double2 *)h->d_planes, (const double2 *)in, nullptr,
+                            (double2 *)h->d_HX, nullptr, h->stream);
+    } else {
+      launch_inv_yz<float>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const float2 *)in,
+                           (float2 *)h->d_planes, nullptr, h->stream);
+      cudaEventRecord(ev[1], h->stream);
+      launch_vmul_x<float>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
+                           (float2 *)h->d_planes, h->d_vloc32, h->stream);
+      cudaEventRecord(ev[2], h->stream);
+      launch_fwd_yz<float>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz,
+                           (const float2 *)h->d_planes, (const float2 *)in, nullptr,
+                           (float2 *)h->d_HX, nullptr, h->stream);
+    }
+    cudaEventRecord(ev[3], h->stream);
+    DEREK_CUDA(h, cudaEventSynchronize(ev[3]));
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      tot[k] += ms;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  DEREK_CUDA(h, cudaGetLastError());
+  if (ms_apply) *ms_apply = (tot[0] + tot[1] + tot[2]) / nrep;
+  if (ms_stage)
+    for (int k = 0; k < 3; ++k) ms_stage[k] = tot[k] / nrep;
   return DEREK_OK;
 }
 

@@ -51,7 +51,8 @@ struct SysDev {
   int n[3];
   int nr;
   int nk;
-  int nb;
+  int nb;                  // bands carried (requested + buffer)
+  int nbr;                 // bands requested and reported
   int ks0;                 // first k-set index of this system
   int active;              // 0 once converged (work items exit early)
   double volume;
@@ -69,7 +70,8 @@ struct KSetDev {
   int kidx;
   int npw;
   int npw_pad;
-  int nb;
+  int nb;                  // bands carried (requested + buffer)
+  int nbr;                 // bands requested and reported
   int nxr;                 // number of x-planes spanned by the sphere
   int mx_min;              // Miller x of plane 0
   int item0;               // first (k-set, band) item of this k-set
@@ -81,6 +83,11 @@ struct KSetDev {
   double wk;
   double kfrac[3];
 };
+
+// Host-side count of kernel launches issued by the library (every launch
+// site calls note_launch; a CUDA graph replay adds its captured kernel count).
+void note_launch(long long n = 1);
+unsigned long long launch_total();
 
 // Error codes mirrored from the C ABI.
 enum Status : int {

@@ -66,13 +66,13 @@ void launch_fft3d_grid(const Tables &t, int sys_begin, int nsys, int max_n, doub
   if (sign < 0) {
     cudaFuncSetAttribute(k_grid_yz<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     cudaFuncSetAttribute(k_grid_x<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_grid_yz<-1><<<grid, 256, sm, st>>>(t, sys_begin, data);
-    k_grid_x<-1><<<grid, 256, sm, st>>>(t, sys_begin, data);
+    derek::note_launch(), k_grid_yz<-1><<<grid, 256, sm, st>>>(t, sys_begin, data);
+    derek::note_launch(), k_grid_x<-1><<<grid, 256, sm, st>>>(t, sys_begin, data);
   } else {
     cudaFuncSetAttribute(k_grid_yz<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     cudaFuncSetAttribute(k_grid_x<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_grid_yz<1><<<grid, 256, sm, st>>>(t, sys_begin, data);
-    k_grid_x<1><<<grid, 256, sm, st>>>(t, sys_begin, data);
+    derek::note_launch(), k_grid_yz<1><<<grid, 256, sm, st>>>(t, sys_begin, data);
+    derek::note_launch(), k_grid_x<1><<<grid, 256, sm, st>>>(t, sys_begin, data);
   }
 }
 
@@ -90,7 +90,7 @@ void launch_lda(long n, const double *rho, double *exc, double *vxc, cudaStream_
   if (n <= 0) return;
   long blocks = (n + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  k_lda<<<(int)blocks, 256, 0, st>>>(n, rho, exc, vxc);
+  derek::note_launch(), k_lda<<<(int)blocks, 256, 0, st>>>(n, rho, exc, vxc);
 }
 
 }  // namespace derek

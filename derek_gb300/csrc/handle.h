@@ -80,6 +80,7 @@ struct derek_gpu {
   std::vector<long long> mat_off;
   cudaGraphExec_t graph_exec[3] = {nullptr, nullptr, nullptr};  // keyed by starting buffer
   int graph_degree = -1;
+  long long graph_nodes[3] = {0, 0, 0};
 
   cudaStream_t stream = nullptr;
   std::string last_error;

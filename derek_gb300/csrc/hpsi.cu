@@ -246,7 +246,7 @@ void launch_inv_yz(const Tables &t, int item_begin, int nitems, int max_nxr, int
   size_t sm = smem_yz<R>(max_plane);
   cudaFuncSetAttribute(k_inv_yz<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid(nitems, max_nxr);
-  k_inv_yz<R><<<grid, 256, sm, st>>>(t, item_begin, psi, planes, occ_skip);
+  derek::note_launch(), k_inv_yz<R><<<grid, 256, sm, st>>>(t, item_begin, psi, planes, occ_skip);
 }
 
 template <typename R>
@@ -256,7 +256,7 @@ void launch_vmul_x(const Tables &t, int item_begin, int nitems, int max_n1, int 
   size_t sm = (2 * (size_t)max_n1 * max_n3 + kMaxDim) * sizeof(cplx<R>);
   cudaFuncSetAttribute(k_vmul_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid(nitems, max_n2);
-  k_vmul_x<R><<<grid, 256, sm, st>>>(t, item_begin, planes, vloc);
+  derek::note_launch(), k_vmul_x<R><<<grid, 256, sm, st>>>(t, item_begin, planes, vloc);
 }
 
 template <typename R>
@@ -267,7 +267,7 @@ void launch_fwd_yz(const Tables &t, int item_begin, int nitems, int max_nxr, int
   size_t sm = smem_yz<R>(max_plane);
   cudaFuncSetAttribute(k_fwd_yz<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid(nitems, max_nxr);
-  k_fwd_yz<R><<<grid, 256, sm, st>>>(t, item_begin, planes, psi, prev, out, coef);
+  derek::note_launch(), k_fwd_yz<R><<<grid, 256, sm, st>>>(t, item_begin, planes, psi, prev, out, coef);
 }
 
 template <typename R>
@@ -279,7 +279,7 @@ void launch_density_x(const Tables &t, int ks_begin, int nks, int max_n1, int ma
   size_t sm = np * sizeof(double) + (2 * np + kMaxDim) * sizeof(cplx<R>);
   cudaFuncSetAttribute(k_density_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid(nks, max_n2);
-  k_density_x<R><<<grid, 256, sm, st>>>(t, ks_begin, planes, occ, partial, partial_off);
+  derek::note_launch(), k_density_x<R><<<grid, 256, sm, st>>>(t, ks_begin, planes, occ, partial, partial_off);
 }
 
 #define DEREK_INST(R)                                                                          \

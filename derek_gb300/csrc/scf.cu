@@ -157,20 +157,27 @@ int steady_iteration(derek_gpu *h) {
   const int start = h->cur;
   if (!h->graph_exec[start]) {
     cudaGraph_t g = nullptr;
+    const unsigned long long before = launch_total();
     DEREK_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int s = subspace_step(h, m);
     if (!s) s = finish_iteration(h);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    // captured launches run only when the graph is replayed
+    note_launch(-(long long)(launch_total() - before));
     if (s) {
       if (g) cudaGraphDestroy(g);
       return s;
     }
     if (e != cudaSuccess) return cuda_status(e, h, "graph capture");
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    h->graph_nodes[start] = (long long)nodes;
     e = cudaGraphInstantiate(&h->graph_exec[start], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_status(e, h, "graph instantiate");
   }
   DEREK_CUDA(h, cudaGraphLaunch(h->graph_exec[start], h->stream));
+  note_launch(h->graph_nodes[start]);
   h->cur = (start + m) % 3;
   return DEREK_OK;
 }
@@ -297,8 +304,10 @@ int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
                           (const float2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S,
                           h->d_mat_off, 0, h->stream);
   DEREK_CUDA(h, cudaGetLastError());
-  DEREK_CUDA(h, cudaMemcpyAsync(out, h->d_S + h->mat_off[ki], (size_t)K.nb * K.nb * sizeof(double2),
-                                cudaMemcpyDeviceToHost, h->stream));
+  // leading nbr x nbr block of the nb x nb matrix
+  DEREK_CUDA(h, cudaMemcpy2DAsync(out, (size_t)K.nbr * sizeof(double2), h->d_S + h->mat_off[ki],
+                                  (size_t)K.nb * sizeof(double2), (size_t)K.nbr * sizeof(double2),
+                                  K.nbr, cudaMemcpyDeviceToHost, h->stream));
   DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
   return DEREK_OK;
 }
@@ -345,9 +354,11 @@ int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol, derek_scf_report
 static int get_items(derek_gpu_t *h, int s, const double *src, double *out) {
   if (!h || s < 0 || s >= h->nsys || !out) return DEREK_ERR_BAD_ARG;
   const SysDev &S = h->sys[s];
+  // first nbr items of each k-point (the buffer bands are not reported)
   const KSetDev &K0 = h->ks[S.ks0];
-  DEREK_CUDA(h, cudaMemcpyAsync(out, src + K0.item0, (size_t)S.nk * S.nb * sizeof(double),
-                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaMemcpy2DAsync(out, (size_t)S.nbr * sizeof(double), src + K0.item0,
+                                  (size_t)S.nb * sizeof(double), (size_t)S.nbr * sizeof(double),
+                                  S.nk, cudaMemcpyDeviceToHost, h->stream));
   DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
   return DEREK_OK;
 }

@@ -111,7 +111,8 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
   const int s = blockIdx.x;
   const SysDev &S = t.sys[s];
   if (!S.active) return;
-  const int nb = S.nb, nk = S.nk;
+  // only the requested bands are occupied; the buffer bands get f = 0
+  const int nb = S.nbr, nk = S.nk;
   const int ntot = nb * nk;
   const double kT = S.kT, ne = S.nelec;
   // bracket
@@ -170,6 +171,13 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
     if (s_done) break;
   }
   const double mu = s_mu;
+  for (int i = threadIdx.x; i < nk * S.nb; i += blockDim.x) {
+    const KSetDev &K = t.ks[S.ks0 + i / S.nb];
+    if (i % S.nb >= nb) {
+      occ[K.item0 + i % S.nb] = 0.0;
+      occw[K.item0 + i % S.nb] = 0.0;
+    }
+  }
   double ent = 0, eb = 0;
   for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
     const KSetDev &K = t.ks[S.ks0 + i / nb];
@@ -534,43 +542,43 @@ __global__ void __launch_bounds__(256) k_uniform_density(const Tables t, double 
 // ---------------------------------------------------------------------------
 template <typename R>
 void launch_init_psi(const Tables &t, int nitems, void *X, unsigned long long seed, cudaStream_t st) {
-  k_init_psi<R><<<nitems, 256, 0, st>>>(t, (cplx<R> *)X, seed);
+  derek::note_launch(), k_init_psi<R><<<nitems, 256, 0, st>>>(t, (cplx<R> *)X, seed);
 }
 template void launch_init_psi<float>(const Tables &, int, void *, unsigned long long, cudaStream_t);
 template void launch_init_psi<double>(const Tables &, int, void *, unsigned long long, cudaStream_t);
 
 void launch_filter_coef(const Tables &t, int nks, const double *eig, const SysState *st, Axpby *coef,
                         int m, cudaStream_t s) {
-  k_filter_coef<<<(nks + 127) / 128, 128, 0, s>>>(t, nks, eig, st, coef, m);
+  derek::note_launch(), k_filter_coef<<<(nks + 127) / 128, 128, 0, s>>>(t, nks, eig, st, coef, m);
 }
 
 void launch_occupations(const Tables &t, int nsys, const double *eig, double *occ, double *occw,
                         SysState *st, cudaStream_t s) {
-  k_occupations<<<nsys, 1024, 0, s>>>(t, eig, occ, occw, st);
+  derek::note_launch(), k_occupations<<<nsys, 1024, 0, s>>>(t, eig, occ, occw, st);
 }
 
 void launch_energies(const Tables &t, int nsys, const double *vhxc, const double *rho_in,
                      const double *rho_out, const double2 *cgrid, double *part, SysState *st,
                      SysDev *sys_rw, const int *ks_status, cudaStream_t s) {
-  k_energy_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, vhxc, rho_in, rho_out, cgrid, part);
-  k_energy_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, sys_rw, ks_status);
+  derek::note_launch(), k_energy_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, vhxc, rho_in, rho_out, cgrid, part);
+  derek::note_launch(), k_energy_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, sys_rw, ks_status);
 }
 
 void launch_mix(const Tables &t, int nsys, int max_nr, double *rho_in, const double *rho_out,
                 double *nin_hist, double *res_hist, const long long *hist_off, SysState *st, int H,
                 double *part, double2 *cgrid, double alpha, double q0, int max_n, cudaStream_t s) {
   const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
-  k_mix_store<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, rho_out, nin_hist, res_hist, hist_off, st, H);
-  k_mix_gram_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, res_hist, hist_off, st, H, part);
-  k_mix_solve<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, H);
+  derek::note_launch(), k_mix_store<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, rho_out, nin_hist, res_hist, hist_off, st, H);
+  derek::note_launch(), k_mix_gram_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, res_hist, hist_off, st, H, part);
+  derek::note_launch(), k_mix_solve<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, H);
   const int kerker = q0 > 0;
-  k_mix_combine<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, nin_hist, res_hist, hist_off, st, cgrid,
+  derek::note_launch(), k_mix_combine<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, nin_hist, res_hist, hist_off, st, cgrid,
                                                alpha, kerker);
   if (kerker) {
     launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
-    k_kerker_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, alpha, q0);
+    derek::note_launch(), k_kerker_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, alpha, q0);
     launch_fft3d_grid(t, 0, nsys, max_n, cgrid, +1, s);
-    k_add_real<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, cgrid);
+    derek::note_launch(), k_add_real<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, cgrid);
   }
 }
 
@@ -578,24 +586,24 @@ void launch_potential(const Tables &t, int nsys, int max_nr, int max_n, const do
                       double2 *cgrid, const double *vext, double *vhxc, double *vloc, float *vloc32,
                       double *part, SysState *st, int all, cudaStream_t s) {
   const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
-  k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, cgrid, all);
+  derek::note_launch(), k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, cgrid, all);
   launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
-  k_hartree_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, all);
+  derek::note_launch(), k_hartree_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, all);
   launch_fft3d_grid(t, 0, nsys, max_n, cgrid, +1, s);
-  k_build_vloc<<<dim3(RB, nsys), 256, 0, s>>>(t, rho_in, cgrid, vext, vhxc, vloc, vloc32, part, all);
-  k_vmax_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, all);
+  derek::note_launch(), k_build_vloc<<<dim3(RB, nsys), 256, 0, s>>>(t, rho_in, cgrid, vext, vhxc, vloc, vloc32, part, all);
+  derek::note_launch(), k_vmax_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, all);
 }
 
 void launch_density_fft(const Tables &t, int nsys, int max_nr, int max_n, const double *rho,
                         double2 *cgrid, cudaStream_t s) {
   const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
-  k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho, cgrid, 0);
+  derek::note_launch(), k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho, cgrid, 0);
   launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
 }
 
 void launch_uniform_density(const Tables &t, int nsys, int max_nr, double *rho, cudaStream_t s) {
   const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
-  k_uniform_density<<<dim3(gx, nsys), 256, 0, s>>>(t, rho);
+  derek::note_launch(), k_uniform_density<<<dim3(gx, nsys), 256, 0, s>>>(t, rho);
 }
 
 }  // namespace derek

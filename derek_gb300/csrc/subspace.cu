@@ -407,8 +407,8 @@ void launch_overlap(const Tables &t, int ks_begin, int nks, int max_nb, int max_
   if (nks <= 0) return;
   const int nt = (max_nb + OT - 1) / OT;
   dim3 grid(nt * nt, (max_npw + ksplit - 1) / ksplit, nks);
-  k_overlap_partial<R><<<grid, 256, 0, st>>>(t, ks_begin, A, B, part, part_off, ksplit);
-  k_overlap_reduce<<<nks, 256, 0, st>>>(t, ks_begin, part, part_off, ksplit, out, mat_off, hermitize);
+  derek::note_launch(), k_overlap_partial<R><<<grid, 256, 0, st>>>(t, ks_begin, A, B, part, part_off, ksplit);
+  derek::note_launch(), k_overlap_reduce<<<nks, 256, 0, st>>>(t, ks_begin, part, part_off, ksplit, out, mat_off, hermitize);
 }
 
 template <typename R>
@@ -418,7 +418,7 @@ void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_n
   const size_t sm = (RI * RG + (size_t)RI * max_nb) * sizeof(cplx<R>);
   cudaFuncSetAttribute(k_rotate<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((max_npw + RG - 1) / RG, nks);
-  k_rotate<R><<<grid, 256, sm, st>>>(t, ks_begin, X, C, mat_off);
+  derek::note_launch(), k_rotate<R><<<grid, 256, sm, st>>>(t, ks_begin, X, C, mat_off);
 }
 
 bool cholesky_fits_smem(int max_nb) { return 2 * (size_t)max_nb * max_nb * 16 <= 200 * 1024; }
@@ -431,7 +431,7 @@ void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, con
   const int use_smem = cholesky_fits_smem(max_nb);
   const size_t sm = use_smem ? 2 * (size_t)max_nb * max_nb * sizeof(double2) : 0;
   cudaFuncSetAttribute(k_cholesky_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_cholesky_inv<<<nks, 256, sm, st>>>(t, ks_begin, S, C, mat_off, scratch, status, use_smem);
+  derek::note_launch(), k_cholesky_inv<<<nks, 256, sm, st>>>(t, ks_begin, S, C, mat_off, scratch, status, use_smem);
 }
 
 void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
@@ -444,7 +444,7 @@ void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const dou
                     (size_t)ne / 2 * (2 * sizeof(double) + sizeof(double2) + 2 * sizeof(int)) +
                     (size_t)(ne + 1) * sizeof(int) + 64;
   cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_jacobi<<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps, tol,
+  derek::note_launch(), k_jacobi<<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps, tol,
                                  v_smem, sweeps_out);
 }
 

@@ -1,0 +1,84 @@
+"""Seeded synthetic inputs with the shapes of the benchmark workloads.
+
+Every workload is a cubic cell holding a uniform jellium background plus
+attractive Gaussian wells (depth U[1,3] Ha, width U[0.8,1.5] bohr, centres
+uniform in the cell), spin-unpolarised, Fermi-Dirac smearing kT = 0.01 Ha:
+
+  gamma_8e     L=10 bohr, Ecut=10 Ha, grid 32^3, Gamma only, 8 electrons in
+               8 bands, 4 wells, Pulay alpha=0.3
+  kpts64       L=16, Ecut=20, grid 72^3, 4x4x4 Monkhorst-Pack (64 k-points),
+               64 electrons in 80 bands, 16 wells, Kerker + Pulay
+  adjoint9k    L=12, Ecut=15, grid 48^3, Gamma + 2x2x2 (9 k-points), 16
+               electrons in 20 bands, 8 wells
+  uneven256    256 systems, L ~ U[8,20], Ecut=15, {2,3}-smooth grids, 2..64
+               electrons, 1..27 k-points, 2..12 wells
+
+The generator is numpy's PCG64 with the stated seed, so the inputs are the
+same on every machine.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import SystemSpec, DEREK_GRID_SMOOTH23
+
+
+def mp_grid(n):
+    """Monkhorst-Pack points k = i d - (1 + d)/2 (DEReK's io_kpoint_grid rule,
+    Source/io.f90:2016-2031), x outermost."""
+    out = []
+    d = [1.0 / x for x in n]
+    for a in range(1, n[0] + 1):
+        for b in range(1, n[1] + 1):
+            for c in range(1, n[2] + 1):
+                out.append([a * d[0] - (1 + d[0]) / 2, b * d[1] - (1 + d[1]) / 2,
+                            c * d[2] - (1 + d[2]) / 2])
+    return np.array(out)
+
+
+def wells(rng, count):
+    c = rng.random((count, 3))
+    dep = rng.uniform(1.0, 3.0, count)
+    wid = rng.uniform(0.8, 1.5, count)
+    return np.concatenate([c, dep[:, None], wid[:, None]], axis=1)
+
+
+def gamma_8e(seed=1):
+    rng = np.random.default_rng(seed)
+    return [SystemSpec(np.eye(3) * 10.0, 10.0, [[0, 0, 0]], 8, 8.0, kT=0.01, wells=wells(rng, 4),
+                       grid_policy=DEREK_GRID_SMOOTH23)], dict(mix_alpha=0.3, kerker_q0=0.0)
+
+
+def kpts64(seed=2):
+    rng = np.random.default_rng(seed)
+    return [SystemSpec(np.eye(3) * 16.0, 20.0, mp_grid((4, 4, 4)), 80, 64.0, kT=0.01,
+                       wells=wells(rng, 16), grid_policy=DEREK_GRID_SMOOTH23)], \
+        dict(mix_alpha=0.3, kerker_q0=0.8)
+
+
+def adjoint9k(seed=3):
+    rng = np.random.default_rng(seed)
+    k = np.concatenate([[[0.0, 0.0, 0.0]], mp_grid((2, 2, 2))])
+    return [SystemSpec(np.eye(3) * 12.0, 15.0, k, 20, 16.0, kT=0.01, wells=wells(rng, 8),
+                       grid_policy=DEREK_GRID_SMOOTH23)], dict(mix_alpha=0.3, kerker_q0=0.0)
+
+
+def uneven(count=256, seed=5):
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(count):
+        L = rng.uniform(8.0, 20.0)
+        ne = int(rng.integers(2, 65))
+        ne += ne % 2
+        nb = ne // 2 + max(4, ne // 8)
+        while True:
+            kg = tuple(int(x) for x in rng.integers(1, 4, 3))
+            if np.prod(kg) <= 27:
+                break
+        specs.append(SystemSpec(np.eye(3) * L, 15.0, mp_grid(kg), nb, float(ne), kT=0.01,
+                                wells=wells(rng, int(rng.integers(2, 13))),
+                                grid_policy=DEREK_GRID_SMOOTH23))
+    return specs, dict(mix_alpha=0.3, kerker_q0=0.8)
+
+
+WORKLOADS = {"gamma_8e": gamma_8e, "kpts64": kpts64, "adjoint9k": adjoint9k, "uneven256": uneven}

@@ -93,6 +93,8 @@ typedef struct {
   int    use_tensor_cores; /* mixed mode: tcgen05 BF16x3 contractions */
   double density_tol;      /* also require max|n_out - n_in| < density_tol
                               (0 = energy criterion only, as the reference) */
+  int    buffer_bands;     /* extra unreported bands carried by the filtered
+                              subspace (-1 = max(4, nbands/10)) */
 } derek_scf_opts;
 
 /* Per-system SCF report (Source/electronic.f90:143-146 table row). */
@@ -121,8 +123,10 @@ int derek_gpu_create(derek_gpu_t **h, const derek_sys_desc *sys, int nsys,
                      const derek_scf_opts *opts);
 int derek_gpu_destroy(derek_gpu_t *h);
 
-/* Sizes: fine grid, standard box and sphere size of (sys, k). */
+/* Sizes: fine grid, standard box and sphere size of (sys, k); bands as
+ * requested and as carried internally (requested + buffer). */
 int derek_gpu_grid(derek_gpu_t *h, int sys, int n_fine[3], int n_std[3]);
+int derek_gpu_bands(derek_gpu_t *h, int sys, int *nbands, int *nbands_internal);
 int derek_gpu_npw(derek_gpu_t *h, int sys, int k, int *npw);
 
 /* Sphere of (sys, k): 0-based row numbers into the standard-box G list
@@ -170,6 +174,22 @@ int derek_gpu_overlap(derek_gpu_t *h, int sys, int k, double *s);
 int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep);
 int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol,
                       derek_scf_report *rep);
+
+/* Replace the external potential of sys (nr FP64 values); the next SCF run
+ * starts from it.  The reference's pot_external_pot (Source/pot.f90:104-190)
+ * fills ext_pot the same way before state_init hands it to the SCF. */
+int derek_gpu_set_vext(derek_gpu_t *h, int sys, const double *vext);
+int derek_gpu_get_vext(derek_gpu_t *h, int sys, double *vext);
+
+/* Measurement hooks.  derek_gpu_stream returns the handle's cudaStream_t;
+ * derek_gpu_launch_count the number of kernels the library has launched in
+ * this process (graph replays count their kernels); derek_gpu_time_apply_h
+ * runs H.psi on every band of every k-point nrep times and returns the mean
+ * device time per application and per stage kernel (3 values: scatter +
+ * backward yz transforms, x transforms with V(r), forward yz + gather). */
+void *derek_gpu_stream(derek_gpu_t *h);
+unsigned long long derek_gpu_launch_count(void);
+int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage);
 
 /* Results of the last SCF iteration. */
 int derek_gpu_get_eigenvalues(derek_gpu_t *h, int sys, double *eig /* nk*nb */);
