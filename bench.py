@@ -153,7 +153,7 @@ def run_ours(args):
     if not args.skip_fp64:
         with dg.Handle(specs, precision=dg.DEREK_PREC_FP64, **scf_opts) as h64:
             t = time.time()
-            rep64 = h64.electronic_scf(max_scf=100, etol=ETOL * 1e-2)
+            rep64 = h64.electronic_scf(max_scf=100, etol=ETOL * 1e-1)
             f64 = [r["free_energy"] for r in rep64]
             fp64_seconds = time.time() - t
 
