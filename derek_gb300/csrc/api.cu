@@ -43,43 +43,41 @@ __global__ void k_to_float(long long n, const double *__restrict__ a, float *__r
     b[i] = (float)a[i];
 }
 
+template <typename R>
+static void apply_h_t(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
+                      void *out, const Axpby *coef, const R *vloc) {
+  launch_x_inv<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0], (const cplx<R> *)in,
+                  (cplx<R> *)h->d_abuf, nullptr, h->stream);
+  launch_plane<R>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2],
+                  (cplx<R> *)h->d_abuf, vloc, h->stream);
+  launch_x_fwd<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0],
+                  (const cplx<R> *)h->d_abuf, (const cplx<R> *)in, (const cplx<R> *)prev,
+                  (cplx<R> *)out, coef, h->stream);
+}
+
 int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
                   void *out, const Axpby *coef) {
-  if (h->prec == DEREK_PREC_FP64) {
-    launch_inv_yz<double>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
-                          (const double2 *)in, (double2 *)h->d_planes, nullptr, h->stream);
-    launch_vmul_x<double>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2],
-                          (double2 *)h->d_planes, h->d_vloc, h->stream);
-    launch_fwd_yz<double>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
-                          (const double2 *)h->d_planes, (const double2 *)in,
-                          (const double2 *)prev, (double2 *)out, coef, h->stream);
-  } else {
-    launch_inv_yz<float>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
-                         (const float2 *)in, (float2 *)h->d_planes, nullptr, h->stream);
-    launch_vmul_x<float>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2],
-                         (float2 *)h->d_planes, h->d_vloc32, h->stream);
-    launch_fwd_yz<float>(h->tab, item_begin, nitems, h->max_nxr, h->max_plane_yz,
-                         (const float2 *)h->d_planes, (const float2 *)in, (const float2 *)prev,
-                         (float2 *)out, coef, h->stream);
-  }
+  if (h->prec == DEREK_PREC_FP64)
+    apply_h_t<double>(h, item_begin, nitems, in, prev, out, coef, h->d_vloc);
+  else
+    apply_h_t<float>(h, item_begin, nitems, in, prev, out, coef, h->d_vloc32);
   DEREK_CUDA(h, cudaGetLastError());
   return DEREK_OK;
 }
 
+template <typename R> static void density_t(derek_gpu *h, const void *psi) {
+  launch_x_inv<R>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const cplx<R> *)psi,
+                  (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
+  launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
+                          (const cplx<R> *)h->d_abuf, h->d_occw, h->d_partial, h->d_partial_off,
+                          h->stream);
+}
+
 int density_items(derek_gpu *h, const void *psi, double *rho) {
-  if (h->prec == DEREK_PREC_FP64) {
-    launch_inv_yz<double>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const double2 *)psi,
-                          (double2 *)h->d_planes, h->d_occw, h->stream);
-    launch_density_x<double>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
-                             (const double2 *)h->d_planes, h->d_occw, h->d_partial,
-                             h->d_partial_off, h->stream);
-  } else {
-    launch_inv_yz<float>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const float2 *)psi,
-                         (float2 *)h->d_planes, h->d_occw, h->stream);
-    launch_density_x<float>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
-                            (const float2 *)h->d_planes, h->d_occw, h->d_partial,
-                            h->d_partial_off, h->stream);
-  }
+  if (h->prec == DEREK_PREC_FP64)
+    density_t<double>(h, psi);
+  else
+    density_t<float>(h, psi);
   for (int s = 0; s < h->nsys; ++s)
     derek::note_launch(), k_reduce_partials<<<152, 256, 0, h->stream>>>(h->d_sys, h->d_ks, s, h->d_partial,
                                                   h->d_partial_off, rho);
@@ -151,12 +149,12 @@ const char *derek_gpu_last_error(derek_gpu_t *h) {
 
 int derek_gpu_destroy(derek_gpu_t *h) {
   if (!h) return DEREK_ERR_BAD_ARG;
-  void *ptrs[] = {h->d_sys,   h->d_ks,      h->d_item_ks, h->d_item_band, h->d_pidx,
-                  h->d_xstart, h->d_rowstart, h->d_rows,  h->d_kin64,     h->d_kin32,
+  void *ptrs[] = {h->d_sys,   h->d_ks,      h->d_item_ks, h->d_item_band, h->d_ent_col,
+                  h->d_col_start, h->d_ent_ix, h->d_col_y, h->d_col_z, h->d_rows,  h->d_kin64,     h->d_kin32,
                   h->d_tw64,  h->d_tw32,    h->d_vext,    h->d_vloc,      h->d_vhxc,
                   h->d_vloc32, h->d_rho_in, h->d_rho_out, h->d_exc,       h->d_vxc,
                   h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
-                  h->d_Yp,    h->d_HX,      h->d_planes,  h->d_occw,      h->d_eig,
+                  h->d_Yp,    h->d_HX,      h->d_abuf,    h->d_occw,      h->d_eig,
                   h->d_occ,   h->d_coef};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -196,14 +194,14 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   if (h->prec != DEREK_PREC_FP64 && h->prec != DEREK_PREC_MIXED) FAIL(DEREK_ERR_BAD_ARG, "precision");
   h->nsys = nsys;
 
-  std::vector<int> pidx, xstart, rowstart;
-  std::vector<short> rows;
+  std::vector<int> ent_col, col_start;
+  std::vector<short> ent_ix, col_y, col_z, rows;
   std::vector<float> kin32;
   std::vector<double> tw64;
   std::map<int, long long> tw_of;  // n -> offset
   std::vector<long long> partial_off;
 
-  long long grid_off = 0, psi_off = 0, ent_off = 0, plane_off = 0, row_off = 0, t_off = 0,
+  long long grid_off = 0, psi_off = 0, ent_off = 0, col_off = 0, row_off = 0, a_off = 0,
             part_off = 0;
   for (int s = 0; s < nsys; ++s) {
     const derek_sys_desc &d = desc[s];
@@ -231,10 +229,12 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       // the sphere must fit without wrapping onto itself
       if (nfine[i] < nstd[i]) FAIL(DEREK_ERR_BAD_ARG, "fine grid smaller than standard box");
     }
-    const size_t plane_bytes_max = (size_t)std::max({nfine[0] * nfine[2], nfine[1] * nfine[2]}) *
-                                   (h->prec == DEREK_PREC_FP64 ? 16 : 8);
-    if (2 * plane_bytes_max + 8 * (size_t)nfine[0] * nfine[2] + 4096 > 227 * 1024)
-      FAIL(DEREK_ERR_UNSUPPORTED, "grid planes exceed shared memory");
+    {
+      // density planes hold an FP64 accumulator plus one (y,z) plane
+      const size_t es = h->prec == DEREK_PREC_FP64 ? 16 : 8;
+      const size_t need = (size_t)nfine[1] * nfine[2] * 8 + ((size_t)nfine[1] * (nfine[2] + 1) + 2 * kMaxDim) * es;
+      if (need > 227 * 1024) FAIL(DEREK_ERR_UNSUPPORTED, "grid planes exceed shared memory");
+    }
     for (int i = 0; i < 3; ++i) {
       S.n[i] = nfine[i];
       h->n_std.push_back(nstd[i]);
@@ -244,6 +244,11 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       p.n = nfine[i];
       if (!radix_plan(nfine[i], p.radix, &p.nstages))
         FAIL(DEREK_ERR_UNSUPPORTED, "grid size " + std::to_string(nfine[i]) + " not 13-smooth");
+      LinePlan &lp = S.lp[i];
+      lp.n = nfine[i];
+      if (!line_plan(nfine[i], &lp.a, &lp.b))
+        FAIL(DEREK_ERR_UNSUPPORTED, "grid size " + std::to_string(nfine[i]) + " has no a*b <= 16*16 split");
+      lp.group = 32 / std::max(lp.a, lp.b);
       auto it = tw_of.find(nfine[i]);
       if (it == tw_of.end()) {
         std::vector<double> w;
@@ -255,8 +260,8 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       } else {
         p.tw_off = it->second;
       }
+      S.lp[i].tw_off = p.tw_off;
     }
-    h->max_plane_yz = std::max(h->max_plane_yz, nfine[1] * nfine[2]);
     S.nr = nfine[0] * nfine[1] * nfine[2];
     S.nk = d.nk;
     const int nbuf = h->opts.buffer_bands >= 0 ? h->opts.buffer_bands : std::max(4, (d.nbands + 9) / 10);
@@ -294,39 +299,45 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       K.nbr = d.nbands;
       K.wk = d.wk ? d.wk[k] : 1.0 / d.nk;
       for (int i = 0; i < 3; ++i) K.kfrac[i] = d.kpts[3 * k + i];
-      const int mxmin = sp.mx.front(), mxmax = sp.mx.back();
-      K.mx_min = mxmin;
-      K.nxr = mxmax - mxmin + 1;
-      if (K.nxr > nfine[0]) FAIL(DEREK_ERR_BAD_ARG, "sphere wider than the fine grid");
+      if (sp.mx.back() - sp.mx.front() + 1 > nfine[0]) FAIL(DEREK_ERR_BAD_ARG, "sphere wider than the fine grid");
       K.item0 = h->nitems;
       K.psi_off = psi_off;
       K.ent_off = ent_off;
-      K.plane_off = plane_off;
+      K.col_off = col_off;
       K.row_off = row_off;
-      K.t_off = t_off;
-      // per-entry tables; entries are sorted by mx (x outermost)
-      std::vector<int> xs(K.nxr + 1, 0), rsv(K.nxr + 1, 0);
-      int e = 0;
-      for (int j = 0; j < K.nxr; ++j) {
-        xs[j] = e;
-        rsv[j] = (int)(rows.size() - row_off);
-        int last_row = -1;
-        while (e < npw && sp.mx[e] == mxmin + j) {
-          const int iy = ((sp.my[e] % nfine[1]) + nfine[1]) % nfine[1];
-          const int iz = ((sp.mz[e] % nfine[2]) + nfine[2]) % nfine[2];
-          pidx.push_back(iy * nfine[2] + iz);
-          if (iy != last_row) {
-            // entries of one (mx,my) are contiguous, so each row appears once
-            rows.push_back((short)iy);
-            last_row = iy;
-          }
+      K.a_off = a_off;
+      // column order: (y,z) columns sorted by centred (my, mz), each a run of
+      // increasing mx (for a sphere the run is contiguous)
+      std::map<std::pair<int, int>, std::vector<int>> cols;
+      for (int i = 0; i < npw; ++i) cols[{sp.my[i], sp.mz[i]}].push_back(i);
+      K.ncol = (int)cols.size();
+      K.ncol_pad = (K.ncol + 15) / 16 * 16;
+      int c = 0, e = 0, last_row = -1;
+      std::vector<short> krows;
+      for (auto &kv : cols) {
+        const int iy = ((kv.first.first % nfine[1]) + nfine[1]) % nfine[1];
+        const int iz = ((kv.first.second % nfine[2]) + nfine[2]) % nfine[2];
+        col_start.push_back(e);
+        col_y.push_back((short)iy);
+        col_z.push_back((short)iz);
+        for (int ref : kv.second) {
+          const int ix = ((sp.mx[ref] % nfine[0]) + nfine[0]) % nfine[0];
+          ent_col.push_back(c);
+          ent_ix.push_back((short)ix);
+          h->perm.push_back(ref);
+          h->kin_col.push_back(sp.kinetic[ref]);
+          kin32.push_back((float)sp.kinetic[ref]);
           ++e;
         }
+        if (kv.first.first != last_row) {
+          krows.push_back((short)iy);
+          last_row = kv.first.first;
+        }
+        ++c;
       }
-      xs[K.nxr] = e;
-      rsv[K.nxr] = (int)(rows.size() - row_off);
-      xstart.insert(xstart.end(), xs.begin(), xs.end());
-      rowstart.insert(rowstart.end(), rsv.begin(), rsv.end());
+      col_start.push_back(e);
+      K.nrow = (int)krows.size();
+      rows.insert(rows.end(), krows.begin(), krows.end());
       for (int i = 0; i < npw; ++i) {
         const int ix = ((sp.mx[i] % nfine[0]) + nfine[0]) % nfine[0];
         const int iy = ((sp.my[i] % nfine[1]) + nfine[1]) % nfine[1];
@@ -334,14 +345,13 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
         h->box_rows.push_back(sp.box_row[i]);
         h->fft_index.push_back((ix * nfine[1] + iy) * nfine[2] + iz);
         h->kin64.push_back(sp.kinetic[i]);
-        kin32.push_back((float)sp.kinetic[i]);
       }
-      h->max_nxr = std::max(h->max_nxr, K.nxr);
+      h->max_nchunk = std::max(h->max_nchunk, (K.ncol + kColChunk - 1) / kColChunk);
       ent_off += npw;
-      plane_off += K.nxr + 1;
-      row_off = (long long)rows.size();
+      col_off += K.ncol + 1;
+      row_off += K.nrow;
       psi_off += (long long)nbi * K.npw_pad;
-      t_off += (long long)nbi * K.nxr * nfine[1] * nfine[2];
+      a_off += (long long)nbi * nfine[0] * K.ncol_pad;
       partial_off.push_back(part_off);
       part_off += S.nr;
       for (int b = 0; b < nbi; ++b) {
@@ -355,7 +365,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   }
   h->nks = (int)h->ks.size();
   h->total_psi = psi_off;
-  h->total_planes = t_off;
+  h->total_abuf = a_off;
   h->total_grid = grid_off;
   std::vector<float> tw32(tw64.begin(), tw64.end());
 
@@ -364,11 +374,13 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   CK(upload(&h->d_ks, h->ks));
   CK(upload(&h->d_item_ks, h->item_ks));
   CK(upload(&h->d_item_band, h->item_band));
-  CK(upload(&h->d_pidx, pidx));
-  CK(upload(&h->d_xstart, xstart));
-  CK(upload(&h->d_rowstart, rowstart));
+  CK(upload(&h->d_ent_col, ent_col));
+  CK(upload(&h->d_ent_ix, ent_ix));
+  CK(upload(&h->d_col_start, col_start));
+  CK(upload(&h->d_col_y, col_y));
+  CK(upload(&h->d_col_z, col_z));
   CK(upload(&h->d_rows, rows));
-  CK(upload(&h->d_kin64, h->kin64));
+  CK(upload(&h->d_kin64, h->kin_col));
   CK(upload(&h->d_kin32, kin32));
   {
     std::vector<double2> t(tw64.size() / 2);
@@ -403,7 +415,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   CK(cudaMemset(h->d_Y, 0, pbytes));
   CK(cudaMemset(h->d_Yp, 0, pbytes));
   CK(cudaMemset(h->d_HX, 0, pbytes));
-  CK(cudaMalloc(&h->d_planes, (size_t)std::max<long long>(h->total_planes, 1) * h->elem_size()));
+  CK(cudaMalloc(&h->d_abuf, (size_t)std::max<long long>(h->total_abuf, 1) * h->elem_size()));
   CK(cudaMalloc((void **)&h->d_occw, (size_t)h->nitems * sizeof(double)));
   CK(cudaMalloc((void **)&h->d_eig, (size_t)h->nitems * sizeof(double)));
   CK(cudaMalloc((void **)&h->d_occ, (size_t)h->nitems * sizeof(double)));
@@ -415,11 +427,13 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   h->tab.ks = h->d_ks;
   h->tab.item_ks = h->d_item_ks;
   h->tab.item_band = h->d_item_band;
-  h->tab.pidx = h->d_pidx;
+  h->tab.ent_col = h->d_ent_col;
+  h->tab.ent_ix = h->d_ent_ix;
+  h->tab.col_start = h->d_col_start;
+  h->tab.col_y = h->d_col_y;
+  h->tab.col_z = h->d_col_z;
   h->tab.kin64 = h->d_kin64;
   h->tab.kin32 = h->d_kin32;
-  h->tab.xstart = h->d_xstart;
-  h->tab.rowstart = h->d_rowstart;
   h->tab.rows = h->d_rows;
   h->tab.tw64 = h->d_tw64;
   h->tab.tw32 = h->d_tw32;
@@ -508,45 +522,45 @@ int derek_gpu_get_vloc(derek_gpu_t *h, int s, double *v) {
   return DEREK_OK;
 }
 
-// copy between a host complex128 [nbr][npw] slice and a padded device buffer
-// (only the requested bands; buffer bands stay on the device)
+// copy between a host complex128 [nbr][npw] slice in the reference's G order
+// and the padded, column-ordered device buffer (only the requested bands;
+// buffer bands stay on the device)
 static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool to_dev) {
   const KSetDev &K = h->ks[ki];
   const size_t es = h->elem_size();
   char *dev = (char *)dev_base + (size_t)K.psi_off * es;
   const int nb = K.nbr;
   const size_t n = (size_t)nb * K.npw_pad;
-  if (h->prec == DEREK_PREC_FP64) {
-    DEREK_CUDA(h, cudaMemcpy2DAsync(to_dev ? (void *)dev : (void *)host,
-                                    to_dev ? K.npw_pad * 16 : K.npw * 16,
-                                    to_dev ? (const void *)host : (const void *)dev,
-                                    to_dev ? K.npw * 16 : K.npw_pad * 16, K.npw * 16, nb,
-                                    to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
-                                    h->stream));
-    if (to_dev) {
-      for (int b = 0; b < nb && K.npw_pad > K.npw; ++b)
-        DEREK_CUDA(h, cudaMemsetAsync(dev + ((size_t)b * K.npw_pad + K.npw) * es, 0,
-                                      (size_t)(K.npw_pad - K.npw) * es, h->stream));
-    }
-    DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
-    return DEREK_OK;
-  }
-  std::vector<float> tmp(2 * n, 0.0f);
+  const int32_t *perm = h->perm.data() + K.ent_off;
+  const bool f64 = h->prec == DEREK_PREC_FP64;
+  std::vector<double> t64(f64 ? 2 * n : 0, 0.0);
+  std::vector<float> t32(f64 ? 0 : 2 * n, 0.0f);
   if (to_dev) {
     for (int b = 0; b < nb; ++b)
       for (int g = 0; g < K.npw; ++g) {
-        tmp[2 * ((size_t)b * K.npw_pad + g)] = (float)host[2 * ((size_t)b * K.npw + g)];
-        tmp[2 * ((size_t)b * K.npw_pad + g) + 1] = (float)host[2 * ((size_t)b * K.npw + g) + 1];
+        const size_t src = 2 * ((size_t)b * K.npw + perm[g]);
+        const size_t dst = 2 * ((size_t)b * K.npw_pad + g);
+        if (f64) {
+          t64[dst] = host[src];
+          t64[dst + 1] = host[src + 1];
+        } else {
+          t32[dst] = (float)host[src];
+          t32[dst + 1] = (float)host[src + 1];
+        }
       }
-    DEREK_CUDA(h, cudaMemcpyAsync(dev, tmp.data(), n * es, cudaMemcpyHostToDevice, h->stream));
+    DEREK_CUDA(h, cudaMemcpyAsync(dev, f64 ? (void *)t64.data() : (void *)t32.data(), n * es,
+                                  cudaMemcpyHostToDevice, h->stream));
     DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
   } else {
-    DEREK_CUDA(h, cudaMemcpyAsync(tmp.data(), dev, n * es, cudaMemcpyDeviceToHost, h->stream));
+    DEREK_CUDA(h, cudaMemcpyAsync(f64 ? (void *)t64.data() : (void *)t32.data(), dev, n * es,
+                                  cudaMemcpyDeviceToHost, h->stream));
     DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
     for (int b = 0; b < nb; ++b)
       for (int g = 0; g < K.npw; ++g) {
-        host[2 * ((size_t)b * K.npw + g)] = tmp[2 * ((size_t)b * K.npw_pad + g)];
-        host[2 * ((size_t)b * K.npw + g) + 1] = tmp[2 * ((size_t)b * K.npw_pad + g) + 1];
+        const size_t dst = 2 * ((size_t)b * K.npw + perm[g]);
+        const size_t src = 2 * ((size_t)b * K.npw_pad + g);
+        host[dst] = f64 ? t64[src] : (double)t32[src];
+        host[dst + 1] = f64 ? t64[src + 1] : (double)t32[src + 1];
       }
   }
   return DEREK_OK;
@@ -659,29 +673,34 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
   cudaEvent_t ev[4];
   for (auto &e : ev) DEREK_CUDA(h, cudaEventCreate(&e));
   double tot[3] = {0, 0, 0};
+  // converged systems are masked off on the device; time every system
+  std::vector<SysDev> all = h->sys;
+  for (auto &s : all) s.active = 1;
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, all.data(), all.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
   const void *in = h->cur_psi();
   for (int r = 0; r < nrep; ++r) {
     cudaEventRecord(ev[0], h->stream);
     if (h->prec == DEREK_PREC_FP64) {
-      launch_inv_yz<double>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const double2 *)in,
-                            (double2 *)h->d_planes, nullptr, h->stream);
+      launch_x_inv<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const double2 *)in,
+                           (double2 *)h->d_abuf, nullptr, h->stream);
       cudaEventRecord(ev[1], h->stream);
-      launch_vmul_x<double>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
-                            (double2 *)h->d_planes, h->d_vloc, h->stream);
+      launch_plane<double>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
+                           (double2 *)h->d_abuf, h->d_vloc, h->stream);
       cudaEventRecord(ev[2], h->stream);
-      launch_fwd_yz<double>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz,
-                            (const double2 *)h->d_planes, (const double2 *)in, nullptr,
-                            (double2 *)h->d_HX, nullptr, h->stream);
+      launch_x_fwd<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0],
+                           (const double2 *)h->d_abuf, (const double2 *)in, nullptr,
+                           (double2 *)h->d_HX, nullptr, h->stream);
     } else {
-      launch_inv_yz<float>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz, (const float2 *)in,
-                           (float2 *)h->d_planes, nullptr, h->stream);
+      launch_x_inv<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const float2 *)in,
+                          (float2 *)h->d_abuf, nullptr, h->stream);
       cudaEventRecord(ev[1], h->stream);
-      launch_vmul_x<float>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
-                           (float2 *)h->d_planes, h->d_vloc32, h->stream);
+      launch_plane<float>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
+                          (float2 *)h->d_abuf, h->d_vloc32, h->stream);
       cudaEventRecord(ev[2], h->stream);
-      launch_fwd_yz<float>(h->tab, 0, h->nitems, h->max_nxr, h->max_plane_yz,
-                           (const float2 *)h->d_planes, (const float2 *)in, nullptr,
-                           (float2 *)h->d_HX, nullptr, h->stream);
+      launch_x_fwd<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0],
+                          (const float2 *)h->d_abuf, (const float2 *)in, nullptr,
+                          (float2 *)h->d_HX, nullptr, h->stream);
     }
     cudaEventRecord(ev[3], h->stream);
     DEREK_CUDA(h, cudaEventSynchronize(ev[3]));

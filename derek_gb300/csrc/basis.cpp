@@ -131,6 +131,26 @@ bool radix_plan(int n, int radices[8], int *nstages) {
   return m == 1 && ns <= 8;
 }
 
+bool line_plan(int n, int *a, int *b) {
+  int best_a = 0, best_span = 1 << 30, best_pow2 = 0;
+  for (int x = 1; x <= 16; ++x) {
+    if (n % x) continue;
+    const int y = n / x;
+    if (y > 16) continue;
+    const int span = x > y ? x : y;
+    const int pow2 = (x & (x - 1)) == 0 && x > 1;
+    if (span < best_span || (span == best_span && pow2 > best_pow2)) {
+      best_a = x;
+      best_span = span;
+      best_pow2 = pow2;
+    }
+  }
+  if (!best_a) return false;
+  *a = best_a;
+  *b = n / best_a;
+  return true;
+}
+
 void twiddles(int n, std::vector<double> &out) {
   out.resize(2 * (size_t)n);
   const long double two_pi = 6.283185307179586476925286766559005768L;

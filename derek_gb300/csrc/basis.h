@@ -41,6 +41,10 @@ void build_sphere(const double inv_cell_cm[9], double ecut, const double kfrac[3
 // Returns false if n has another prime factor.
 bool radix_plan(int n, int radices[8], int *nstages);
 
+// Split n = a * b with a, b <= 16 for the four-step line kernels: the
+// smallest max(a, b), ties broken toward a power-of-two a.
+bool line_plan(int n, int *a, int *b);
+
 // exp(-2 pi i t / n), t = 0..n-1, interleaved (re, im).
 void twiddles(int n, std::vector<double> &out);
 

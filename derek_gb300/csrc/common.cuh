@@ -46,6 +46,13 @@ struct FftPlan {
   long long tw_off;   // offset of this length's twiddle table (n entries)
 };
 
+// Factorisation of one transform length for the four-step line kernels:
+// n = a * b with a, b <= 16; group = lines per warp (32 / max(a, b)).
+struct LinePlan {
+  int n, a, b, group;
+  long long tw_off;        // twiddle table exp(-2 pi i t / n), t < n
+};
+
 // One independent Kohn-Sham system of a batch.
 struct SysDev {
   int n[3];
@@ -61,10 +68,13 @@ struct SysDev {
   double nelec;
   double kT;
   long long grid_off;      // offset of this system's grids (nr entries)
-  FftPlan plan[3];
+  FftPlan plan[3];         // Stockham plans (full-grid transforms)
+  LinePlan lp[3];          // four-step plans (H.psi and density)
 };
 
-// One (system, k-point) pair: its plane-wave sphere and buffers.
+// One (system, k-point) pair: its plane-wave sphere and buffers.  The
+// sphere's coefficients are stored in column order: the ncol (y,z) columns
+// the sphere occupies, each a contiguous run of increasing Miller x.
 struct KSetDev {
   int sys;
   int kidx;
@@ -72,14 +82,15 @@ struct KSetDev {
   int npw_pad;
   int nb;                  // bands carried (requested + buffer)
   int nbr;                 // bands requested and reported
-  int nxr;                 // number of x-planes spanned by the sphere
-  int mx_min;              // Miller x of plane 0
+  int ncol;                // (y,z) columns of the sphere
+  int ncol_pad;
+  int nrow;                // distinct y rows holding columns
   int item0;               // first (k-set, band) item of this k-set
   long long psi_off;       // element offset of band 0 in psi-shaped buffers
   long long ent_off;       // offset into per-sphere-entry tables
-  long long plane_off;     // offset into per-plane tables (nxr + 1 entries)
-  long long row_off;       // offset into active-row lists
-  long long t_off;         // element offset of this k-set in the plane buffer
+  long long col_off;       // offset into per-column tables (ncol + 1 entries)
+  long long row_off;       // offset into the active-row lists
+  long long a_off;         // element offset in the x-line buffer (nb * n1 * ncol_pad)
   double wk;
   double kfrac[3];
 };

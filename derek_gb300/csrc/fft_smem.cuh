@@ -25,6 +25,16 @@ template <> struct RadixConst<5> {
     return t[m];
   }
 };
+template <> struct RadixConst<6> {
+  __device__ __forceinline__ static double c(int m) {
+    constexpr double t[6] = {1.0, 0.5, -0.5, -1.0, -0.5, 0.5};
+    return t[m];
+  }
+  __device__ __forceinline__ static double s(int m) {
+    constexpr double t[6] = {0.0, 0.866025403784438646764, 0.866025403784438646764, 0.00000000000000000000000000000000000000000041340642196527976473, -0.866025403784438646764, -0.866025403784438646764};
+    return t[m];
+  }
+};
 template <> struct RadixConst<7> {
   __device__ __forceinline__ static double c(int m) {
     constexpr double t[7] = {1.0, 0.623489801858733530525, -0.222520933956314404289, -0.900968867902419126236, -0.900968867902419126236, -0.222520933956314404289, 0.623489801858733530525};
@@ -32,6 +42,26 @@ template <> struct RadixConst<7> {
   }
   __device__ __forceinline__ static double s(int m) {
     constexpr double t[7] = {0.0, 0.781831482468029808708, 0.974927912181823607018, 0.433883739117558120476, -0.433883739117558120476, -0.974927912181823607018, -0.781831482468029808708};
+    return t[m];
+  }
+};
+template <> struct RadixConst<9> {
+  __device__ __forceinline__ static double c(int m) {
+    constexpr double t[9] = {1.0, 0.766044443118978035202, 0.173648177666930348852, -0.5, -0.939692620785908384054, -0.939692620785908384054, -0.5, 0.173648177666930348852, 0.766044443118978035202};
+    return t[m];
+  }
+  __device__ __forceinline__ static double s(int m) {
+    constexpr double t[9] = {0.0, 0.642787609686539326323, 0.984807753012208059367, 0.866025403784438646764, 0.342020143325668733044, -0.342020143325668733044, -0.866025403784438646764, -0.984807753012208059367, -0.642787609686539326323};
+    return t[m];
+  }
+};
+template <> struct RadixConst<10> {
+  __device__ __forceinline__ static double c(int m) {
+    constexpr double t[10] = {1.0, 0.809016994374947424102, 0.309016994374947424102, -0.309016994374947424102, -0.809016994374947424102, -1.0, -0.809016994374947424102, -0.309016994374947424102, 0.309016994374947424102, 0.809016994374947424102};
+    return t[m];
+  }
+  __device__ __forceinline__ static double s(int m) {
+    constexpr double t[10] = {0.0, 0.587785252292473129169, 0.951056516295153572116, 0.951056516295153572116, 0.587785252292473129169, 0.00000000000000000000000000000000000000000041340642196527976473, -0.587785252292473129169, -0.951056516295153572116, -0.951056516295153572116, -0.587785252292473129169};
     return t[m];
   }
 };
@@ -45,6 +75,16 @@ template <> struct RadixConst<11> {
     return t[m];
   }
 };
+template <> struct RadixConst<12> {
+  __device__ __forceinline__ static double c(int m) {
+    constexpr double t[12] = {1.0, 0.866025403784438646764, 0.5, 0.000000000000000000000000000000000000000000206703210982639882365, -0.5, -0.866025403784438646764, -1.0, -0.866025403784438646764, -0.5, 0.0000000000000000000000000000000000000000223387644065498832429, 0.5, 0.866025403784438646764};
+    return t[m];
+  }
+  __device__ __forceinline__ static double s(int m) {
+    constexpr double t[12] = {0.0, 0.5, 0.866025403784438646764, 1.0, 0.866025403784438646764, 0.5, 0.00000000000000000000000000000000000000000041340642196527976473, -0.5, -0.866025403784438646764, -1.0, -0.866025403784438646764, -0.5};
+    return t[m];
+  }
+};
 template <> struct RadixConst<13> {
   __device__ __forceinline__ static double c(int m) {
     constexpr double t[13] = {1.0, 0.8854560256532098959, 0.568064746731155802512, 0.120536680255323053349, -0.35460488704253562597, -0.748510748171101098635, -0.970941817426052027157, -0.970941817426052027157, -0.748510748171101098635, -0.35460488704253562597, 0.120536680255323053349, 0.568064746731155802512, 0.8854560256532098959};
@@ -52,6 +92,36 @@ template <> struct RadixConst<13> {
   }
   __device__ __forceinline__ static double s(int m) {
     constexpr double t[13] = {0.0, 0.464723172043768545656, 0.82298386589365639458, 0.992708874098053992801, 0.93501624268541482344, 0.663122658240795202377, 0.239315664287557767149, -0.239315664287557767149, -0.663122658240795202377, -0.93501624268541482344, -0.992708874098053992801, -0.82298386589365639458, -0.464723172043768545656};
+    return t[m];
+  }
+};
+template <> struct RadixConst<14> {
+  __device__ __forceinline__ static double c(int m) {
+    constexpr double t[14] = {1.0, 0.900968867902419126236, 0.623489801858733530525, 0.222520933956314404289, -0.222520933956314404289, -0.623489801858733530525, -0.900968867902419126236, -1.0, -0.900968867902419126236, -0.623489801858733530525, -0.222520933956314404289, 0.222520933956314404289, 0.623489801858733530525, 0.900968867902419126236};
+    return t[m];
+  }
+  __device__ __forceinline__ static double s(int m) {
+    constexpr double t[14] = {0.0, 0.433883739117558120476, 0.781831482468029808708, 0.974927912181823607018, 0.974927912181823607018, 0.781831482468029808708, 0.433883739117558120476, 0.00000000000000000000000000000000000000000041340642196527976473, -0.433883739117558120476, -0.781831482468029808708, -0.974927912181823607018, -0.974927912181823607018, -0.781831482468029808708, -0.433883739117558120476};
+    return t[m];
+  }
+};
+template <> struct RadixConst<15> {
+  __device__ __forceinline__ static double c(int m) {
+    constexpr double t[15] = {1.0, 0.913545457642600895502, 0.669130606358858213826, 0.309016994374947424102, -0.1045284632676534714, -0.5, -0.809016994374947424102, -0.978147600733805637929, -0.978147600733805637929, -0.809016994374947424102, -0.5, -0.1045284632676534714, 0.309016994374947424102, 0.669130606358858213826, 0.913545457642600895502};
+    return t[m];
+  }
+  __device__ __forceinline__ static double s(int m) {
+    constexpr double t[15] = {0.0, 0.406736643075800207754, 0.743144825477394235015, 0.951056516295153572116, 0.994521895368273336923, 0.866025403784438646764, 0.587785252292473129169, 0.207911690817759337102, -0.207911690817759337102, -0.587785252292473129169, -0.866025403784438646764, -0.994521895368273336923, -0.951056516295153572116, -0.743144825477394235015, -0.406736643075800207754};
+    return t[m];
+  }
+};
+template <> struct RadixConst<16> {
+  __device__ __forceinline__ static double c(int m) {
+    constexpr double t[16] = {1.0, 0.923879532511286756128, 0.707106781186547524401, 0.382683432365089771728, 0.000000000000000000000000000000000000000000206703210982639882365, -0.382683432365089771728, -0.707106781186547524401, -0.923879532511286756128, -1.0, -0.923879532511286756128, -0.707106781186547524401, -0.382683432365089771728, 0.0000000000000000000000000000000000000000223387644065498832429, 0.382683432365089771728, 0.707106781186547524401, 0.923879532511286756128};
+    return t[m];
+  }
+  __device__ __forceinline__ static double s(int m) {
+    constexpr double t[16] = {0.0, 0.382683432365089771728, 0.707106781186547524401, 0.923879532511286756128, 1.0, 0.923879532511286756128, 0.707106781186547524401, 0.382683432365089771728, 0.00000000000000000000000000000000000000000041340642196527976473, -0.382683432365089771728, -0.707106781186547524401, -0.923879532511286756128, -1.0, -0.923879532511286756128, -0.707106781186547524401, -0.382683432365089771728};
     return t[m];
   }
 };

@@ -17,11 +17,10 @@ struct derek_gpu {
   int nitems = 0;
   int max_n[3] = {0, 0, 0};
   int max_nmax = 0;        // max over all axes and systems
-  int max_nxr = 0;
-  int max_plane_yz = 0;    // max n2*n3
+  int max_nchunk = 0;      // column chunks of the largest sphere
   int max_nb = 0;
   long long total_psi = 0; // elements per psi-shaped buffer
-  long long total_planes = 0;
+  long long total_abuf = 0;
   long long total_grid = 0;
 
   // ---- host copies
@@ -29,8 +28,10 @@ struct derek_gpu {
   std::vector<derek::KSetDev> ks;
   std::vector<int> n_std;          // 3 per system
   std::vector<int> item_ks, item_band;
-  std::vector<int32_t> box_rows, fft_index;  // per sphere entry (parity hooks)
-  std::vector<double> kin64;
+  std::vector<int32_t> box_rows, fft_index;  // per sphere entry, reference order
+  std::vector<double> kin64;                 // reference order
+  std::vector<int32_t> perm;                 // column-order entry -> reference entry
+  std::vector<double> kin_col;               // kinetic energies, column order
   std::vector<double> vext_host;   // per system grid, concatenated
 
   // ---- device tables
@@ -38,8 +39,8 @@ struct derek_gpu {
   derek::SysDev *d_sys = nullptr;
   derek::KSetDev *d_ks = nullptr;
   int *d_item_ks = nullptr, *d_item_band = nullptr;
-  int *d_pidx = nullptr, *d_xstart = nullptr, *d_rowstart = nullptr;
-  short *d_rows = nullptr;
+  int *d_ent_col = nullptr, *d_col_start = nullptr;
+  short *d_ent_ix = nullptr, *d_col_y = nullptr, *d_col_z = nullptr, *d_rows = nullptr;
   double *d_kin64 = nullptr;
   float *d_kin32 = nullptr;
   double2 *d_tw64 = nullptr;
@@ -56,7 +57,7 @@ struct derek_gpu {
 
   // ---- device psi-shaped buffers (element type by precision)
   void *d_X = nullptr, *d_Y = nullptr, *d_Yp = nullptr, *d_HX = nullptr;
-  void *d_planes = nullptr;
+  void *d_abuf = nullptr;          // x-line buffer of the H.psi passes
   double *d_occw = nullptr;        // per item: w_k f / Omega (density weights)
   double *d_eig = nullptr;         // per item
   double *d_occ = nullptr;         // per item: f in [0, 2]

@@ -11,12 +11,14 @@ struct Tables {
   const KSetDev *ks;
   const int *item_ks;     // item -> k-set
   const int *item_band;   // item -> band
-  const int *pidx;        // sphere entry -> position iy*n3 + iz in its x-plane
-  const double *kin64;    // sphere entry -> 1/2|k+G|^2
+  const double *kin64;    // sphere entry (column order) -> 1/2|k+G|^2
   const float *kin32;
-  const int *xstart;      // per plane: first sphere entry (local), nxr+1 per k-set
-  const int *rowstart;    // per plane: first active row (local), nxr+1 per k-set
-  const short *rows;      // active y rows of each plane
+  const int *ent_col;     // sphere entry -> its column (local index)
+  const short *ent_ix;    // sphere entry -> FFT index along x
+  const int *col_start;   // per column: first entry (local), ncol + 1 per k-set
+  const short *col_y;     // per column: FFT indices along y and z
+  const short *col_z;
+  const short *rows;      // per k-set: the y rows holding columns
   const double2 *tw64;    // twiddle tables exp(-2 pi i t/n)
   const float2 *tw32;
 };
@@ -34,27 +36,23 @@ struct Axpby {
   double alpha, beta, gamma;
 };
 
-// ---- H.psi and density pipeline (hpsi.cu) ---------------------------------
+// ---- H.psi and density pipeline (hpsi4.cu) --------------------------------
 // Launch geometry: items [item_begin, item_begin + nitems) of the batch.
-//   inv_yz : scatter sphere -> backward z and y transforms -> plane buffer
-//   vmul_x : backward x transform, V(r) multiply, forward x transform
-//   fwd_yz : forward y and z transforms -> gather sphere, kinetic, epilogue
 template <typename R>
-void launch_inv_yz(const Tables &t, int item_begin, int nitems, int max_nxr, int max_plane,
-                   const cplx<R> *psi, cplx<R> *planes, const double *occ_skip,
-                   cudaStream_t st);
+void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                  const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip, cudaStream_t st);
 template <typename R>
-void launch_vmul_x(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2,
-                   int max_n3, cplx<R> *planes, const R *vloc, cudaStream_t st);
+void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2, int max_n3,
+                  cplx<R> *abuf, const R *vloc, cudaStream_t st);
 template <typename R>
-void launch_fwd_yz(const Tables &t, int item_begin, int nitems, int max_nxr, int max_plane,
-                   const cplx<R> *planes, const cplx<R> *psi, const cplx<R> *prev,
-                   cplx<R> *out, const Axpby *coef, cudaStream_t st);
-// density: per (k-set, y) loop over bands, accumulate occ-weighted |psi(r)|^2
+void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                  const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev, cplx<R> *out,
+                  const Axpby *coef, cudaStream_t st);
 template <typename R>
-void launch_density_x(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2,
-                      int max_n3, const cplx<R> *planes, const double *occ,
-                      double *partial, const long long *partial_off, cudaStream_t st);
+void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
+                          const cplx<R> *abuf, const double *occ, double *partial,
+                          const long long *partial_off, cudaStream_t st);
+constexpr int kColChunk = 64;   // columns per x-line chunk (kCC in hpsi4.cu)
 
 // ---- full-grid FFT (grid.cu) -----------------------------------------------
 // In-place unnormalised 3D FFT of one complex FP64 grid per system in

@@ -185,8 +185,8 @@ int derek_gpu_get_vext(derek_gpu_t *h, int sys, double *vext);
  * derek_gpu_launch_count the number of kernels the library has launched in
  * this process (graph replays count their kernels); derek_gpu_time_apply_h
  * runs H.psi on every band of every k-point nrep times and returns the mean
- * device time per application and per stage kernel (3 values: scatter +
- * backward yz transforms, x transforms with V(r), forward yz + gather). */
+ * device time per application and per stage kernel (3 values: backward x
+ * lines, (y,z) planes with V(r), forward x lines + gather + kinetic). */
 void *derek_gpu_stream(derek_gpu_t *h);
 unsigned long long derek_gpu_launch_count(void);
 int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage);
