@@ -48,8 +48,8 @@ static void apply_h_t(derek_gpu *h, int item_begin, int nitems, const void *in, 
                       void *out, const Axpby *coef, const R *vloc) {
   launch_x_inv<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0], (const cplx<R> *)in,
                   (cplx<R> *)h->d_abuf, nullptr, h->stream);
-  launch_plane<R>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2],
-                  (cplx<R> *)h->d_abuf, vloc, h->stream);
+  launch_plane<R>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
+                  h->min_n[2], (cplx<R> *)h->d_abuf, vloc, h->stream);
   launch_x_fwd<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0],
                   (const cplx<R> *)h->d_abuf, (const cplx<R> *)in, (const cplx<R> *)prev,
                   (cplx<R> *)out, coef, h->stream);
@@ -239,6 +239,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       S.n[i] = nfine[i];
       h->n_std.push_back(nstd[i]);
       h->max_n[i] = std::max(h->max_n[i], nfine[i]);
+      h->min_n[i] = s == 0 ? nfine[i] : std::min(h->min_n[i], nfine[i]);
       h->max_nmax = std::max(h->max_nmax, nfine[i]);
       FftPlan &p = S.plan[i];
       p.n = nfine[i];
@@ -336,6 +337,9 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
         ++c;
       }
       col_start.push_back(e);
+      // keep col_y / col_z aligned with col_start (ncol + 1 entries per k-set)
+      col_y.push_back(0);
+      col_z.push_back(0);
       K.nrow = (int)krows.size();
       rows.insert(rows.end(), krows.begin(), krows.end());
       for (int i = 0; i < npw; ++i) {
@@ -685,8 +689,8 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       launch_x_inv<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const double2 *)in,
                            (double2 *)h->d_abuf, nullptr, h->stream);
       cudaEventRecord(ev[1], h->stream);
-      launch_plane<double>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
-                           (double2 *)h->d_abuf, h->d_vloc, h->stream);
+      launch_plane<double>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
+                           h->min_n[2], (double2 *)h->d_abuf, h->d_vloc, h->stream);
       cudaEventRecord(ev[2], h->stream);
       launch_x_fwd<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0],
                            (const double2 *)h->d_abuf, (const double2 *)in, nullptr,
@@ -695,8 +699,8 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       launch_x_inv<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const float2 *)in,
                           (float2 *)h->d_abuf, nullptr, h->stream);
       cudaEventRecord(ev[1], h->stream);
-      launch_plane<float>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2],
-                          (float2 *)h->d_abuf, h->d_vloc32, h->stream);
+      launch_plane<float>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
+                          h->min_n[2], (float2 *)h->d_abuf, h->d_vloc32, h->stream);
       cudaEventRecord(ev[2], h->stream);
       launch_x_fwd<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0],
                           (const float2 *)h->d_abuf, (const float2 *)in, nullptr,

@@ -136,3 +136,76 @@ __device__ void fft4_lines(cplx<R_> *buf, const LinePlan &p, int nlines, int ldi
 }
 
 }  // namespace derek
+
+namespace derek {
+
+// ---- compile-time variant: n = A * B, element stride ES and line distance
+// LD known at compile time (the (y,z) planes of cubic grids).
+constexpr int plan_a(int n) {
+  int best = 0, span = 1 << 30, p2 = 0;
+  for (int x = 1; x <= 16; ++x) {
+    if (n % x) continue;
+    const int y = n / x;
+    if (y > 16) continue;
+    const int s = x > y ? x : y;
+    const int q = ((x & (x - 1)) == 0 && x > 1) ? 1 : 0;
+    if (s < span || (s == span && q > p2)) {
+      best = x;
+      span = s;
+      p2 = q;
+    }
+  }
+  return best;
+}
+
+template <typename R_, int SIGN, int N, int ES, int LD>
+__device__ __forceinline__ void fft4_fixed(cplx<R_> *buf, int nlines, const short *lines,
+                                           const cplx<R_> *__restrict__ tw) {
+  constexpr int A = plan_a(N);
+  constexpr int B = N / A;
+  constexpr int SPAN = A > B ? A : B;
+  constexpr int G = 32 / SPAN;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const int g = lane / SPAN;
+  const int r = lane - g * SPAN;
+  for (int l0 = warp * G; l0 < nlines; l0 += nwarps * G) {
+    const int l = l0 + g;
+    const bool live = g < G && l < nlines;
+    cplx<R_> *line = buf + (live ? (lines ? (int)lines[l] : l) * LD : 0);
+    if (live && r < B && A > 1) {
+      cplx<R_> v[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) v[n1] = line[(B * n1 + r) * ES];
+      Dft<R_, A, SIGN>::run(v);
+#pragma unroll
+      for (int k1 = 1; k1 < A; ++k1) {
+        cplx<R_> w = tw[(r * k1) % N];
+        if (SIGN > 0) w.y = -w.y;
+        v[k1] = cmul<R_>(v[k1], w);
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) line[(B * k1 + r) * ES] = v[k1];
+    }
+    __syncwarp();
+    if (B > 1) {
+      cplx<R_> v[B];
+      const bool act = live && r < A;
+      if (act) {
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) v[n2] = line[(B * r + n2) * ES];
+      }
+      __syncwarp();
+      if (act) {
+        Dft<R_, B, SIGN>::run(v);
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) line[(r + A * k2) * ES] = v[k2];
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+}
+
+}  // namespace derek

@@ -16,6 +16,7 @@ struct derek_gpu {
   int nks = 0;
   int nitems = 0;
   int max_n[3] = {0, 0, 0};
+  int min_n[3] = {0, 0, 0};
   int max_nmax = 0;        // max over all axes and systems
   int max_nchunk = 0;      // column chunks of the largest sphere
   int max_nb = 0;

@@ -114,6 +114,45 @@ __global__ void __launch_bounds__(512) k_plane(Tables t, int item_begin, cplx<R>
   for (int c = threadIdx.x; c < K.ncol; c += blockDim.x) a[c] = P[cy[c] * pz + cz[c]];
 }
 
+// Same pass for n2 = n3 = N known at compile time (cubic grids).
+template <typename R, int N>
+__global__ void __launch_bounds__(512) k_plane_fixed(Tables t, int item_begin, cplx<R> *__restrict__ abuf,
+                                                     const R *__restrict__ vloc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int PZ = N + 1;
+  const int item = item_begin + blockIdx.x;
+  const int x = blockIdx.y;
+  const int ksi = t.item_ks[item];
+  const KSetDev &K = t.ks[ksi];
+  const SysDev &S = t.sys[K.sys];
+  if (!S.active) return;
+  const int n1 = S.n[0];
+  if (x >= n1) return;
+  const int b = t.item_band[item];
+  cplx<R> *P = reinterpret_cast<cplx<R> *>(smem_raw);
+  cplx<R> *tw = P + N * PZ;
+  for (int i = threadIdx.x; i < N * PZ; i += blockDim.x) P[i] = mk<R>(0, 0);
+  load_tw<R>(tw, twtab<R>(t) + S.lp[1].tw_off, N);
+  __syncthreads();
+  cplx<R> *a = abuf + K.a_off + ((long long)b * n1 + x) * K.ncol_pad;
+  const short *cy = t.col_y + K.col_off;
+  const short *cz = t.col_z + K.col_off;
+  for (int c = threadIdx.x; c < K.ncol; c += blockDim.x) P[cy[c] * PZ + cz[c]] = a[c];
+  __syncthreads();
+  const short *rows = t.rows + K.row_off;
+  fft4_fixed<R, +1, N, 1, PZ>(P, K.nrow, rows, tw);
+  fft4_fixed<R, +1, N, PZ, 1>(P, N, nullptr, tw);
+  const R *v = vloc + S.grid_off + (long long)x * N * N;
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    const int y = i / N, z = i - y * N;
+    P[y * PZ + z] = cscale<R>(P[y * PZ + z], v[i]);
+  }
+  __syncthreads();
+  fft4_fixed<R, -1, N, PZ, 1>(P, N, nullptr, tw);
+  fft4_fixed<R, -1, N, 1, PZ>(P, K.nrow, rows, tw);
+  for (int c = threadIdx.x; c < K.ncol; c += blockDim.x) a[c] = P[cy[c] * PZ + cz[c]];
+}
+
 // ---- pass 3: forward x transforms, gather, kinetic, epilogue --------------
 template <typename R>
 __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const cplx<R> *__restrict__ abuf,
@@ -237,10 +276,26 @@ void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, i
   derek::note_launch(), k_x_inv<R><<<dim3(nitems, max_nchunk), 256, sm, st>>>(t, item_begin, psi, abuf, occ_skip);
 }
 
+template <typename R, int N>
+static bool try_plane_fixed(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2,
+                            int max_n3, int min_n2, int min_n3, cplx<R> *abuf, const R *vloc,
+                            cudaStream_t st) {
+  if (max_n2 != N || max_n3 != N || min_n2 != N || min_n3 != N) return false;
+  const size_t sm = ((size_t)N * (N + 1) + N) * sizeof(cplx<R>);
+  cudaFuncSetAttribute(k_plane_fixed<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  derek::note_launch(), k_plane_fixed<R, N><<<dim3(nitems, max_n1), 512, sm, st>>>(t, item_begin, abuf, vloc);
+  return true;
+}
+
 template <typename R>
 void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2, int max_n3,
-                  cplx<R> *abuf, const R *vloc, cudaStream_t st) {
+                  int min_n2, int min_n3, cplx<R> *abuf, const R *vloc, cudaStream_t st) {
   if (nitems <= 0) return;
+  if (try_plane_fixed<R, 72>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
+      try_plane_fixed<R, 64>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
+      try_plane_fixed<R, 48>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
+      try_plane_fixed<R, 32>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st))
+    return;
   const size_t sm = smem_plane<R>(max_n2, max_n3);
   cudaFuncSetAttribute(k_plane<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   derek::note_launch(), k_plane<R><<<dim3(nitems, max_n1), 512, sm, st>>>(t, item_begin, abuf, vloc);
@@ -269,8 +324,8 @@ void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, in
 #define DEREK_INST(R)                                                                             \
   template void launch_x_inv<R>(const Tables &, int, int, int, int, const cplx<R> *, cplx<R> *,  \
                                 const double *, cudaStream_t);                                    \
-  template void launch_plane<R>(const Tables &, int, int, int, int, int, cplx<R> *, const R *,   \
-                                cudaStream_t);                                                    \
+  template void launch_plane<R>(const Tables &, int, int, int, int, int, int, int, cplx<R> *,     \
+                                const R *, cudaStream_t);                                         \
   template void launch_x_fwd<R>(const Tables &, int, int, int, int, const cplx<R> *,             \
                                 const cplx<R> *, const cplx<R> *, cplx<R> *, const Axpby *,      \
                                 cudaStream_t);                                                    \

@@ -26,8 +26,16 @@ template <typename T> cudaError_t dalloc(T **p, size_t n) {
 }
 
 // -- pieces of an iteration -------------------------------------------------
+bool use_tc(const derek_gpu *h) {
+  return h->prec == DEREK_PREC_MIXED && h->opts.use_tensor_cores && h->max_nb <= kMaxBands;
+}
+
 int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int hermitize) {
-  if (h->prec == DEREK_PREC_FP64)
+  if (use_tc(h))
+    launch_overlap_tc(h->tab, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit, (const float2 *)A,
+                      (const float2 *)B, h->d_opart, h->d_opart_off, out, h->d_mat_off, hermitize,
+                      h->d_status, h->stream);
+  else if (h->prec == DEREK_PREC_FP64)
     launch_overlap<double>(h->tab, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit,
                            (const double2 *)A, (const double2 *)B, h->d_opart, h->d_opart_off, out,
                            h->d_mat_off, hermitize, h->stream);
@@ -295,7 +303,11 @@ int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
   if (!h || s < 0 || s >= h->nsys || k < 0 || k >= h->sys[s].nk || !out) return DEREK_ERR_BAD_ARG;
   const int ki = h->sys[s].ks0 + k;
   const KSetDev &K = h->ks[ki];
-  if (h->prec == DEREK_PREC_FP64)
+  if (use_tc(h))
+    launch_overlap_tc(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const float2 *)h->cur_psi(),
+                      (const float2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S, h->d_mat_off,
+                      0, h->d_status, h->stream);
+  else if (h->prec == DEREK_PREC_FP64)
     launch_overlap<double>(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const double2 *)h->cur_psi(),
                            (const double2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S,
                            h->d_mat_off, 0, h->stream);

@@ -408,6 +408,12 @@ void launch_overlap(const Tables &t, int ks_begin, int nks, int max_nb, int max_
   const int nt = (max_nb + OT - 1) / OT;
   dim3 grid(nt * nt, (max_npw + ksplit - 1) / ksplit, nks);
   derek::note_launch(), k_overlap_partial<R><<<grid, 256, 0, st>>>(t, ks_begin, A, B, part, part_off, ksplit);
+  launch_overlap_reduce(t, ks_begin, nks, part, part_off, ksplit, out, mat_off, hermitize, st);
+}
+
+void launch_overlap_reduce(const Tables &t, int ks_begin, int nks, const double2 *part,
+                           const long long *part_off, int ksplit, double2 *out,
+                           const long long *mat_off, int hermitize, cudaStream_t st) {
   derek::note_launch(), k_overlap_reduce<<<nks, 256, 0, st>>>(t, ks_begin, part, part_off, ksplit, out, mat_off, hermitize);
 }
 
