@@ -126,10 +126,20 @@ template <> struct RadixConst<16> {
   }
 };
 
-// In-register DFT of length R with exponent sign SIGN.
-template <typename R_, int R, int SIGN> struct Dft {
+// In-register DFT of length R with exponent sign SIGN.  Prime lengths use the
+// direct O(R^2) sum; composite lengths R = P * Q (P the smallest prime
+// factor) split Cooley-Tukey style into P-point and Q-point DFTs with
+// compile-time twiddles; 2, 3, 4 and 8 are written out below.
+constexpr int smallest_factor(int r) {
+  for (int p = 2; p * p <= r; ++p)
+    if (r % p == 0) return p;
+  return r;
+}
+
+template <typename R_, int R, int SIGN, bool PRIME = (smallest_factor(R) == R)> struct DftGen;
+
+template <typename R_, int R, int SIGN> struct DftGen<R_, R, SIGN, true> {
   __device__ __forceinline__ static void run(cplx<R_> *v) {
-    // generic O(R^2) form
     cplx<R_> out[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -147,6 +157,48 @@ template <typename R_, int R, int SIGN> struct Dft {
 #pragma unroll
     for (int k = 0; k < R; ++k) v[k] = out[k];
   }
+};
+
+template <typename R_, int R, int SIGN> struct Dft;
+
+template <typename R_, int R, int SIGN> struct DftGen<R_, R, SIGN, false> {
+  static constexpr int P = smallest_factor(R);
+  static constexpr int Q = R / P;
+  __device__ __forceinline__ static void run(cplx<R_> *v) {
+    // y[n2][k1] = W_R^{n2 k1} sum_{n1} x[Q n1 + n2] W_P^{n1 k1}
+    cplx<R_> y[R];
+#pragma unroll
+    for (int n2 = 0; n2 < Q; ++n2) {
+      cplx<R_> t[P];
+#pragma unroll
+      for (int n1 = 0; n1 < P; ++n1) t[n1] = v[Q * n1 + n2];
+      Dft<R_, P, SIGN>::run(t);
+#pragma unroll
+      for (int k1 = 0; k1 < P; ++k1) {
+        const int m = (n2 * k1) % R;
+        if (m == 0) {
+          y[n2 * P + k1] = t[k1];
+        } else {
+          const cplx<R_> w = mk<R_>((R_)RadixConst<R>::c(m), (R_)(SIGN * RadixConst<R>::s(m)));
+          y[n2 * P + k1] = cmul<R_>(t[k1], w);
+        }
+      }
+    }
+    // X[k1 + P k2] = sum_{n2} y[n2][k1] W_Q^{n2 k2}
+#pragma unroll
+    for (int k1 = 0; k1 < P; ++k1) {
+      cplx<R_> t[Q];
+#pragma unroll
+      for (int n2 = 0; n2 < Q; ++n2) t[n2] = y[n2 * P + k1];
+      Dft<R_, Q, SIGN>::run(t);
+#pragma unroll
+      for (int k2 = 0; k2 < Q; ++k2) v[k1 + P * k2] = t[k2];
+    }
+  }
+};
+
+template <typename R_, int R, int SIGN> struct Dft {
+  __device__ __forceinline__ static void run(cplx<R_> *v) { DftGen<R_, R, SIGN>::run(v); }
 };
 
 template <typename R_, int SIGN> struct Dft<R_, 2, SIGN> {
