@@ -46,11 +46,11 @@ __global__ void k_to_float(long long n, const double *__restrict__ a, float *__r
 template <typename R>
 static void apply_h_t(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
                       void *out, const Axpby *coef, const R *vloc) {
-  launch_x_inv<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0], (const cplx<R> *)in,
+  launch_x_inv<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const cplx<R> *)in,
                   (cplx<R> *)h->d_abuf, nullptr, h->stream);
   launch_plane<R>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
                   h->min_n[2], (cplx<R> *)h->d_abuf, vloc, h->stream);
-  launch_x_fwd<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0],
+  launch_x_fwd<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0], h->min_n[0],
                   (const cplx<R> *)h->d_abuf, (const cplx<R> *)in, (const cplx<R> *)prev,
                   (cplx<R> *)out, coef, h->stream);
 }
@@ -66,7 +66,7 @@ int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, cons
 }
 
 template <typename R> static void density_t(derek_gpu *h, const void *psi) {
-  launch_x_inv<R>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const cplx<R> *)psi,
+  launch_x_inv<R>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const cplx<R> *)psi,
                   (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
   launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
                           (const cplx<R> *)h->d_abuf, h->d_occw, h->d_partial, h->d_partial_off,
@@ -686,23 +686,23 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
   for (int r = 0; r < nrep; ++r) {
     cudaEventRecord(ev[0], h->stream);
     if (h->prec == DEREK_PREC_FP64) {
-      launch_x_inv<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const double2 *)in,
+      launch_x_inv<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const double2 *)in,
                            (double2 *)h->d_abuf, nullptr, h->stream);
       cudaEventRecord(ev[1], h->stream);
       launch_plane<double>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
                            h->min_n[2], (double2 *)h->d_abuf, h->d_vloc, h->stream);
       cudaEventRecord(ev[2], h->stream);
-      launch_x_fwd<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0],
+      launch_x_fwd<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0],
                            (const double2 *)h->d_abuf, (const double2 *)in, nullptr,
                            (double2 *)h->d_HX, nullptr, h->stream);
     } else {
-      launch_x_inv<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], (const float2 *)in,
+      launch_x_inv<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const float2 *)in,
                           (float2 *)h->d_abuf, nullptr, h->stream);
       cudaEventRecord(ev[1], h->stream);
       launch_plane<float>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
                           h->min_n[2], (float2 *)h->d_abuf, h->d_vloc32, h->stream);
       cudaEventRecord(ev[2], h->stream);
-      launch_x_fwd<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0],
+      launch_x_fwd<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0],
                           (const float2 *)h->d_abuf, (const float2 *)in, nullptr,
                           (float2 *)h->d_HX, nullptr, h->stream);
     }

@@ -201,6 +201,10 @@ template <typename R_, int R, int SIGN> struct Dft {
   __device__ __forceinline__ static void run(cplx<R_> *v) { DftGen<R_, R, SIGN>::run(v); }
 };
 
+template <typename R_, int SIGN> struct Dft<R_, 1, SIGN> {
+  __device__ __forceinline__ static void run(cplx<R_> *) {}
+};
+
 template <typename R_, int SIGN> struct Dft<R_, 2, SIGN> {
   __device__ __forceinline__ static void run(cplx<R_> *v) {
     cplx<R_> a = v[0], b = v[1];

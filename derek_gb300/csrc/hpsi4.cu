@@ -36,7 +36,7 @@ __device__ __forceinline__ void load_tw(cplx<R> *dst, const cplx<R> *src, int n)
 }
 
 // ---- pass 1: backward x transforms of the sphere's columns ----------------
-template <typename R>
+template <typename R, int NX>
 __global__ void __launch_bounds__(256) k_x_inv(Tables t, int item_begin, const cplx<R> *__restrict__ psi,
                                                cplx<R> *__restrict__ abuf,
                                                const double *__restrict__ occ_skip) {
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) k_x_inv(Tables t, int item_begin, const c
   if (!S.active) return;
   if (occ_skip && occ_skip[item] == 0.0) return;
   const int b = t.item_band[item];
-  const int n1 = S.n[0];
+  const int n1 = NX ? NX : S.n[0];
   const int pl = n1 + 1;  // odd line pitch
   const int nc = min(kCC, K.ncol - c0);
   cplx<R> *L = reinterpret_cast<cplx<R> *>(smem_raw);
@@ -65,7 +65,10 @@ __global__ void __launch_bounds__(256) k_x_inv(Tables t, int item_begin, const c
   const short *eix = t.ent_ix + K.ent_off;
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) L[(ecol[e] - c0) * pl + eix[e]] = src[e];
   __syncthreads();
-  fft4_lines<R, +1>(L, S.lp[0], nc, pl, 1, nullptr, tw);
+  if (NX)
+    fft4_fixed<R, +1, NX ? NX : 1, 1, NX + 1>(L, nc, nullptr, tw);
+  else
+    fft4_lines<R, +1>(L, S.lp[0], nc, pl, 1, nullptr, tw);
   cplx<R> *dst = abuf + K.a_off + (long long)b * n1 * K.ncol_pad + c0;
   for (int i = threadIdx.x; i < n1 * nc; i += blockDim.x) {
     const int x = i / nc, c = i - x * nc;
@@ -154,7 +157,7 @@ __global__ void __launch_bounds__(512) k_plane_fixed(Tables t, int item_begin, c
 }
 
 // ---- pass 3: forward x transforms, gather, kinetic, epilogue --------------
-template <typename R>
+template <typename R, int NX>
 __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const cplx<R> *__restrict__ abuf,
                                                const cplx<R> *__restrict__ psi,
                                                const cplx<R> *__restrict__ prev,
@@ -169,7 +172,7 @@ __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const c
   const SysDev &S = t.sys[K.sys];
   if (!S.active) return;
   const int b = t.item_band[item];
-  const int n1 = S.n[0];
+  const int n1 = NX ? NX : S.n[0];
   const int pl = n1 + 1;
   const int nc = min(kCC, K.ncol - c0);
   cplx<R> *L = reinterpret_cast<cplx<R> *>(smem_raw);
@@ -181,7 +184,10 @@ __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const c
     L[c * pl + x] = src[(long long)x * K.ncol_pad + c];
   }
   __syncthreads();
-  fft4_lines<R, -1>(L, S.lp[0], nc, pl, 1, nullptr, tw);
+  if (NX)
+    fft4_fixed<R, -1, NX ? NX : 1, 1, NX + 1>(L, nc, nullptr, tw);
+  else
+    fft4_lines<R, -1>(L, S.lp[0], nc, pl, 1, nullptr, tw);
   const int *cs = t.col_start + K.col_off;
   const int e0 = cs[c0], e1 = cs[c0 + nc];
   const int *ecol = t.ent_col + K.ent_off;
@@ -267,13 +273,49 @@ template <typename R> static size_t smem_plane(int max_n2, int max_n3) {
   return ((size_t)max_n2 * (max_n3 + 1) + 2 * kMaxDim) * sizeof(cplx<R>);
 }
 
+
+template <typename R, int NX>
+static void x_inv_go(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                     const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip, cudaStream_t st) {
+  const size_t sm = smem_x<R>(max_n1);
+  cudaFuncSetAttribute(k_x_inv<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  derek::note_launch(), k_x_inv<R, NX><<<dim3(nitems, max_nchunk), 256, sm, st>>>(t, item_begin, psi, abuf, occ_skip);
+}
+
+// compile-time x length when every system has the same n1 in {32, 48, 64, 72}
 template <typename R>
 void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip, cudaStream_t st) {
+                  int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
+                  cudaStream_t st) {
   if (nitems <= 0) return;
+  const int n = max_n1 == min_n1 ? max_n1 : 0;
+  if (n == 72) x_inv_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
+  else if (n == 64) x_inv_go<R, 64>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
+  else if (n == 48) x_inv_go<R, 48>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
+  else if (n == 32) x_inv_go<R, 32>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
+  else x_inv_go<R, 0>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
+}
+
+template <typename R, int NX>
+static void x_fwd_go(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                     const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev, cplx<R> *out,
+                     const Axpby *coef, cudaStream_t st) {
   const size_t sm = smem_x<R>(max_n1);
-  cudaFuncSetAttribute(k_x_inv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  derek::note_launch(), k_x_inv<R><<<dim3(nitems, max_nchunk), 256, sm, st>>>(t, item_begin, psi, abuf, occ_skip);
+  cudaFuncSetAttribute(k_x_fwd<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  derek::note_launch(), k_x_fwd<R, NX><<<dim3(nitems, max_nchunk), 256, sm, st>>>(t, item_begin, abuf, psi, prev, out, coef);
+}
+
+template <typename R>
+void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                  int min_n1, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
+                  cplx<R> *out, const Axpby *coef, cudaStream_t st) {
+  if (nitems <= 0) return;
+  const int n = max_n1 == min_n1 ? max_n1 : 0;
+  if (n == 72) x_fwd_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
+  else if (n == 64) x_fwd_go<R, 64>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
+  else if (n == 48) x_fwd_go<R, 48>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
+  else if (n == 32) x_fwd_go<R, 32>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
+  else x_fwd_go<R, 0>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
 }
 
 template <typename R, int N>
@@ -301,15 +343,6 @@ void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int m
   derek::note_launch(), k_plane<R><<<dim3(nitems, max_n1), 512, sm, st>>>(t, item_begin, abuf, vloc);
 }
 
-template <typename R>
-void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev, cplx<R> *out,
-                  const Axpby *coef, cudaStream_t st) {
-  if (nitems <= 0) return;
-  const size_t sm = smem_x<R>(max_n1);
-  cudaFuncSetAttribute(k_x_fwd<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  derek::note_launch(), k_x_fwd<R><<<dim3(nitems, max_nchunk), 256, sm, st>>>(t, item_begin, abuf, psi, prev, out, coef);
-}
 
 template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
@@ -322,11 +355,11 @@ void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, in
 }
 
 #define DEREK_INST(R)                                                                             \
-  template void launch_x_inv<R>(const Tables &, int, int, int, int, const cplx<R> *, cplx<R> *,  \
-                                const double *, cudaStream_t);                                    \
+  template void launch_x_inv<R>(const Tables &, int, int, int, int, int, const cplx<R> *,        \
+                                cplx<R> *, const double *, cudaStream_t);                         \
   template void launch_plane<R>(const Tables &, int, int, int, int, int, int, int, cplx<R> *,     \
                                 const R *, cudaStream_t);                                         \
-  template void launch_x_fwd<R>(const Tables &, int, int, int, int, const cplx<R> *,             \
+  template void launch_x_fwd<R>(const Tables &, int, int, int, int, int, const cplx<R> *,        \
                                 const cplx<R> *, const cplx<R> *, cplx<R> *, const Axpby *,      \
                                 cudaStream_t);                                                    \
   template void launch_density_plane<R>(const Tables &, int, int, int, int, int, const cplx<R> *, \

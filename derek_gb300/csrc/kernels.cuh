@@ -40,7 +40,8 @@ struct Axpby {
 // Launch geometry: items [item_begin, item_begin + nitems) of the batch.
 template <typename R>
 void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip, cudaStream_t st);
+                  int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
+                  cudaStream_t st);
 // (y,z)-plane pass; a compile-time kernel is used when every system has
 // n2 = n3 = N for N in {32, 48, 64, 72}
 template <typename R>
@@ -48,8 +49,8 @@ void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int m
                   int min_n2, int min_n3, cplx<R> *abuf, const R *vloc, cudaStream_t st);
 template <typename R>
 void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev, cplx<R> *out,
-                  const Axpby *coef, cudaStream_t st);
+                  int min_n1, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
+                  cplx<R> *out, const Axpby *coef, cudaStream_t st);
 template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
                           const cplx<R> *abuf, const double *occ, double *partial,

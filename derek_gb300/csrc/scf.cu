@@ -47,7 +47,10 @@ int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int he
 }
 
 int rotate_all(derek_gpu *h, void *X, const double2 *C) {
-  if (h->prec == DEREK_PREC_FP64)
+  if (use_tc(h) && h->opts.use_tensor_cores >= 2)
+    launch_rotate_tc(h->tab, 0, h->nks, h->max_nb, h->max_npw, (float2 *)X, C, h->d_mat_off,
+                     h->d_status, h->stream);
+  else if (h->prec == DEREK_PREC_FP64)
     launch_rotate<double>(h->tab, 0, h->nks, h->max_nb, h->max_npw, (double2 *)X, C, h->d_mat_off,
                           h->stream);
   else

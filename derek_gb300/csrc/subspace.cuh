@@ -22,6 +22,9 @@ void launch_overlap_tc(const Tables &t, int ks_begin, int nks, int max_nb, int m
                        const float2 *X, const float2 *Y, double2 *part, const long long *part_off,
                        double2 *out, const long long *mat_off, int hermitize, int *status,
                        cudaStream_t st);
+// BF16x3 tcgen05 rotation X <- X C (complex64, nb <= 128), in place
+void launch_rotate_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, float2 *X,
+                      const double2 *C, const long long *mat_off, int *status, cudaStream_t st);
 template <typename R>
 void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, cplx<R> *X,
                    const double2 *C, const long long *mat_off, cudaStream_t st);

@@ -301,3 +301,175 @@ void launch_overlap_tc(const Tables &t, int ks_begin, int nks, int max_nb, int m
 }
 
 }  // namespace derek
+
+// ---------------------------------------------------------------------------
+// Rotation X <- X C on the tensor cores (BF16x3), in place per 128-G tile.
+//
+// Real form per coefficient G: with x_G = (Re X_0, Im X_0, Re X_1, ...) the
+// rotated row is y_G = M x_G, M = [[Re C, -Im C], [Im C, Re C]] per (i, j)
+// block.  A = the tile's x_G rows (M = 128 G, K = 2 nb), B = M's rows
+// (N = 2 nb): B[2j][2i] = Re C_ij, B[2j][2i+1] = -Im C_ij,
+// B[2j+1][2i] = Im C_ij, B[2j+1][2i+1] = Re C_ij.  The accumulator row G,
+// columns (2j, 2j+1) is the new coefficient X_j(G).
+// ---------------------------------------------------------------------------
+namespace derek {
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_rotate_tc(const Tables t, int ks_begin, float2 *__restrict__ X, const double2 *__restrict__ C,
+                const long long *__restrict__ mat_off, int *__restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[3];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_ok;
+  const int ksi = ks_begin + blockIdx.y;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;
+  const int g0 = blockIdx.x * TC_M;
+  if (g0 >= K.npw) return;
+  const int nb = K.nb;
+  const int N = ((2 * nb + 15) / 16) * 16;  // output columns
+  const int KT = 2 * nb;                     // contraction length (reals)
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t a_bytes = TC_M * TC_KB * 2, b_bytes = (uint32_t)N * TC_KB * 2;
+  const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+  unsigned char *stage[2] = {smem_raw, smem_raw + stage_bytes};
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(256)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = idesc_bf16(TC_M, N);
+  float2 *Xb = X + K.psi_off;
+  const double2 *Cb = C + mat_off[ksi];
+  const int nkb = (KT + TC_KB - 1) / TC_KB;
+  bool ok = true;
+  for (int kb = 0; kb < nkb; ++kb) {
+    const int s = kb & 1;
+    if (kb >= 2) {
+      if (tid == 0) s_ok = mbar_wait(&bars[s], ((kb - 2) >> 1) & 1) ? 1 : 0;
+      __syncthreads();
+      if (!s_ok) {
+        ok = false;
+        break;
+      }
+    }
+    unsigned char *A_hi = stage[s], *A_lo = A_hi + a_bytes, *B_hi = A_lo + a_bytes,
+                  *B_lo = B_hi + b_bytes;
+    const int ib = kb * (TC_KB / 2);  // first band of this K block
+    // A: row g, chunk k8 holds bands ib + 4 k8 .. +3 as (re, im) pairs
+    for (int c = tid; c < TC_M * 8; c += TC_THREADS) {
+      const int row = c % TC_M, k8 = c / TC_M;
+      const int g = g0 + row;
+      float v[8];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = ib + 4 * k8 + q;
+        float2 x = make_float2(0.f, 0.f);
+        if (g < K.npw && i < nb) x = Xb[(long long)i * K.npw_pad + g];
+        v[2 * q] = x.x;
+        v[2 * q + 1] = x.y;
+      }
+      uint4 hi, lo;
+      split8(v, hi, lo);
+      *reinterpret_cast<uint4 *>(A_hi + core_off(row, k8)) = hi;
+      *reinterpret_cast<uint4 *>(A_lo + core_off(row, k8)) = lo;
+    }
+    // B: row n = 2 j + part, chunk k8 holds bands ib + 4 k8 .. +3
+    for (int c = tid; c < N * 8; c += TC_THREADS) {
+      const int row = c >> 3, k8 = c & 7;
+      const int j = row >> 1, part = row & 1;
+      float v[8];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = ib + 4 * k8 + q;
+        double2 cij = make_double2(0.0, 0.0);
+        if (row < 2 * nb && i < nb) cij = Cb[(long long)i * nb + j];
+        if (part == 0) {
+          v[2 * q] = (float)cij.x;
+          v[2 * q + 1] = (float)(-cij.y);
+        } else {
+          v[2 * q] = (float)cij.y;
+          v[2 * q + 1] = (float)cij.x;
+        }
+      }
+      uint4 hi, lo;
+      split8(v, hi, lo);
+      *reinterpret_cast<uint4 *>(B_hi + core_off(row, k8)) = hi;
+      *reinterpret_cast<uint4 *>(B_lo + core_off(row, k8)) = lo;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t ah = smem_u32(A_hi), al = smem_u32(A_lo), bh = smem_u32(B_hi), bl = smem_u32(B_lo);
+#pragma unroll
+      for (int ks = 0; ks < TC_KB / 16; ++ks) {
+        const uint32_t o = ks * 256;
+        const uint64_t dah = smem_desc(ah + o, 128, 1024), dal = smem_desc(al + o, 128, 1024);
+        const uint64_t dbh = smem_desc(bh + o, 128, 1024), dbl = smem_desc(bl + o, 128, 1024);
+        mma_bf16(tmem, dah, dbh, idesc, (kb > 0 || ks > 0) ? 1u : 0u);
+        mma_bf16(tmem, dah, dbl, idesc, 1u);
+        mma_bf16(tmem, dal, dbh, idesc, 1u);
+      }
+      mma_commit(&bars[s]);
+    }
+  }
+  if (tid == 0) {
+    mma_commit(&bars[2]);
+    s_ok = mbar_wait(&bars[2], 0) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!s_ok) ok = false;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = quarter * 32 + (tid & 31);
+    const int g = g0 + row;
+    const int ncol_half = N / 2;  // multiple of 8
+    const int cbeg = half * ncol_half;
+    for (int c = cbeg; c < cbeg + ncol_half; c += 16) {
+      uint32_t r[16];
+      tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, r);
+      if (g < K.npw) {
+#pragma unroll
+        for (int q = 0; q < 16; q += 2) {
+          const int j = (c + q) >> 1;
+          if (c + q < 2 * nb)
+            Xb[(long long)j * K.npw_pad + g] = make_float2(__uint_as_float(r[q]), __uint_as_float(r[q + 1]));
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(status + ksi, DEREK_ERR_TIMEOUT);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+  }
+}
+
+void launch_rotate_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, float2 *X,
+                      const double2 *C, const long long *mat_off, int *status, cudaStream_t st) {
+  if (nks <= 0) return;
+  const size_t sm = overlap_tc_smem(max_nb);
+  cudaFuncSetAttribute(k_rotate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((max_npw + TC_M - 1) / TC_M, nks);
+  derek::note_launch(), k_rotate_tc<<<grid, TC_THREADS, sm, st>>>(t, ks_begin, X, C, mat_off, status);
+}
+
+}  // namespace derek

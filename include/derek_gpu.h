@@ -90,7 +90,8 @@ typedef struct {
   int    first_degree;     /* filter degree of those passes */
   uint64_t seed;           /* start-vector hash seed */
   int    use_graph;        /* capture each SCF iteration in a CUDA graph */
-  int    use_tensor_cores; /* mixed mode: tcgen05 BF16x3 contractions */
+  int    use_tensor_cores; /* mixed mode: 1 = tcgen05 BF16x3 overlaps,
+                              2 = overlaps and rotations, 0 = CUDA cores */
   double density_tol;      /* also require max|n_out - n_in| < density_tol
                               (0 = energy criterion only, as the reference) */
   int    buffer_bands;     /* extra unreported bands carried by the filtered

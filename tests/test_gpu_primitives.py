@@ -162,7 +162,8 @@ def test_overlap_tensor_cores_match_fp64(oracle, nb):
     FP32 CUDA-core path against FP64 numpy on the same (FP32-rounded) data.
     Tolerance relative to max|S|: 5e-5 for BF16x3 (hi*hi + hi*lo + lo*hi
     leaves ~2^-16 per product and the tensor-core FP32 accumulation of a
-    2048-coefficient split adds to it; measured 1.6e-5), 1e-6 for FP32."""
+    2048-coefficient split adds to it; measured 1.6e-5), 5e-6 for FP32
+    (single-precision sums over npw ~ 1000 terms; measured 1.6e-6)."""
     import derek_gb300 as dg
     L = 9.0 if nb < 50 else 12.0
     s, spec = make_pair(oracle, L=L, ecut=6.0, nb=nb, nelec=2.0)
@@ -171,7 +172,7 @@ def test_overlap_tensor_cores_match_fp64(oracle, nb):
     psi = rng.standard_normal((nb, kb.npw)) + 1j * rng.standard_normal((nb, kb.npw))
     psi32 = psi.astype(np.complex64).astype(np.complex128)
     ref = psi32.conj() @ psi32.T
-    for tc, tol in ((1, 5e-5), (0, 1e-6)):
+    for tc, tol in ((1, 5e-5), (0, 5e-6)):
         with dg.Handle(spec, precision=1, use_tensor_cores=tc, buffer_bands=0) as h:
             h.set_wfn(psi)
             got = h.wave_dot()

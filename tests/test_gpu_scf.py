@@ -50,9 +50,10 @@ def test_scf_fp64_matches_oracle(oracle, name):
     assert rel < 1e-7, rel
 
 
-def test_scf_mixed_precision_accuracy(oracle):
+@pytest.mark.parametrize("tc", [0, 1, 2])
+def test_scf_mixed_precision_accuracy(oracle, tc):
     d = load("scf_c1")
-    with make_handle(oracle, d, precision=1, density_tol=0.0) as h:
+    with make_handle(oracle, d, precision=1, density_tol=0.0, use_tensor_cores=tc) as h:
         rep = h.electronic_scf(max_scf=200, etol=1e-7)[0]
         eig = h.eigenvalues()
         rho = h.density()
