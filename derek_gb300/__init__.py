@@ -232,6 +232,13 @@ class Handle:
         _check(lib.derek_gpu_scf_iterate(self._h, rep), self._h, "scf_iterate")
         return [_abi.report_dict(r) for r in rep]
 
+    def grad_wells(self, sys=0):
+        """Hellmann-Feynman dF/d(cx, cy, cz, depth, width) per well, (nwells, 5)."""
+        nw = len(self.systems[sys].wells)
+        g = np.zeros((nw, 5))
+        _check(lib.derek_gpu_grad_wells(self._h, sys, _dptr(g)), self._h, "grad_wells")
+        return g
+
     def eigenvalues(self, sys=0):
         s = self.systems[sys]
         e = np.zeros((len(s.kpts), s.nbands))

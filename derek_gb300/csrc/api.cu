@@ -1,6 +1,7 @@
 // Handle creation and the primitive C-ABI entry points (tables, FFT, H.psi,
 // density, XC).  The SCF entry points live in scf.cu.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -44,15 +45,34 @@ __global__ void k_to_float(long long n, const double *__restrict__ a, float *__r
 }
 
 template <typename R>
+static void apply_h_class(derek_gpu *h, const Tables &t, int item_begin, int nitems, int nchunk,
+                          const int n[3], const void *in, const void *prev, void *out,
+                          const Axpby *coef, const R *vloc) {
+  launch_x_inv<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)in,
+                  (cplx<R> *)h->d_abuf, nullptr, h->stream);
+  launch_plane<R>(t, item_begin, nitems, n[0], n[1], n[2], n[1], n[2], (cplx<R> *)h->d_abuf, vloc,
+                  h->stream);
+  launch_x_fwd<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)h->d_abuf,
+                  (const cplx<R> *)in, (const cplx<R> *)prev, (cplx<R> *)out, coef, h->stream);
+}
+
+// H.psi over items [item_begin, item_begin + nitems): all items (one launch
+// per grid-size class) or the items of one k-set (a single class)
+template <typename R>
 static void apply_h_t(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
                       void *out, const Axpby *coef, const R *vloc) {
-  launch_x_inv<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const cplx<R> *)in,
-                  (cplx<R> *)h->d_abuf, nullptr, h->stream);
-  launch_plane<R>(h->tab, item_begin, nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
-                  h->min_n[2], (cplx<R> *)h->d_abuf, vloc, h->stream);
-  launch_x_fwd<R>(h->tab, item_begin, nitems, h->max_nchunk, h->max_n[0], h->min_n[0],
-                  (const cplx<R> *)h->d_abuf, (const cplx<R> *)in, (const cplx<R> *)prev,
-                  (cplx<R> *)out, coef, h->stream);
+  if (item_begin == 0 && nitems == h->nitems) {
+    for (const auto &c : h->classes) {
+      Tables t = h->tab;
+      t.item_list = c.d_list;
+      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, in, prev, out, coef, vloc);
+    }
+    return;
+  }
+  const KSetDev &K = h->ks[h->item_ks[item_begin]];
+  const SysDev &S = h->sys[K.sys];
+  apply_h_class<R>(h, h->tab, item_begin, nitems, (K.ncol + kColChunk - 1) / kColChunk, S.n, in,
+                   prev, out, coef, vloc);
 }
 
 int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
@@ -66,8 +86,12 @@ int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, cons
 }
 
 template <typename R> static void density_t(derek_gpu *h, const void *psi) {
-  launch_x_inv<R>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const cplx<R> *)psi,
-                  (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
+  for (const auto &c : h->classes) {
+    Tables t = h->tab;
+    t.item_list = c.d_list;
+    launch_x_inv<R>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const cplx<R> *)psi,
+                    (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
+  }
   launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
                           (const cplx<R> *)h->d_abuf, h->d_occw, h->d_partial, h->d_partial_off,
                           h->stream);
@@ -155,9 +179,12 @@ int derek_gpu_destroy(derek_gpu_t *h) {
                   h->d_vloc32, h->d_rho_in, h->d_rho_out, h->d_exc,       h->d_vxc,
                   h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
                   h->d_Yp,    h->d_HX,      h->d_abuf,    h->d_occw,      h->d_eig,
-                  h->d_occ,   h->d_coef};
+                  h->d_occ,   h->d_coef,    h->d_cells,   h->d_wells,     h->d_well_off,
+                  h->d_hfpart, h->d_hfgrad};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  for (auto &c : h->classes)
+    if (c.d_list) cudaFree(c.d_list);
   derek_scf_free(h);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -284,6 +311,10 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       v.assign(d.vext, d.vext + S.nr);
     else
       build_vext(d.cell, nfine, d.nelec, d.nwells, d.wells, v);
+    h->well_off.push_back((int)(h->wells_host.size() / 5));
+    if (d.nwells > 0 && d.wells) h->wells_host.insert(h->wells_host.end(), d.wells, d.wells + 5 * d.nwells);
+    h->wells_define_vext.push_back(d.vext == nullptr);
+    h->max_wells = std::max(h->max_wells, d.nwells > 0 && d.wells ? d.nwells : 0);
     h->vext_host.insert(h->vext_host.end(), v.begin(), v.end());
 
     for (int k = 0; k < d.nk; ++k) {
@@ -367,6 +398,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     }
     h->sys.push_back(S);
   }
+  h->well_off.push_back((int)(h->wells_host.size() / 5));
   h->nks = (int)h->ks.size();
   h->total_psi = psi_off;
   h->total_abuf = a_off;
@@ -397,6 +429,15 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     CK(upload(&h->d_tw32, t32));
   }
   CK(upload(&h->d_vext, h->vext_host));
+  {
+    std::vector<double> cells;
+    for (int s = 0; s < nsys; ++s) cells.insert(cells.end(), desc[s].cell, desc[s].cell + 9);
+    CK(upload(&h->d_cells, cells));
+    CK(upload(&h->d_wells, h->wells_host));
+    CK(upload(&h->d_well_off, h->well_off));
+    CK(cudaMalloc((void **)&h->d_hfpart, (size_t)nsys * 64 * std::max(h->max_wells, 1) * 5 * sizeof(double)));
+    CK(cudaMalloc((void **)&h->d_hfgrad, std::max<size_t>(h->wells_host.size(), 1) * sizeof(double)));
+  }
   CK(upload(&h->d_partial_off, partial_off));
   const size_t gbytes = (size_t)grid_off * sizeof(double);
   CK(cudaMalloc((void **)&h->d_vloc, gbytes));
@@ -441,6 +482,28 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   h->tab.rows = h->d_rows;
   h->tab.tw64 = h->d_tw64;
   h->tab.tw32 = h->d_tw32;
+  h->tab.item_list = nullptr;
+  {
+    // group items by grid size; a single class over all items needs no list
+    std::map<std::array<int, 3>, std::vector<int>> groups;
+    std::map<std::array<int, 3>, int> chunks;
+    for (int it = 0; it < h->nitems; ++it) {
+      const KSetDev &K = h->ks[h->item_ks[it]];
+      const SysDev &S = h->sys[K.sys];
+      const std::array<int, 3> key = {S.n[0], S.n[1], S.n[2]};
+      groups[key].push_back(it);
+      chunks[key] = std::max(chunks[key], (K.ncol + kColChunk - 1) / kColChunk);
+    }
+    for (auto &g : groups) {
+      derek_gpu::ItemClass c{};
+      for (int i = 0; i < 3; ++i) c.n[i] = g.first[i];
+      c.count = (int)g.second.size();
+      c.nchunk = chunks[g.first];
+      c.d_list = nullptr;
+      if (groups.size() > 1) CK(upload(&c.d_list, g.second));
+      h->classes.push_back(c);
+    }
+  }
   if (refresh_vloc32(h) != DEREK_OK) FAIL(DEREK_ERR_CUDA, h->last_error);
   int st = derek_scf_alloc(h);
   if (st != DEREK_OK) FAIL(st, h->last_error);
@@ -685,26 +748,37 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
   const void *in = h->cur_psi();
   for (int r = 0; r < nrep; ++r) {
     cudaEventRecord(ev[0], h->stream);
-    if (h->prec == DEREK_PREC_FP64) {
-      launch_x_inv<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const double2 *)in,
-                           (double2 *)h->d_abuf, nullptr, h->stream);
-      cudaEventRecord(ev[1], h->stream);
-      launch_plane<double>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
-                           h->min_n[2], (double2 *)h->d_abuf, h->d_vloc, h->stream);
-      cudaEventRecord(ev[2], h->stream);
-      launch_x_fwd<double>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0],
-                           (const double2 *)h->d_abuf, (const double2 *)in, nullptr,
-                           (double2 *)h->d_HX, nullptr, h->stream);
-    } else {
-      launch_x_inv<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0], (const float2 *)in,
-                          (float2 *)h->d_abuf, nullptr, h->stream);
-      cudaEventRecord(ev[1], h->stream);
-      launch_plane<float>(h->tab, 0, h->nitems, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
-                          h->min_n[2], (float2 *)h->d_abuf, h->d_vloc32, h->stream);
-      cudaEventRecord(ev[2], h->stream);
-      launch_x_fwd<float>(h->tab, 0, h->nitems, h->max_nchunk, h->max_n[0], h->min_n[0],
-                          (const float2 *)h->d_abuf, (const float2 *)in, nullptr,
-                          (float2 *)h->d_HX, nullptr, h->stream);
+    for (const auto &c : h->classes) {
+      Tables t = h->tab;
+      t.item_list = c.d_list;
+      if (h->prec == DEREK_PREC_FP64)
+        launch_x_inv<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const double2 *)in,
+                             (double2 *)h->d_abuf, nullptr, h->stream);
+      else
+        launch_x_inv<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const float2 *)in,
+                            (float2 *)h->d_abuf, nullptr, h->stream);
+    }
+    cudaEventRecord(ev[1], h->stream);
+    for (const auto &c : h->classes) {
+      Tables t = h->tab;
+      t.item_list = c.d_list;
+      if (h->prec == DEREK_PREC_FP64)
+        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2],
+                             (double2 *)h->d_abuf, h->d_vloc, h->stream);
+      else
+        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2],
+                            (float2 *)h->d_abuf, h->d_vloc32, h->stream);
+    }
+    cudaEventRecord(ev[2], h->stream);
+    for (const auto &c : h->classes) {
+      Tables t = h->tab;
+      t.item_list = c.d_list;
+      if (h->prec == DEREK_PREC_FP64)
+        launch_x_fwd<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const double2 *)h->d_abuf,
+                             (const double2 *)in, nullptr, (double2 *)h->d_HX, nullptr, h->stream);
+      else
+        launch_x_fwd<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const float2 *)h->d_abuf,
+                            (const float2 *)in, nullptr, (float2 *)h->d_HX, nullptr, h->stream);
     }
     cudaEventRecord(ev[3], h->stream);
     DEREK_CUDA(h, cudaEventSynchronize(ev[3]));

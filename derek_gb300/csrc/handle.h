@@ -84,6 +84,23 @@ struct derek_gpu {
   int graph_degree = -1;
   long long graph_nodes[3] = {0, 0, 0};
 
+  // ---- Gaussian wells (Hellmann-Feynman gradient)
+  std::vector<double> wells_host;   // 5 per well, all systems
+  std::vector<int> well_off;        // nsys + 1
+  std::vector<int> wells_define_vext;
+  int max_wells = 0;
+  double *d_wells = nullptr, *d_cells = nullptr, *d_hfpart = nullptr, *d_hfgrad = nullptr;
+  int *d_well_off = nullptr;
+
+  // ---- items grouped by grid size (one launch per class on uneven batches)
+  struct ItemClass {
+    int n[3];
+    int count;
+    int nchunk;
+    int *d_list;   // nullptr when the class is the contiguous range of all items
+  };
+  std::vector<ItemClass> classes;
+
   cudaStream_t stream = nullptr;
   std::string last_error;
 

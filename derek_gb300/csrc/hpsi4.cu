@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256) k_x_inv(Tables t, int item_begin, const c
                                                cplx<R> *__restrict__ abuf,
                                                const double *__restrict__ occ_skip) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int item = item_begin + blockIdx.x;
+  const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
   const int ksi = t.item_ks[item];
   const KSetDev &K = t.ks[ksi];
   const int c0 = blockIdx.y * kCC;
@@ -81,7 +81,7 @@ template <typename R>
 __global__ void __launch_bounds__(512) k_plane(Tables t, int item_begin, cplx<R> *__restrict__ abuf,
                                                const R *__restrict__ vloc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int item = item_begin + blockIdx.x;
+  const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
   const int x = blockIdx.y;
   const int ksi = t.item_ks[item];
   const KSetDev &K = t.ks[ksi];
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(512) k_plane_fixed(Tables t, int item_begin, c
                                                      const R *__restrict__ vloc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int PZ = N + 1;
-  const int item = item_begin + blockIdx.x;
+  const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
   const int x = blockIdx.y;
   const int ksi = t.item_ks[item];
   const KSetDev &K = t.ks[ksi];
@@ -156,6 +156,105 @@ __global__ void __launch_bounds__(512) k_plane_fixed(Tables t, int item_begin, c
   for (int c = threadIdx.x; c < K.ncol; c += blockDim.x) a[c] = P[cy[c] * PZ + cz[c]];
 }
 
+// (y,z) pass for n2 = n3 = N known at compile time, with the backward and
+// forward y transforms of a column fused around V(r).  The backward transform
+// uses N = A * B (step 1 radix A, step 2 radix B); its step-2 thread for k1
+// holds X[k1 + A k2], k2 < B, which is exactly the step-1 input of a forward
+// transform factored the other way (N = B * A, n2' = k1, n1' = k2).  So the
+// column goes  step1_bwd -> [smem] -> step2_bwd * V -> step1_fwd -> [smem]
+// -> step2_fwd  with V(r) applied in registers and no block barrier between.
+template <typename R, int N, int NT>
+__global__ void __launch_bounds__(NT) k_plane_fused(Tables t, int item_begin, cplx<R> *__restrict__ abuf,
+                                                    const R *__restrict__ vloc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int PZ = N + 1;
+  constexpr int A = plan_a(N);
+  constexpr int B = N / A;
+  constexpr int SPAN = A > B ? A : B;
+  constexpr int G = 32 / SPAN;
+  const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
+  const int x = blockIdx.y;
+  const int ksi = t.item_ks[item];
+  const KSetDev &K = t.ks[ksi];
+  const SysDev &S = t.sys[K.sys];
+  if (!S.active) return;
+  const int n1 = S.n[0];
+  if (x >= n1) return;
+  const int b = t.item_band[item];
+  cplx<R> *P = reinterpret_cast<cplx<R> *>(smem_raw);
+  cplx<R> *tw = P + N * PZ;
+  for (int i = threadIdx.x; i < N * PZ; i += NT) P[i] = mk<R>(0, 0);
+  for (int i = threadIdx.x; i < N; i += NT) tw[i] = twtab<R>(t)[S.lp[1].tw_off + i];
+  __syncthreads();
+  cplx<R> *a = abuf + K.a_off + ((long long)b * n1 + x) * K.ncol_pad;
+  const short *cy = t.col_y + K.col_off;
+  const short *cz = t.col_z + K.col_off;
+  for (int c = threadIdx.x; c < K.ncol; c += NT) P[cy[c] * PZ + cz[c]] = a[c];
+  __syncthreads();
+  const short *rows = t.rows + K.row_off;
+  fft4_fixed<R, +1, N, 1, PZ>(P, K.nrow, rows, tw);  // backward z on the rows with columns
+  const R *v = vloc + S.grid_off + (long long)x * N * N;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane / SPAN, r = lane - g * SPAN;
+  for (int l0 = warp * G; l0 < N; l0 += (NT / 32) * G) {
+    const int z = l0 + g;
+    const bool live = g < G && z < N;
+    cplx<R> *col = P + (live ? z : 0);
+    // backward step 1: radix A over n1 for n2 = r
+    if (live && r < B) {
+      cplx<R> u[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) u[n1] = col[(B * n1 + r) * PZ];
+      Dft<R, A, +1>::run(u);
+#pragma unroll
+      for (int k1 = 1; k1 < A; ++k1) {
+        cplx<R> w = tw[(r * k1) % N];
+        w.y = -w.y;
+        u[k1] = cmul<R>(u[k1], w);
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) col[(B * k1 + r) * PZ] = u[k1];
+    }
+    __syncwarp();
+    // backward step 2 (radix B) for k1 = r, times V, forward step 1 (radix B)
+    cplx<R> u[B];
+    const bool act = live && r < A;
+    if (act) {
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) u[n2] = col[(B * r + n2) * PZ];
+    }
+    __syncwarp();
+    if (act) {
+      Dft<R, B, +1>::run(u);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) u[k2] = cscale<R>(u[k2], v[(r + A * k2) * N + z]);
+      Dft<R, B, -1>::run(u);
+#pragma unroll
+      for (int k1 = 1; k1 < B; ++k1) u[k1] = cmul<R>(u[k1], tw[(r * k1) % N]);
+#pragma unroll
+      for (int k1 = 0; k1 < B; ++k1) col[(A * k1 + r) * PZ] = u[k1];
+    }
+    __syncwarp();
+    // forward step 2 (radix A) for k1' = r < B: natural-order output r + B k2
+    cplx<R> q[A];
+    const bool act2 = live && r < B;
+    if (act2) {
+#pragma unroll
+      for (int n2 = 0; n2 < A; ++n2) q[n2] = col[(A * r + n2) * PZ];
+    }
+    __syncwarp();
+    if (act2) {
+      Dft<R, A, -1>::run(q);
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) col[(r + B * k2) * PZ] = q[k2];
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  fft4_fixed<R, -1, N, 1, PZ>(P, K.nrow, rows, tw);  // forward z on the rows needed
+  for (int c = threadIdx.x; c < K.ncol; c += NT) a[c] = P[cy[c] * PZ + cz[c]];
+}
+
 // ---- pass 3: forward x transforms, gather, kinetic, epilogue --------------
 template <typename R, int NX>
 __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const cplx<R> *__restrict__ abuf,
@@ -164,7 +263,7 @@ __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const c
                                                cplx<R> *__restrict__ out,
                                                const Axpby *__restrict__ coef) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int item = item_begin + blockIdx.x;
+  const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
   const int ksi = t.item_ks[item];
   const KSetDev &K = t.ks[ksi];
   const int c0 = blockIdx.y * kCC;
@@ -324,8 +423,9 @@ static bool try_plane_fixed(const Tables &t, int item_begin, int nitems, int max
                             cudaStream_t st) {
   if (max_n2 != N || max_n3 != N || min_n2 != N || min_n3 != N) return false;
   const size_t sm = ((size_t)N * (N + 1) + N) * sizeof(cplx<R>);
-  cudaFuncSetAttribute(k_plane_fixed<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  derek::note_launch(), k_plane_fixed<R, N><<<dim3(nitems, max_n1), 512, sm, st>>>(t, item_begin, abuf, vloc);
+  constexpr int NT = 384;
+  cudaFuncSetAttribute(k_plane_fused<R, N, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  derek::note_launch(), k_plane_fused<R, N, NT><<<dim3(nitems, max_n1), NT, sm, st>>>(t, item_begin, abuf, vloc);
   return true;
 }
 

@@ -21,6 +21,7 @@ struct Tables {
   const short *rows;      // per k-set: the y rows holding columns
   const double2 *tw64;    // twiddle tables exp(-2 pi i t/n)
   const float2 *tw32;
+  const int *item_list;   // optional: block x -> item (one grid-size class)
 };
 
 template <typename R> __device__ __forceinline__ const cplx<R> *twtab(const Tables &t);

@@ -390,4 +390,20 @@ int derek_gpu_get_density(derek_gpu_t *h, int s, double *rho) {
   return DEREK_OK;
 }
 
+int derek_gpu_grad_wells(derek_gpu_t *h, int s, double *grad) {
+  if (!h || s < 0 || s >= h->nsys || !grad) return DEREK_ERR_BAD_ARG;
+  const int nw = h->well_off[s + 1] - h->well_off[s];
+  if (nw == 0 || !h->wells_define_vext[s]) {
+    h->last_error = "system has no Gaussian wells defining its external potential";
+    return DEREK_ERR_BAD_ARG;
+  }
+  launch_hf_gradient(h->tab, h->nsys, h->d_rho_out, h->d_wells, h->d_well_off, h->d_cells,
+                     h->d_hfpart, h->max_wells, h->d_hfgrad, h->stream);
+  DEREK_CUDA(h, cudaGetLastError());
+  DEREK_CUDA(h, cudaMemcpyAsync(grad, h->d_hfgrad + 5 * h->well_off[s], (size_t)nw * 5 * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
 }  // extern "C"

@@ -607,3 +607,86 @@ void launch_uniform_density(const Tables &t, int nsys, int max_nr, double *rho, 
 }
 
 }  // namespace derek
+
+namespace derek {
+
+// ---- Hellmann-Feynman gradient of the free energy with respect to the
+// Gaussian-well parameters: dF/dp = int n(r) dV_ext/dp dr at self-consistency.
+// V_ext = 0.5 Ne / N - sum_w U_w exp(-|r - R_w|^2 / (2 s_w^2)), r sampled at
+// frac = (i+1)/n (the reference's real grid, Source/basis.f90:156-188) with
+// the minimum-image displacement d = frac - c - rint(frac - c), r = cell d:
+//   dV/dU   = -e,   dV/ds = -U e |r|^2 / s^3,
+//   dV/dc_a = -U e (r . a_a) / s^2   (a_a = lattice vector a, c fractional).
+// Output per well: (dF/dcx, dF/dcy, dF/dcz, dF/dU, dF/ds).
+__global__ void __launch_bounds__(256) k_hf_partials(const Tables t, const double *__restrict__ rho,
+                                                     const double *__restrict__ wells,
+                                                     const int *__restrict__ well_off,
+                                                     const double *__restrict__ cells,
+                                                     double *__restrict__ part, int max_wells) {
+  __shared__ double red[256];
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  const int n1 = S.n[0], n2 = S.n[1], n3 = S.n[2];
+  const long long n = S.nr;
+  const long long chunk = (n + RB - 1) / RB;
+  const long long r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+  const double *cell = cells + 9 * s;  // column-major
+  const int w0 = well_off[s], nw = well_off[s + 1] - w0;
+  for (int w = 0; w < nw; ++w) {
+    const double *p = wells + 5 * (w0 + w);
+    const double cx = p[0], cy = p[1], cz = p[2], U = p[3], sw = p[4];
+    const double inv2 = 1.0 / (2.0 * sw * sw);
+    double q[5] = {0, 0, 0, 0, 0};
+    for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      const int iz = (int)(r % n3), iy = (int)((r / n3) % n2), ix = (int)(r / ((long long)n2 * n3));
+      double dx = (double)(ix + 1) / n1 - cx;
+      dx -= nearbyint(dx);
+      double dy = (double)(iy + 1) / n2 - cy;
+      dy -= nearbyint(dy);
+      double dz = (double)(iz + 1) / n3 - cz;
+      dz -= nearbyint(dz);
+      double rv[3], r2 = 0.0;
+      for (int i = 0; i < 3; ++i) {
+        rv[i] = cell[i] * dx + cell[3 + i] * dy + cell[6 + i] * dz;
+        r2 += rv[i] * rv[i];
+      }
+      const double e = exp(-r2 * inv2);
+      const double nr = rho[S.grid_off + r];
+      for (int a = 0; a < 3; ++a) {
+        const double ra = rv[0] * cell[3 * a] + rv[1] * cell[3 * a + 1] + rv[2] * cell[3 * a + 2];
+        q[a] += nr * (-U * e * ra / (sw * sw));
+      }
+      q[3] += nr * (-e);
+      q[4] += nr * (-U * e * r2 / (sw * sw * sw));
+    }
+    for (int a = 0; a < 5; ++a) {
+      const double v = block_sum(q[a], red);
+      if (threadIdx.x == 0) part[(((long long)s * RB + blockIdx.x) * max_wells + w) * 5 + a] = v;
+    }
+  }
+}
+
+__global__ void k_hf_final(const Tables t, int nsys, const double *__restrict__ part,
+                           const int *__restrict__ well_off, double *__restrict__ grad,
+                           int max_wells) {
+  const int s = blockIdx.x;
+  if (s >= nsys) return;
+  const SysDev &S = t.sys[s];
+  const int w0 = well_off[s], nw = well_off[s + 1] - w0;
+  const double dv = S.volume / S.nr;
+  for (int e = threadIdx.x; e < nw * 5; e += blockDim.x) {
+    double acc = 0;
+    for (int b = 0; b < RB; ++b) acc += part[((long long)s * RB + b) * max_wells * 5 + e];
+    grad[5 * w0 + e] = dv * acc;
+  }
+}
+
+void launch_hf_gradient(const Tables &t, int nsys, const double *rho, const double *wells,
+                        const int *well_off, const double *cells, double *part, int max_wells,
+                        double *grad, cudaStream_t s) {
+  if (max_wells <= 0) return;
+  derek::note_launch(), k_hf_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, rho, wells, well_off, cells, part, max_wells);
+  derek::note_launch(), k_hf_final<<<nsys, 128, 0, s>>>(t, nsys, part, well_off, grad, max_wells);
+}
+
+}  // namespace derek

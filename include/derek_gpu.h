@@ -192,6 +192,14 @@ void *derek_gpu_stream(derek_gpu_t *h);
 unsigned long long derek_gpu_launch_count(void);
 int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage);
 
+/* Hellmann-Feynman gradient of the converged free energy with respect to the
+ * Gaussian-well parameters of sys: dF/dp = int n(r) dV_ext/dp dr.  Writes
+ * (dF/dcx, dF/dcy, dF/dcz, dF/ddepth, dF/dwidth) per well (nwells*5).  The
+ * reference parses these wells ($data gaussian_pot, Source/io.f90:1888-1922)
+ * but never uses them (Source/pot.f90:165-166).  Needs a system whose V_ext
+ * was built from its wells and a converged SCF. */
+int derek_gpu_grad_wells(derek_gpu_t *h, int sys, double *grad);
+
 /* Results of the last SCF iteration. */
 int derek_gpu_get_eigenvalues(derek_gpu_t *h, int sys, double *eig /* nk*nb */);
 int derek_gpu_get_occupations(derek_gpu_t *h, int sys, double *occ /* nk*nb */);

@@ -113,3 +113,25 @@ def test_nan_in_potential_is_reported(oracle):
         with pytest.raises(dg.DerekError) as e:
             h.electronic_scf(max_scf=5, etol=1e-8)
         assert e.value.status in (dg._abi.DEREK_ERR_NAN, dg._abi.DEREK_ERR_CHOLESKY)
+
+
+def test_uneven_batch_scf_matches_single_systems():
+    """Several independent systems with different cells, grids, electron
+    counts and k-point sets converge in one batched SCF to the same free
+    energies as when each runs alone (FP64, 1e-9 Ha)."""
+    import derek_gb300 as dg
+    from derek_gb300 import workloads
+    specs, mix = workloads.uneven(count=5, seed=7)
+    # keep the test small: smaller cells and cutoff, at most 4 k-points
+    small = []
+    for i, s in enumerate(specs):
+        L = 6.0 + i * 0.7
+        small.append(dg.SystemSpec(np.eye(3) * L, 5.0, s.kpts[:4], s.nbands // 2 + 2,
+                                   min(s.nelec, 8.0), kT=0.01, wells=s.wells[:3]))
+    with dg.Handle(small, precision=dg.DEREK_PREC_FP64, density_tol=1e-9, **mix) as h:
+        batch = h.electronic_scf(max_scf=300, etol=1e-11)
+    for s, rb in zip(small, batch):
+        assert rb["converged"]
+        with dg.Handle(s, precision=dg.DEREK_PREC_FP64, density_tol=1e-9, **mix) as h1:
+            r1 = h1.electronic_scf(max_scf=300, etol=1e-11)[0]
+        assert abs(rb["free_energy"] - r1["free_energy"]) < 1e-9, (rb["free_energy"], r1["free_energy"])
