@@ -86,6 +86,7 @@ SIGNATURES = {
     "derek_gpu_density": (_i, [_vp, _i, _pd, _pd]),
     "derek_gpu_xc_lda": (_i, [_vp, ctypes.c_long, _pd, _pd, _pd]),
     "derek_gpu_overlap": (_i, [_vp, _i, _i, _pd]),
+    "derek_gpu_overlap_noalloc": (_i, [_vp, _vp, _i, _i, ctypes.c_long, _i, _vp, _vp]),
     "derek_gpu_scf_iterate": (_i, [_vp, ctypes.POINTER(ScfReport)]),
     "derek_gpu_scf_run": (_i, [_vp, _i, _d, ctypes.POINTER(ScfReport)]),
     "derek_gpu_grad_wells": (_i, [_vp, _i, _pd]),

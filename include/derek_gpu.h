@@ -169,6 +169,22 @@ int derek_gpu_xc_lda(derek_gpu_t *h, long n, const double *rho, double *exc,
  * The reference's wave_dot_* (Source/wave.f90:929-1036), as a full matrix. */
 int derek_gpu_overlap(derek_gpu_t *h, int sys, int k, double *s);
 
+/* Overlap S = X^H Y that allocates nothing, for callers that cannot call
+ * cudaMalloc (a host code that owns the device memory pool, or that forbids
+ * allocation once its set-up is done).  No counterpart in the reference: the
+ * handle path above allocates its split-K scratch at derek_gpu_create, this
+ * variant keeps it in a 4 MiB file-scope device array instead.
+ *   x, y     device pointers, nb rows of npw coefficients, row stride ld
+ *            (complex128 for DEREK_PREC_FP64, complex64 for DEREK_PREC_MIXED)
+ *   s        device pointer, nb x nb complex128, s[i*nb + j] = <x_i|y_j>
+ *   stream   cudaStream_t to launch on (NULL = default stream)
+ * Limits: nb <= 128 and npw <= 16 * 4096 = 65536, else DEREK_ERR_UNSUPPORTED.
+ * The first call on a device looks up the array's device address, so make
+ * that first call before any stream capture.  Calls share the array: calls
+ * that overlap on the GPU race and give wrong results. */
+int derek_gpu_overlap_noalloc(const void *x, const void *y, int nb, int npw, long ld,
+                              int precision, void *s, void *stream);
+
 /* Self-consistent field.  scf_iterate runs one iteration on every active
  * system; scf_run iterates until |dF| < etol or max_scf iterations
  * (Source/electronic.f90:86-175).  rep has one entry per system. */
