@@ -44,7 +44,7 @@ sys.path.insert(0, ROOT)
 METRIC = "converged ground states/sec at |dE|<1e-6 Ha/e vs FP64 path"
 UNIT = "ground_states/s"
 WORKLOAD = "kpts64: L=16 bohr, Ecut=20 Ha, 72^3 grid, 4x4x4 MP (64 k), 64 e / 80 bands, 16 wells"
-ETOL_PER_E = 1e-6    # Ha per electron: SCF stops at |F - F_prev| < ETOL_PER_E * N_e
+ETOL_PER_E = 1e-7    # Ha per electron: SCF stops at |F - F_prev| < ETOL_PER_E * N_e
 FP64_TOL = 1e-6      # Ha per electron: |F_mixed - F_FP64| / N_e must stay below
 
 
@@ -229,7 +229,7 @@ def run_ours(args):
         "value": round(value, 4),
         "ms_per_step": round(ms / args.steps, 2),
         "config": {"workload": WORKLOAD, "precision": "mixed", "etol_Ha": ETOL,
-                   "etol_rule": "|F - F_prev| < 1e-6 Ha x N_e",
+                   "etol_rule": "|F - F_prev| < 1e-7 Ha x N_e",
                    "iterations": iters, "chebyshev_degree": scf_opts["cheb_degree"],
                    "l2": "inputs larger than L2 (planes buffer ~7 GB), no flush",
                    "parallelism": f"replicas x{args.gpus}"},

@@ -92,9 +92,9 @@ template <typename R> static void density_t(derek_gpu *h, const void *psi) {
     launch_x_inv<R>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const cplx<R> *)psi,
                     (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
   }
-  launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2],
-                          (const cplx<R> *)h->d_abuf, h->d_occw, h->d_partial, h->d_partial_off,
-                          h->stream);
+  launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
+                          h->min_n[2], (const cplx<R> *)h->d_abuf, h->d_occw, h->d_partial,
+                          h->d_partial_off, h->stream);
 }
 
 int density_items(derek_gpu *h, const void *psi, double *rho) {
@@ -292,7 +292,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     }
     S.nr = nfine[0] * nfine[1] * nfine[2];
     S.nk = d.nk;
-    const int nbuf = h->opts.buffer_bands >= 0 ? h->opts.buffer_bands : std::max(4, (d.nbands + 9) / 10);
+    const int nbuf = h->opts.buffer_bands >= 0 ? h->opts.buffer_bands : std::max(4, (d.nbands + 19) / 20);
     const int nbi = d.nbands + nbuf;
     S.nb = nbi;
     S.nbr = d.nbands;
@@ -483,6 +483,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   h->tab.tw64 = h->d_tw64;
   h->tab.tw32 = h->d_tw32;
   h->tab.item_list = nullptr;
+  h->tab.item_shift = nullptr;
   {
     // group items by grid size; a single class over all items needs no list
     std::map<std::array<int, 3>, std::vector<int>> groups;

@@ -294,16 +294,18 @@ __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const c
   const R *kin = kintab<R>(t) + K.ent_off;
   const long long off = K.psi_off + (long long)b * K.npw_pad;
   const R inv_n = (R)(1.0 / (double)S.nr);
-  R al = 1, be = 0, ga = 0;
+  R al = 1, be = 0, ga = 0, tk = 1;
   if (coef) {
     al = (R)coef[ksi].alpha;
     be = (R)coef[ksi].beta;
     ga = (R)coef[ksi].gamma;
+    tk = (R)coef[ksi].tk;
   }
+  if (t.item_shift) be += (R)t.item_shift[item];
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const cplx<R> p = psi[off + e];
     const cplx<R> f = L[(ecol[e] - c0) * pl + eix[e]];
-    const R k = kin[e];
+    const R k = tk * kin[e];
     const R hx = f.x * inv_n + k * p.x;
     const R hy = f.y * inv_n + k * p.y;
     R ox = al * hx + be * p.x;
@@ -362,6 +364,51 @@ __global__ void __launch_bounds__(512) k_density_plane(Tables t, int ks_begin, c
   __syncthreads();
   double *dst = partial + partial_off[ksi] + (long long)x * n2 * n3;
   for (int i = threadIdx.x; i < n2 * n3; i += blockDim.x) dst[i] = acc[i];
+}
+
+// Density pass for n2 = n3 = N known at compile time.
+template <typename R, int N, int NT>
+__global__ void __launch_bounds__(NT) k_density_fixed(Tables t, int ks_begin, const cplx<R> *__restrict__ abuf,
+                                                      const double *__restrict__ occ,
+                                                      double *__restrict__ partial,
+                                                      const long long *__restrict__ partial_off) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int PZ = N + 1;
+  const int ksi = ks_begin + blockIdx.x;
+  const int x = blockIdx.y;
+  const KSetDev &K = t.ks[ksi];
+  const SysDev &S = t.sys[K.sys];
+  if (!S.active) return;
+  const int n1 = S.n[0];
+  if (x >= n1) return;
+  double *acc = reinterpret_cast<double *>(smem_raw);
+  cplx<R> *P = reinterpret_cast<cplx<R> *>(acc + N * N);
+  cplx<R> *tw = P + N * PZ;
+  for (int i = threadIdx.x; i < N * N; i += NT) acc[i] = 0.0;
+  for (int i = threadIdx.x; i < N; i += NT) tw[i] = twtab<R>(t)[S.lp[1].tw_off + i];
+  const short *cy = t.col_y + K.col_off;
+  const short *cz = t.col_z + K.col_off;
+  const short *rows = t.rows + K.row_off;
+  for (int b = 0; b < K.nb; ++b) {
+    const double w = occ[K.item0 + b];
+    if (w == 0.0) continue;
+    __syncthreads();
+    for (int i = threadIdx.x; i < N * PZ; i += NT) P[i] = mk<R>(0, 0);
+    __syncthreads();
+    const cplx<R> *a = abuf + K.a_off + ((long long)b * n1 + x) * K.ncol_pad;
+    for (int c = threadIdx.x; c < K.ncol; c += NT) P[cy[c] * PZ + cz[c]] = a[c];
+    __syncthreads();
+    fft4_fixed<R, +1, N, 1, PZ>(P, K.nrow, rows, tw);
+    fft4_fixed<R, +1, N, PZ, 1>(P, N, nullptr, tw);
+    for (int i = threadIdx.x; i < N * N; i += NT) {
+      const int y = i / N, z = i - y * N;
+      const cplx<R> c = P[y * PZ + z];
+      acc[i] += w * ((double)c.x * (double)c.x + (double)c.y * (double)c.y);
+    }
+  }
+  __syncthreads();
+  double *dst = partial + partial_off[ksi] + (long long)x * N * N;
+  for (int i = threadIdx.x; i < N * N; i += NT) dst[i] = acc[i];
 }
 
 // ---- launchers --------------------------------------------------------------
@@ -444,11 +491,29 @@ void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int m
 }
 
 
+template <typename R, int N>
+static bool try_density_fixed(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2,
+                              int max_n3, int min_n2, int min_n3, const cplx<R> *abuf,
+                              const double *occ, double *partial, const long long *partial_off,
+                              cudaStream_t st) {
+  if (max_n2 != N || max_n3 != N || min_n2 != N || min_n3 != N) return false;
+  constexpr int NT = 384;
+  const size_t sm = (size_t)N * N * sizeof(double) + ((size_t)N * (N + 1) + N) * sizeof(cplx<R>);
+  cudaFuncSetAttribute(k_density_fixed<R, N, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  derek::note_launch(), k_density_fixed<R, N, NT><<<dim3(nks, max_n1), NT, sm, st>>>(t, ks_begin, abuf, occ, partial, partial_off);
+  return true;
+}
+
 template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
-                          const cplx<R> *abuf, const double *occ, double *partial,
-                          const long long *partial_off, cudaStream_t st) {
+                          int min_n2, int min_n3, const cplx<R> *abuf, const double *occ,
+                          double *partial, const long long *partial_off, cudaStream_t st) {
   if (nks <= 0) return;
+  if (try_density_fixed<R, 72>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
+      try_density_fixed<R, 64>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
+      try_density_fixed<R, 48>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
+      try_density_fixed<R, 32>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st))
+    return;
   const size_t sm = (size_t)max_n2 * max_n3 * sizeof(double) + smem_plane<R>(max_n2, max_n3);
   cudaFuncSetAttribute(k_density_plane<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   derek::note_launch(), k_density_plane<R><<<dim3(nks, max_n1), 512, sm, st>>>(t, ks_begin, abuf, occ, partial, partial_off);
@@ -462,8 +527,9 @@ void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, in
   template void launch_x_fwd<R>(const Tables &, int, int, int, int, int, const cplx<R> *,        \
                                 const cplx<R> *, const cplx<R> *, cplx<R> *, const Axpby *,      \
                                 cudaStream_t);                                                    \
-  template void launch_density_plane<R>(const Tables &, int, int, int, int, int, const cplx<R> *, \
-                                        const double *, double *, const long long *, cudaStream_t);
+  template void launch_density_plane<R>(const Tables &, int, int, int, int, int, int, int,        \
+                                        const cplx<R> *, const double *, double *,                \
+                                        const long long *, cudaStream_t);
 DEREK_INST(float)
 DEREK_INST(double)
 #undef DEREK_INST

@@ -22,6 +22,7 @@ struct Tables {
   const double2 *tw64;    // twiddle tables exp(-2 pi i t/n)
   const float2 *tw32;
   const int *item_list;   // optional: block x -> item (one grid-size class)
+  const double *item_shift;  // optional: per-item extra beta in the H.psi epilogue
 };
 
 template <typename R> __device__ __forceinline__ const cplx<R> *twtab(const Tables &t);
@@ -32,9 +33,10 @@ template <> __device__ __forceinline__ const float *kintab<float>(const Tables &
 template <> __device__ __forceinline__ const double *kintab<double>(const Tables &t) { return t.kin64; }
 
 // Per-k-set coefficients of the fused H.psi epilogue:
-//   out = alpha * (H psi) + beta * psi + gamma * prev
+//   out = alpha * (tk T psi + V psi) + (beta + shift[item]) * psi + gamma * prev
+// (tk = 1 is H; tk = 0 applies the potential alone).
 struct Axpby {
-  double alpha, beta, gamma;
+  double alpha, beta, gamma, tk;
 };
 
 // ---- H.psi and density pipeline (hpsi4.cu) --------------------------------
@@ -54,8 +56,8 @@ void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, i
                   cplx<R> *out, const Axpby *coef, cudaStream_t st);
 template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
-                          const cplx<R> *abuf, const double *occ, double *partial,
-                          const long long *partial_off, cudaStream_t st);
+                          int min_n2, int min_n3, const cplx<R> *abuf, const double *occ,
+                          double *partial, const long long *partial_off, cudaStream_t st);
 constexpr int kColChunk = 64;   // columns per x-line chunk (kCC in hpsi4.cu)
 
 // ---- full-grid FFT (grid.cu) -----------------------------------------------

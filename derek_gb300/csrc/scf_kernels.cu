@@ -91,11 +91,11 @@ __global__ void k_filter_coef(const Tables t, int nks, const double *__restrict_
   const double e = 0.5 * (b - a), c = 0.5 * (b + a);
   const double sigma1 = e / (a0 - c);
   double sigma = sigma1;
-  coef[ksi] = Axpby{sigma1 / e, -c * sigma1 / e, 0.0};
+  coef[ksi] = Axpby{sigma1 / e, -c * sigma1 / e, 0.0, 1.0};
   for (int i = 1; i < m; ++i) {
     const double sn = 1.0 / (2.0 / sigma1 - sigma);
     const double al = 2.0 * sn / e;
-    coef[(long long)i * nks + ksi] = Axpby{al, -c * al, -sigma * sn};
+    coef[(long long)i * nks + ksi] = Axpby{al, -c * al, -sigma * sn, 1.0};
     sigma = sn;
   }
 }

@@ -308,6 +308,7 @@ __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
       __syncthreads();
     }
     const bool done = red[0] <= tol * tol * red2[0];
+    const double skip = tol * sqrt(red2[0]) / (4.0 * n);
     __syncthreads();
     if (done) break;
     for (int round = 0; round < ne - 1; ++round) {
@@ -326,7 +327,9 @@ __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
           const double a = A[p * n + p].x, d = A[q * n + q].x;
           const double2 b = A[p * n + q];
           const double e = hypot(b.x, b.y);
-          if (e > 0.0) {
+          // skip rotations whose element cannot matter for the convergence
+          // test (threshold Jacobi): |a_pq| below tol * ||A||_F / n
+          if (e > skip) {
             ph = make_double2(b.x / e, b.y / e);
             const double tau = (d - a) / (2.0 * e);
             const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
@@ -428,7 +431,10 @@ void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_n
 }
 
 bool cholesky_fits_smem(int max_nb) { return 2 * (size_t)max_nb * max_nb * 16 <= 200 * 1024; }
-bool jacobi_v_fits_smem(int max_nb) { return 2 * (size_t)max_nb * max_nb * 16 + 64 * max_nb + 256 <= 210 * 1024; }
+bool jacobi_v_fits_smem(int max_nb) {
+  // A and V (2 nb^2 complex FP64) plus the pair tables and 4 KB of reduction scratch
+  return 2 * (size_t)max_nb * max_nb * 16 + 48 * (size_t)max_nb + 4096 + 512 <= 232448;
+}
 
 void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *S,
                          double2 *C, const long long *mat_off, double2 *scratch, int *status,

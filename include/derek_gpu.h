@@ -95,7 +95,7 @@ typedef struct {
   double density_tol;      /* also require max|n_out - n_in| < density_tol
                               (0 = energy criterion only, as the reference) */
   int    buffer_bands;     /* extra unreported bands carried by the filtered
-                              subspace (-1 = max(4, nbands/10)) */
+                              subspace (-1 = max(4, nbands/20)) */
 } derek_scf_opts;
 
 /* Per-system SCF report (Source/electronic.f90:143-146 table row). */
