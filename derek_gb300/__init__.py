@@ -239,6 +239,17 @@ class Handle:
         _check(lib.derek_gpu_grad_wells(self._h, sys, _dptr(g)), self._h, "grad_wells")
         return g
 
+    def grad_density_loss(self, n_target, sys=0, max_iter=60, tol=1e-9):
+        """(L, dL/d(cx, cy, cz, depth, width) per well) for L = sum (n - n_target)^2 dV,
+        via the adjoint linear-response solve (FP64 handle, converged SCF)."""
+        nt = np.ascontiguousarray(np.asarray(n_target, dtype=np.float64))
+        nw = len(self.systems[sys].wells)
+        g = np.zeros((nw, 5))
+        loss = ctypes.c_double()
+        _check(lib.derek_gpu_grad_density_loss(self._h, sys, _dptr(nt), ctypes.byref(loss), _dptr(g),
+                                               int(max_iter), float(tol)), self._h, "grad_density_loss")
+        return loss.value, g
+
     def eigenvalues(self, sys=0):
         s = self.systems[sys]
         e = np.zeros((len(s.kpts), s.nbands))

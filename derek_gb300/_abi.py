@@ -90,6 +90,7 @@ SIGNATURES = {
     "derek_gpu_scf_iterate": (_i, [_vp, ctypes.POINTER(ScfReport)]),
     "derek_gpu_scf_run": (_i, [_vp, _i, _d, ctypes.POINTER(ScfReport)]),
     "derek_gpu_grad_wells": (_i, [_vp, _i, _pd]),
+    "derek_gpu_grad_density_loss": (_i, [_vp, _i, _pd, _pd, _pd, _i, _d]),
     "derek_gpu_get_eigenvalues": (_i, [_vp, _i, _pd]),
     "derek_gpu_get_occupations": (_i, [_vp, _i, _pd]),
     "derek_gpu_get_density": (_i, [_vp, _i, _pd]),

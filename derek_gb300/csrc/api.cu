@@ -59,11 +59,11 @@ static void apply_h_class(derek_gpu *h, const Tables &t, int item_begin, int nit
 // H.psi over items [item_begin, item_begin + nitems): all items (one launch
 // per grid-size class) or the items of one k-set (a single class)
 template <typename R>
-static void apply_h_t(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
-                      void *out, const Axpby *coef, const R *vloc) {
+static void apply_h_t(derek_gpu *h, const Tables &base, int item_begin, int nitems, const void *in,
+                      const void *prev, void *out, const Axpby *coef, const R *vloc) {
   if (item_begin == 0 && nitems == h->nitems) {
     for (const auto &c : h->classes) {
-      Tables t = h->tab;
+      Tables t = base;
       t.item_list = c.d_list;
       apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, in, prev, out, coef, vloc);
     }
@@ -71,16 +71,26 @@ static void apply_h_t(derek_gpu *h, int item_begin, int nitems, const void *in, 
   }
   const KSetDev &K = h->ks[h->item_ks[item_begin]];
   const SysDev &S = h->sys[K.sys];
-  apply_h_class<R>(h, h->tab, item_begin, nitems, (K.ncol + kColChunk - 1) / kColChunk, S.n, in,
+  apply_h_class<R>(h, base, item_begin, nitems, (K.ncol + kColChunk - 1) / kColChunk, S.n, in,
                    prev, out, coef, vloc);
 }
 
 int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
                   void *out, const Axpby *coef) {
   if (h->prec == DEREK_PREC_FP64)
-    apply_h_t<double>(h, item_begin, nitems, in, prev, out, coef, h->d_vloc);
+    apply_h_t<double>(h, h->tab, item_begin, nitems, in, prev, out, coef, h->d_vloc);
   else
-    apply_h_t<float>(h, item_begin, nitems, in, prev, out, coef, h->d_vloc32);
+    apply_h_t<float>(h, h->tab, item_begin, nitems, in, prev, out, coef, h->d_vloc32);
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+int apply_h_items_ex(derek_gpu *h, const Tables &base, int item_begin, int nitems, const void *in,
+                     const void *prev, void *out, const Axpby *coef, const void *vloc) {
+  if (h->prec == DEREK_PREC_FP64)
+    apply_h_t<double>(h, base, item_begin, nitems, in, prev, out, coef, (const double *)vloc);
+  else
+    apply_h_t<float>(h, base, item_begin, nitems, in, prev, out, coef, (const float *)vloc);
   DEREK_CUDA(h, cudaGetLastError());
   return DEREK_OK;
 }

@@ -124,6 +124,10 @@ int cuda_status(cudaError_t e, derek_gpu *h, const char *what);
 // (coef = nullptr: plain H in).
 int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
                   void *out, const Axpby *coef);
+// Same with a caller-provided table copy (item_shift) and potential (element
+// type of the handle's precision).
+int apply_h_items_ex(derek_gpu *h, const Tables &base, int item_begin, int nitems, const void *in,
+                     const void *prev, void *out, const Axpby *coef, const void *vloc);
 // Density of every active system from psi buffer `psi` and per-item weights
 // h->d_occw into rho (FP64 grids).
 int density_items(derek_gpu *h, const void *psi, double *rho);

@@ -690,3 +690,39 @@ void launch_hf_gradient(const Tables &t, int nsys, const double *rho, const doub
 }
 
 }  // namespace derek
+
+namespace derek {
+
+// V_H[rho] into cgrid (.x), every system (FP64 grids).
+void launch_hartree_only(const Tables &t, int nsys, int max_nr, int max_n, const double *rho,
+                         double2 *cgrid, cudaStream_t s) {
+  const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
+  derek::note_launch(), k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho, cgrid, 1);
+  launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
+  derek::note_launch(), k_hartree_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, 1);
+  launch_fft3d_grid(t, 0, nsys, max_n, cgrid, +1, s);
+}
+
+// dv_xc/dn at rho (central difference, relative step 1e-4; zero below 1e-10)
+__global__ void k_fxc(long long n, const double *__restrict__ rho, double *__restrict__ fxc) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double r = rho[i];
+    double f = 0.0;
+    if (r > 1e-10) {
+      const double h = 1e-4 * r;
+      double e1, v1, e2, v2;
+      lda_point(r + h, e1, v1);
+      lda_point(r - h, e2, v2);
+      f = (v1 - v2) / (2.0 * h);
+    }
+    fxc[i] = f;
+  }
+}
+
+void launch_fxc(long long n, const double *rho, double *fxc, cudaStream_t s) {
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+  derek::note_launch(), k_fxc<<<blocks, 256, 0, s>>>(n, rho, fxc);
+}
+
+}  // namespace derek

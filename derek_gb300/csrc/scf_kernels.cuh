@@ -27,6 +27,9 @@ void launch_density_fft(const Tables &t, int nsys, int max_nr, int max_n, const 
 void launch_hf_gradient(const Tables &t, int nsys, const double *rho, const double *wells,
                         const int *well_off, const double *cells, double *part, int max_wells,
                         double *grad, cudaStream_t s);
+void launch_hartree_only(const Tables &t, int nsys, int max_nr, int max_n, const double *rho,
+                         double2 *cgrid, cudaStream_t s);
+void launch_fxc(long long n, const double *rho, double *fxc, cudaStream_t s);
 void launch_uniform_density(const Tables &t, int nsys, int max_nr, double *rho, cudaStream_t s);
 
 }  // namespace derek

@@ -216,6 +216,17 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
  * was built from its wells and a converged SCF. */
 int derek_gpu_grad_wells(derek_gpu_t *h, int sys, double *grad);
 
+/* Gradient of the density-matching loss L = sum_r (n - n_target)^2 dV with
+ * respect to the Gaussian-well parameters of sys, through the converged SCF:
+ * one self-consistent linear-response (adjoint) solve with Sternheimer
+ * equations for the bands of the filtered subspace.  No counterpart in the
+ * reference.  Needs an FP64 handle over one system and a converged SCF;
+ * n_target has nr values; writes L to *loss and nwells*5 derivatives
+ * (cx, cy, cz, depth, width order) to grad.  max_iter <= 0 and tol <= 0
+ * take defaults (60, 1e-9 relative response residual). */
+int derek_gpu_grad_density_loss(derek_gpu_t *h, int sys, const double *n_target, double *loss,
+                                double *grad, int max_iter, double tol);
+
 /* Results of the last SCF iteration. */
 int derek_gpu_get_eigenvalues(derek_gpu_t *h, int sys, double *eig /* nk*nb */);
 int derek_gpu_get_occupations(derek_gpu_t *h, int sys, double *occ /* nk*nb */);

@@ -45,3 +45,36 @@ def test_hellmann_feynman_matches_finite_differences(oracle):
         e = np.exp(-r2 / (2 * wells[w, 4] ** 2))
         ref = -np.sum(rho * e) * np.linalg.det(cell) / rho.size
         assert abs(ref - g[w, 3]) < 1e-10 * max(1.0, abs(ref))
+
+
+def test_adjoint_density_loss_gradient_matches_finite_differences(oracle):
+    """dL/dp of L = sum (n - n_target)^2 dV through the converged SCF (adjoint
+    linear response) against central differences of L from full FP64 SCF runs
+    (h = 1e-4); n_target comes from a second seeded well set."""
+    import derek_gb300 as dg
+    cell = np.eye(3) * 7.0
+    kpts = [[0.0, 0.0, 0.0], [0.25, 0.25, 0.25]]
+    rng = np.random.default_rng(4)
+    wells = oracle.random_wells(rng, 3)
+    target_wells = oracle.random_wells(np.random.default_rng(5), 3)
+    _, _, n_t, _ = _free_energy(dg, cell, kpts, target_wells)
+
+    def loss_and_grad(w, want_grad):
+        spec = dg.SystemSpec(cell, 6.0, kpts, 6, 4.0, kT=0.01, wells=w)
+        with dg.Handle(spec, precision=dg.DEREK_PREC_FP64, density_tol=1e-11) as h:
+            h.electronic_scf(max_scf=400, etol=1e-14)
+            if want_grad:
+                return h.grad_density_loss(n_t, tol=1e-10)
+            rho = h.density()
+            return float(np.sum((rho - n_t) ** 2) * np.linalg.det(cell) / rho.size), None
+
+    L0, g = loss_and_grad(wells, True)
+    assert L0 > 0
+    h = 1e-4
+    for (w, p) in ((0, 3), (1, 4), (2, 1)):
+        wp = wells.copy()
+        wm = wells.copy()
+        wp[w, p] += h
+        wm[w, p] -= h
+        fd = (loss_and_grad(wp, False)[0] - loss_and_grad(wm, False)[0]) / (2 * h)
+        assert abs(fd - g[w, p]) < 1e-4 * max(1.0, abs(fd)), (w, p, fd, g[w, p])
