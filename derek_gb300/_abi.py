@@ -49,7 +49,7 @@ class ScfOpts(ctypes.Structure):
         ("precision", _i), ("mix_alpha", _d), ("kerker_q0", _d), ("pulay_history", _i),
         ("cheb_degree", _i), ("first_passes", _i), ("first_degree", _i),
         ("seed", ctypes.c_uint64), ("use_graph", _i), ("use_tensor_cores", _i),
-        ("density_tol", _d), ("buffer_bands", _i),
+        ("density_tol", _d), ("buffer_bands", _i), ("etol_per_electron", _i),
     ]
 
 

@@ -160,6 +160,7 @@ void derek_gpu_default_opts(derek_scf_opts *o) {
   o->use_tensor_cores = 1;
   o->density_tol = 0.0;
   o->buffer_bands = -1;
+  o->etol_per_electron = 0;
 }
 
 const char *derek_gpu_strerror(int s) {

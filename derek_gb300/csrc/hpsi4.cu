@@ -428,7 +428,7 @@ static void x_inv_go(const Tables &t, int item_begin, int nitems, int max_nchunk
   derek::note_launch(), k_x_inv<R, NX><<<dim3(nitems, max_nchunk), 256, sm, st>>>(t, item_begin, psi, abuf, occ_skip);
 }
 
-// compile-time x length when every system has the same n1 in {32, 48, 64, 72}
+// compile-time x length when every item has the same n1 in {32, 36, 48, 54, 64, 72}
 template <typename R>
 void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
                   int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
@@ -436,6 +436,8 @@ void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, i
   if (nitems <= 0) return;
   const int n = max_n1 == min_n1 ? max_n1 : 0;
   if (n == 72) x_inv_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
+  else if (n == 54) x_inv_go<R, 54>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
+  else if (n == 36) x_inv_go<R, 36>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
   else if (n == 64) x_inv_go<R, 64>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
   else if (n == 48) x_inv_go<R, 48>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
   else if (n == 32) x_inv_go<R, 32>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
@@ -458,6 +460,8 @@ void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, i
   if (nitems <= 0) return;
   const int n = max_n1 == min_n1 ? max_n1 : 0;
   if (n == 72) x_fwd_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
+  else if (n == 54) x_fwd_go<R, 54>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
+  else if (n == 36) x_fwd_go<R, 36>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
   else if (n == 64) x_fwd_go<R, 64>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
   else if (n == 48) x_fwd_go<R, 48>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
   else if (n == 32) x_fwd_go<R, 32>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
@@ -481,6 +485,8 @@ void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int m
                   int min_n2, int min_n3, cplx<R> *abuf, const R *vloc, cudaStream_t st) {
   if (nitems <= 0) return;
   if (try_plane_fixed<R, 72>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
+      try_plane_fixed<R, 54>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
+      try_plane_fixed<R, 36>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
       try_plane_fixed<R, 64>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
       try_plane_fixed<R, 48>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
       try_plane_fixed<R, 32>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st))
@@ -510,6 +516,8 @@ void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, in
                           double *partial, const long long *partial_off, cudaStream_t st) {
   if (nks <= 0) return;
   if (try_density_fixed<R, 72>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
+      try_density_fixed<R, 54>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
+      try_density_fixed<R, 36>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
       try_density_fixed<R, 64>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
       try_density_fixed<R, 48>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
       try_density_fixed<R, 32>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st))

@@ -46,7 +46,7 @@ void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, i
                   int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
                   cudaStream_t st);
 // (y,z)-plane pass; a compile-time kernel is used when every system has
-// n2 = n3 = N for N in {32, 48, 64, 72}
+// n2 = n3 = N for N in {32, 36, 48, 54, 64, 72}
 template <typename R>
 void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2, int max_n3,
                   int min_n2, int min_n3, cplx<R> *abuf, const R *vloc, cudaStream_t st);

@@ -120,10 +120,11 @@ int scf_start(derek_gpu *h, double etol) {
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
                                 cudaMemcpyHostToDevice, h->stream));
   std::vector<SysState> st(h->nsys);
-  for (auto &x : st) {
+  for (int s = 0; s < h->nsys; ++s) {
+    SysState &x = st[s];
     std::memset(&x, 0, sizeof(x));
     x.slot = -1;
-    x.etol = etol;
+    x.etol = h->opts.etol_per_electron ? etol * h->sys[s].nelec : etol;
     x.rtol = h->opts.density_tol;
     x.free = 0.0;
   }

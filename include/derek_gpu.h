@@ -96,6 +96,8 @@ typedef struct {
                               (0 = energy criterion only, as the reference) */
   int    buffer_bands;     /* extra unreported bands carried by the filtered
                               subspace (-1 = max(4, nbands/20)) */
+  int    etol_per_electron;/* 1: scf_run's etol is per electron (each system
+                              stops at |dF| < etol * nelec) */
 } derek_scf_opts;
 
 /* Per-system SCF report (Source/electronic.f90:143-146 table row). */
