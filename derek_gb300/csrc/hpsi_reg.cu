@@ -1,0 +1,367 @@
+// FP32 (y,z)-plane passes with every line transform held in one thread's
+// registers (regfft.cuh).
+//
+// A block owns XP consecutive x-planes of one item (apply H) or of one k-set
+// (density).  Each plane sits in shared memory as the rows of centred Miller
+// index my in [-RY, RY] (row my + RY), PZ elements per row: the rows a
+// sphere's columns can occupy.  Every other y row of the plane is zero after
+// the backward z transforms and is not needed after the forward y
+// transforms, so it is never stored: the y transforms take those inputs as
+// compile-time zeros and drop those outputs.  RY = N / 2 keeps every row.
+//   z pass:  one thread per (plane, row holding sphere columns): load the
+//            row, transform it in registers, store it back.
+//   y pass:  one thread per (plane, z): load the column, backward transform,
+//            multiply by V(r), forward transform, store it back (apply H), or
+//            backward transform and accumulate f |psi(r)|^2 (density).
+// Consecutive threads walk consecutive rows (z pass) or consecutive columns
+// (y pass), so no shared-memory access has a bank conflict, and a whole line
+// costs one load and one store per element.  The V(r) planes of the block
+// are copied into shared memory with cp.async while the columns are gathered
+// and the z transforms run.
+#include "kernels.cuh"
+#include "regfft.cuh"
+
+namespace derek {
+
+// Shared-memory layout of one plane (rows my in [-RY, RY]) and of one V(r)
+// plane.  The plane pitch PP is congruent to N mod 16 and the V pitch VP to N
+// mod 32, so a warp straddling two planes still reads consecutive banks.
+template <int N, int RY> struct RowsLayout {
+  static_assert(RY >= 0 && 2 * RY + 1 <= N + 1, "row bound");
+  static constexpr int NRW = 2 * RY + 1;
+  static constexpr int PZ = N | 1;
+  static constexpr int PP0 = NRW * PZ;
+  static constexpr int PP = PP0 + ((N - PP0) % 16 + 16) % 16;
+  static constexpr int VP = N * N + ((N - N * N) % 32 + 32) % 32;
+  // centred index of y row j (0 <= j < N)
+  __host__ __device__ static constexpr int my_of(int j) { return j > N / 2 ? j - N : j; }
+  __host__ __device__ static constexpr bool kept(int j) { return my_of(j) >= -RY && my_of(j) <= RY; }
+  __host__ __device__ static constexpr int row_of(int j) { return my_of(j) + RY; }
+};
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void load_line(float2 (&v)[N], const float2 *p, int stride) {
+  static_for<0, N>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    v[j] = p[j * stride];
+  });
+}
+
+// store X[m] (slot line_slot(m, L)) to p[m * stride]
+template <int N, int L>
+__device__ __forceinline__ void store_line(const float2 (&v)[N], float2 *p, int stride) {
+  static_for<0, N>([&](auto mc) {
+    constexpr int m = decltype(mc)::value;
+    p[m * stride] = v[line_slot<N>(m, L)];
+  });
+}
+
+// column z of a plane: the kept rows from shared memory, zeros elsewhere
+template <int N, int RY>
+__device__ __forceinline__ void load_column(float2 (&v)[N], const float2 *col) {
+  using Lay = RowsLayout<N, RY>;
+  static_for<0, N>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    if constexpr (Lay::kept(j))
+      v[j] = col[Lay::row_of(j) * Lay::PZ];
+    else
+      v[j] = make_float2(0.f, 0.f);
+  });
+}
+
+// z transforms of the rows holding columns, planes [0, np)
+template <int N, int RY, int SIGN>
+__device__ __forceinline__ void z_pass(float2 *P, int np, int nrow, const short *__restrict__ rows) {
+  using Lay = RowsLayout<N, RY>;
+  const int tid = threadIdx.x;
+  if (tid < np * nrow) {
+    const int p = tid / nrow;
+    const int l = tid - p * nrow;
+    float2 *line = P + p * Lay::PP + Lay::row_of(rows[l]) * Lay::PZ;
+    float2 v[N];
+    load_line<N>(v, line, 1);
+    reg_fft<N, SIGN, 0>(v);
+    store_line<N, 1>(v, line, 1);
+  }
+}
+
+// columns of the item's sphere into (IN) or out of the planes
+template <int N, int RY, int XP, int NT, bool IN>
+__device__ __forceinline__ void move_columns(float2 *P, float2 *a0, long long ld, int np, int ncol,
+                                             const short *__restrict__ cy, const short *__restrict__ cz) {
+  using Lay = RowsLayout<N, RY>;
+  for (int c = threadIdx.x; c < ncol; c += NT) {
+    const int off = Lay::row_of(cy[c]) * Lay::PZ + cz[c];
+#pragma unroll
+    for (int p = 0; p < XP; ++p) {
+      if (p < np) {
+        if (IN)
+          P[p * Lay::PP + off] = a0[p * ld + c];
+        else
+          a0[p * ld + c] = P[p * Lay::PP + off];
+      }
+    }
+  }
+}
+
+template <int N, int RY, int XP, int NT>
+__global__ void __launch_bounds__(NT, 1) k_plane_rows(Tables t, int item_begin, float2 *__restrict__ abuf,
+                                                      const float *__restrict__ vloc) {
+  using Lay = RowsLayout<N, RY>;
+  constexpr int PZ = Lay::PZ, PP = Lay::PP, VP = Lay::VP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *P = reinterpret_cast<float2 *>(smem_raw);
+  float *Vs = reinterpret_cast<float *>(P + XP * PP);
+  const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
+  const int ksi = t.item_ks[item];
+  const KSetDev &K = t.ks[ksi];
+  const SysDev &S = t.sys[K.sys];
+  if (!S.active) return;
+  const int n1 = S.n[0];
+  const int x0 = blockIdx.y * XP;
+  if (x0 >= n1) return;
+  const int np = min(XP, n1 - x0);
+  const int b = t.item_band[item];
+  const int tid = threadIdx.x;
+  // V(r) of the block's planes -> shared memory, in flight until the y pass
+  const float *vsrc = vloc + S.grid_off + (long long)x0 * N * N;
+  if (N % 4 == 0 && (reinterpret_cast<uintptr_t>(vsrc) & 15) == 0 &&
+      (reinterpret_cast<uintptr_t>(Vs) & 15) == 0) {
+    constexpr int Q = N * N / 4;
+    for (int i = tid; i < np * Q; i += NT) {
+      const int p = i / Q, r = i - p * Q;
+      cp_async16(Vs + p * VP + 4 * r, vsrc + (long long)p * N * N + 4 * r);
+    }
+  } else {
+    for (int i = tid; i < np * N * N; i += NT) {
+      const int p = i / (N * N), r = i - p * (N * N);
+      cp_async4(Vs + p * VP + r, vsrc + (long long)p * N * N + r);
+    }
+  }
+  cp_async_commit();
+  for (int i = tid; i < np * PP; i += NT) P[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  const long long ld = K.ncol_pad;
+  float2 *a0 = abuf + K.a_off + ((long long)b * n1 + x0) * ld;
+  const short *cy = t.col_y + K.col_off;
+  const short *cz = t.col_z + K.col_off;
+  move_columns<N, RY, XP, NT, true>(P, a0, ld, np, K.ncol, cy, cz);
+  __syncthreads();
+  const short *rows = t.rows + K.row_off;
+  z_pass<N, RY, +1>(P, np, K.nrow, rows);
+  cp_async_wait_all();
+  __syncthreads();
+  if (tid < np * N) {
+    const int p = tid / N;
+    const int z = tid - p * N;
+    float2 *col = P + p * PP + z;
+    const float *vz = Vs + p * VP + z;
+    float2 v[N];
+    load_column<N, RY>(v, col);
+    reg_fft<N, +1, 0>(v);
+    static_for<0, N>([&](auto mc) {
+      constexpr int m = decltype(mc)::value;
+      const float w = vz[m * N];
+      float2 &e = v[line_slot<N>(m, 1)];
+      e.x *= w;
+      e.y *= w;
+    });
+    reg_fft<N, -1, 1>(v);
+    static_for<0, N>([&](auto mc) {
+      constexpr int m = decltype(mc)::value;
+      if constexpr (Lay::kept(m)) col[Lay::row_of(m) * PZ] = v[line_slot<N>(m, 2)];
+    });
+  }
+  __syncthreads();
+  z_pass<N, RY, -1>(P, np, K.nrow, rows);
+  __syncthreads();
+  move_columns<N, RY, XP, NT, false>(P, a0, ld, np, K.ncol, cy, cz);
+}
+
+// Density of one k-set over XP x-planes: loop over bands, accumulate
+// f_b |psi_b(r)|^2 per point in FP32 for up to kFlush bands, then add that
+// sum into the FP64 per-k-set partial grid (each point owned by one thread).
+constexpr int kFlush = 8;
+
+template <int N, int RY, int XP, int NT>
+__global__ void __launch_bounds__(NT, 1) k_density_rows(Tables t, int ks_begin, const float2 *__restrict__ abuf,
+                                                        const double *__restrict__ occ,
+                                                        double *__restrict__ partial,
+                                                        const long long *__restrict__ partial_off) {
+  using Lay = RowsLayout<N, RY>;
+  constexpr int PZ = Lay::PZ, PP = Lay::PP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *P = reinterpret_cast<float2 *>(smem_raw);
+  float *acc = reinterpret_cast<float *>(P + XP * PP);
+  short *rows_s = reinterpret_cast<short *>(acc + XP * N * N);
+  const int ksi = ks_begin + blockIdx.x;
+  const KSetDev &K = t.ks[ksi];
+  const SysDev &S = t.sys[K.sys];
+  if (!S.active) return;
+  const int n1 = S.n[0];
+  const int x0 = blockIdx.y * XP;
+  if (x0 >= n1) return;
+  const int np = min(XP, n1 - x0);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < np * PP; i += NT) P[i] = make_float2(0.f, 0.f);
+  const bool owner = tid < np * N;
+  const int p = owner ? tid / N : 0;
+  const int z = owner ? tid - p * N : 0;
+  float *accz = acc + p * N * N + z;
+  if (owner)
+    static_for<0, N>([&](auto mc) { accz[decltype(mc)::value * N] = 0.f; });
+  double *dst = partial + partial_off[ksi] + (long long)(x0 + p) * N * N + z;
+  const int nrow = K.nrow;
+  const long long ld = K.ncol_pad;
+  const short *cy = t.col_y + K.col_off;
+  const short *cz = t.col_z + K.col_off;
+  const short *rows = t.rows + K.row_off;
+  for (int l = tid; l < nrow; l += NT) rows_s[l] = (short)Lay::row_of(rows[l]);
+  int pending = 0;     // bands summed in acc since the last flush
+  bool first = true;   // dst not yet written
+  for (int b = 0; b < K.nb; ++b) {
+    const double w = occ[K.item0 + b];
+    if (w == 0.0) continue;
+    __syncthreads();   // previous band's column reads done; P's rows are zero again
+    float2 *a0 = const_cast<float2 *>(abuf) + K.a_off + ((long long)b * n1 + x0) * ld;
+    move_columns<N, RY, XP, NT, true>(P, a0, ld, np, K.ncol, cy, cz);
+    __syncthreads();
+    z_pass<N, RY, +1>(P, np, nrow, rows);
+    __syncthreads();
+    if (owner) {
+      float2 *col = P + p * PP + z;
+      float2 v[N];
+      load_column<N, RY>(v, col);
+      // clear this column's rows for the next band's gather
+      for (int l = 0; l < nrow; ++l) col[rows_s[l] * PZ] = make_float2(0.f, 0.f);
+      reg_fft<N, +1, 0>(v);
+      const float wf = (float)w;
+      static_for<0, N>([&](auto mc) {
+        constexpr int m = decltype(mc)::value;
+        const float2 e = v[line_slot<N>(m, 1)];
+        accz[m * N] += wf * (e.x * e.x + e.y * e.y);
+      });
+      if (++pending == kFlush) {
+        static_for<0, N>([&](auto mc) {
+          constexpr int m = decltype(mc)::value;
+          const double s = (double)accz[m * N];
+          dst[m * N] = first ? s : dst[m * N] + s;
+          accz[m * N] = 0.f;
+        });
+        first = false;
+        pending = 0;
+      }
+    }
+  }
+  if (owner && (pending || first)) {
+    static_for<0, N>([&](auto mc) {
+      constexpr int m = decltype(mc)::value;
+      const double s = (double)accz[m * N];
+      dst[m * N] = first ? s : dst[m * N] + s;
+    });
+  }
+}
+
+// ---- launch shapes -----------------------------------------------------------
+// Row bound of the compact kernels: a fine grid of N points along y holds the
+// sphere's |my| <= N / 4 + 1 whenever the grid is about twice the sphere's
+// diameter (the density cutoff); other spheres use every row (RY = N / 2).
+template <int N> constexpr int compact_ry() { return N / 4 + 1; }
+
+constexpr int kSmemMax = 227 * 1024;
+constexpr int kThreadsMax = 384;
+
+// planes per block: as many as fit the shared memory and kThreadsMax threads
+template <int N, int RY, bool DENSITY> struct RowsShape {
+  using Lay = RowsLayout<N, RY>;
+  static constexpr int PLANE = Lay::PP * 8 + (DENSITY ? N * N * 4 : Lay::VP * 4);
+  static constexpr int BY_SMEM = (kSmemMax - 2 * N - 16) / PLANE;
+  static constexpr int BY_THREADS = kThreadsMax / N;
+  static constexpr int XP0 = BY_SMEM < BY_THREADS ? BY_SMEM : BY_THREADS;
+  static constexpr int XP = XP0 < 1 ? 1 : XP0;
+  static constexpr int NT = (N * XP + 31) / 32 * 32;
+  static constexpr size_t SMEM = (size_t)XP * PLANE + 2 * N + 16;
+};
+
+template <int N, int RY>
+static void plane_rows_go(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
+                          const float *vloc, cudaStream_t st) {
+  using Sh = RowsShape<N, RY, false>;
+  auto kern = k_plane_rows<N, RY, Sh::XP, Sh::NT>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM);
+  const int ng = (max_n1 + Sh::XP - 1) / Sh::XP;
+  derek::note_launch(), kern<<<dim3(nitems, ng), Sh::NT, Sh::SMEM, st>>>(t, item_begin, abuf, vloc);
+}
+
+template <int N, int RY>
+static void density_rows_go(const Tables &t, int ks_begin, int nks, int max_n1, const float2 *abuf,
+                            const double *occ, double *partial, const long long *partial_off,
+                            cudaStream_t st) {
+  using Sh = RowsShape<N, RY, true>;
+  auto kern = k_density_rows<N, RY, Sh::XP, Sh::NT>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM);
+  const int ng = (max_n1 + Sh::XP - 1) / Sh::XP;
+  derek::note_launch(), kern<<<dim3(nks, ng), Sh::NT, Sh::SMEM, st>>>(t, ks_begin, abuf, occ, partial, partial_off);
+}
+
+template <int N>
+static void plane_go(const Tables &t, int item_begin, int nitems, int max_n1, int max_my, float2 *abuf,
+                     const float *vloc, cudaStream_t st) {
+  if (max_my <= compact_ry<N>())
+    plane_rows_go<N, compact_ry<N>()>(t, item_begin, nitems, max_n1, abuf, vloc, st);
+  else
+    plane_rows_go<N, N / 2>(t, item_begin, nitems, max_n1, abuf, vloc, st);
+}
+
+template <int N>
+static void density_go(const Tables &t, int ks_begin, int nks, int max_n1, int max_my, const float2 *abuf,
+                       const double *occ, double *partial, const long long *partial_off, cudaStream_t st) {
+  if (max_my <= compact_ry<N>())
+    density_rows_go<N, compact_ry<N>()>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
+  else
+    density_rows_go<N, N / 2>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
+}
+
+bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_my,
+                      float2 *abuf, const float *vloc, cudaStream_t st) {
+  switch (n) {
+    case 72: plane_go<72>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 64: plane_go<64>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 54: plane_go<54>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 48: plane_go<48>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 36: plane_go<36>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 32: plane_go<32>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 27: plane_go<27>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 24: plane_go<24>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    default: return false;
+  }
+}
+
+bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_my,
+                        const float2 *abuf, const double *occ, double *partial,
+                        const long long *partial_off, cudaStream_t st) {
+  switch (n) {
+    case 72: density_go<72>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 64: density_go<64>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 54: density_go<54>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 48: density_go<48>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 36: density_go<36>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 32: density_go<32>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 27: density_go<27>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 24: density_go<24>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    default: return false;
+  }
+}
+
+}  // namespace derek

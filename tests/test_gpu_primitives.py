@@ -111,6 +111,65 @@ def test_density_matches_oracle(oracle, precision, tol):
     assert abs(got.sum() * s.volume / s.nr - (s.wk[:, None] * occ).sum()) < 1e-9 * occ.sum() + tol
 
 
+REG_LENGTHS = [24, 27, 32, 36, 48, 54, 64, 72]
+
+
+def reg_plane_pair(oracle, n, rows, kpts, nb, seed):
+    """Cubic cell on an n^3 grid whose sphere reaches |my| = N/4 + 1 ("compact":
+    the FP32 plane kernels keep only those rows) or N/4 + 3 ("all": every
+    row kept)."""
+    L = 8.0
+    rmax = n // 4 + 1 if rows == "compact" else n // 4 + 3
+    rho = rmax + 0.25   # Miller radius; k_y = 0.2 puts the extreme rows at +-rmax
+    ecut = 0.5 * (rho * 2 * np.pi / L) ** 2
+    s, spec = make_pair(oracle, L=L, ecut=ecut, nb=nb, kpts=kpts, seed=seed, n_fine=(n, n, n))
+    my = np.concatenate([oracle.KBasis(s, ik).miller[:, 1] for ik in range(len(kpts))])
+    assert int(np.abs(my).max()) == rmax
+    return s, spec
+
+
+@pytest.mark.parametrize("rows", ["compact", "all"])
+@pytest.mark.parametrize("n", REG_LENGTHS)
+def test_apply_h_register_planes(oracle, n, rows):
+    """FP32 H.psi through the register-line plane kernels at every compiled
+    length, against the FP64 oracle."""
+    import derek_gb300 as dg
+    s, spec = reg_plane_pair(oracle, n, rows, ((0.1, 0.2, -0.3),), 3, seed=n)
+    kb = oracle.KBasis(s, 0)
+    rng = np.random.default_rng(n + 1)
+    psi = rng.standard_normal((s.nbands, kb.npw)) + 1j * rng.standard_normal((s.nbands, kb.npw))
+    v = s.vext + 0.3 * rng.standard_normal(s.nr)
+    with dg.Handle(spec, precision=1) as h:
+        h.set_vloc(v)
+        h.set_wfn(psi)
+        got = h.pot_apply_wfn()
+    assert rel_err(got, oracle.apply_h(s, kb, v, psi)) < FP32_TOL
+
+
+@pytest.mark.parametrize("rows", ["compact", "all"])
+@pytest.mark.parametrize("n", REG_LENGTHS)
+def test_density_register_planes(oracle, n, rows):
+    """FP32 density through the register-line plane kernels (band loop with
+    FP32 partial sums flushed to FP64), against the FP64 oracle."""
+    import derek_gb300 as dg
+    kpts = [(0.1, 0.2, -0.3), (-0.25, 0.2, 0.25)]
+    nb = 11   # more bands than one flush period
+    s, spec = reg_plane_pair(oracle, n, rows, kpts, nb, seed=2 * n)
+    rng = np.random.default_rng(n + 3)
+    occ = rng.uniform(0, 2, (len(kpts), nb))
+    occ[0, 4] = 0.0
+    ref = np.zeros(s.nr)
+    with dg.Handle(spec, precision=1) as h:
+        for ik in range(len(kpts)):
+            kb = oracle.KBasis(s, ik)
+            psi = rng.standard_normal((nb, kb.npw)) + 1j * rng.standard_normal((nb, kb.npw))
+            psi /= np.linalg.norm(psi, axis=1)[:, None]
+            h.set_wfn(psi, 0, ik)
+            ref += s.wk[ik] * oracle.band_density(s, kb, psi, occ[ik])
+        got = h.density_calculate(occ)
+    assert rel_err(got, ref) < FP32_TOL
+
+
 def test_xc_lda_matches_oracle_and_libxc(oracle):
     import derek_gb300 as dg
     spec = dg.SystemSpec(np.eye(3) * 6.0, 2.0, [[0, 0, 0]], 2, 2.0, n_fine=(8, 8, 8))
