@@ -434,6 +434,11 @@ void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, i
                   int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
                   cudaStream_t st) {
   if (nitems <= 0) return;
+  if constexpr (std::is_same<R, float>::value) {
+    if (max_n1 == min_n1 &&
+        launch_xinv_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, psi, abuf, occ_skip, st))
+      return;
+  }
   const int n = max_n1 == min_n1 ? max_n1 : 0;
   if (n == 72) x_inv_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
   else if (n == 54) x_inv_go<R, 54>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
@@ -458,6 +463,11 @@ void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, i
                   int min_n1, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
                   cplx<R> *out, const Axpby *coef, cudaStream_t st) {
   if (nitems <= 0) return;
+  if constexpr (std::is_same<R, float>::value) {
+    if (max_n1 == min_n1 &&
+        launch_xfwd_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, abuf, psi, prev, out, coef, st))
+      return;
+  }
   const int n = max_n1 == min_n1 ? max_n1 : 0;
   if (n == 72) x_fwd_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
   else if (n == 54) x_fwd_go<R, 54>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);

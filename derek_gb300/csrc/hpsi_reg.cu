@@ -21,6 +21,8 @@
 #include "kernels.cuh"
 #include "regfft.cuh"
 
+#include <cstdlib>
+
 namespace derek {
 
 // Shared-memory layout of one plane (rows my in [-RY, RY]) and of one V(r)
@@ -115,8 +117,8 @@ __device__ __forceinline__ void move_columns(float2 *P, float2 *a0, long long ld
   }
 }
 
-template <int N, int RY, int XP, int NT>
-__global__ void __launch_bounds__(NT, 1) k_plane_rows(Tables t, int item_begin, float2 *__restrict__ abuf,
+template <int N, int RY, int XP, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_plane_rows(Tables t, int item_begin, float2 *__restrict__ abuf,
                                                       const float *__restrict__ vloc) {
   using Lay = RowsLayout<N, RY>;
   constexpr int PZ = Lay::PZ, PP = Lay::PP, VP = Lay::VP;
@@ -294,14 +296,39 @@ template <int N, int RY, bool DENSITY> struct RowsShape {
   static constexpr size_t SMEM = (size_t)XP * PLANE + 2 * N + 16;
 };
 
+template <int N, int RY, int XP, int MINB>
+static void plane_rows_go_x(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
+                            const float *vloc, cudaStream_t st) {
+  using Lay = RowsLayout<N, RY>;
+  constexpr int NT = (N * XP + 31) / 32 * 32;
+  const size_t smem = (size_t)XP * (Lay::PP * 8 + Lay::VP * 4) + 16;
+  auto kern = k_plane_rows<N, RY, XP, NT, MINB>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int ng = (max_n1 + XP - 1) / XP;
+  derek::note_launch(), kern<<<dim3(nitems, ng), NT, smem, st>>>(t, item_begin, abuf, vloc);
+}
+
+static int plane_variant() {
+  static int v = [] {
+    const char *e = getenv("DEREK_PLANE_VARIANT");
+    return e ? atoi(e) : 0;
+  }();
+  return v;
+}
+
 template <int N, int RY>
 static void plane_rows_go(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
                           const float *vloc, cudaStream_t st) {
   using Sh = RowsShape<N, RY, false>;
-  auto kern = k_plane_rows<N, RY, Sh::XP, Sh::NT>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM);
-  const int ng = (max_n1 + Sh::XP - 1) / Sh::XP;
-  derek::note_launch(), kern<<<dim3(nitems, ng), Sh::NT, Sh::SMEM, st>>>(t, item_begin, abuf, vloc);
+  if (N == 72 && RY < N / 2) {
+    switch (plane_variant()) {
+      case 1: plane_rows_go_x<N, RY, 2, 2>(t, item_begin, nitems, max_n1, abuf, vloc, st); return;
+      case 2: plane_rows_go_x<N, RY, 1, 4>(t, item_begin, nitems, max_n1, abuf, vloc, st); return;
+      case 3: plane_rows_go_x<N, RY, 4, 1>(t, item_begin, nitems, max_n1, abuf, vloc, st); return;
+      default: break;
+    }
+  }
+  plane_rows_go_x<N, RY, Sh::XP, 1>(t, item_begin, nitems, max_n1, abuf, vloc, st);
 }
 
 template <int N, int RY>

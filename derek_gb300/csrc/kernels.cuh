@@ -66,6 +66,11 @@ constexpr int kColChunk = 64;   // columns per x-line chunk (kCC in hpsi4.cu)
 // they return false for any other n.
 bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_my,
                       float2 *abuf, const float *vloc, cudaStream_t st);
+bool launch_xinv_reg(const Tables &t, int item_begin, int nitems, int max_ncol, int n, const float2 *psi,
+                     float2 *abuf, const double *occ_skip, cudaStream_t st);
+bool launch_xfwd_reg(const Tables &t, int item_begin, int nitems, int max_ncol, int n, const float2 *abuf,
+                     const float2 *psi, const float2 *prev, float2 *out, const Axpby *coef,
+                     cudaStream_t st);
 bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_my,
                         const float2 *abuf, const double *occ, double *partial,
                         const long long *partial_off, cudaStream_t st);
