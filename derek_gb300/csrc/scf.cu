@@ -70,7 +70,7 @@ int cholqr_rr(derek_gpu *h) {
   if (st) return st;
   overlap_all(h, X, h->d_HX, h->d_Hs, 1);
   launch_jacobi(h->tab, 0, h->nks, h->max_nb, h->d_Hs, h->d_C, h->d_mat_off, h->d_eig,
-                h->d_scratch, 30, 1e-14, h->d_sweeps, h->stream);
+                h->d_scratch, 30, 1e-14, 0, h->d_sweeps, h->stream);
   rotate_all(h, X, h->d_C);
   return DEREK_OK;
 }

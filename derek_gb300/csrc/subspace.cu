@@ -252,41 +252,77 @@ __global__ void __launch_bounds__(256) k_cholesky_inv(const Tables t, int ks_beg
 
 // ---------------------------------------------------------------------------
 // Hermitian Jacobi eigensolver (parallel cyclic, round-robin pair ordering).
-// A <- U^H A U with U = diag(1, e^{-i phi}) [[c, s], [-s, c]] on each pair.
-// Eigenvalues ascending go to eig[item0 + j]; eigenvectors (columns) to C.
+// Each round rotates np = ne/2 disjoint index pairs (p, q) at once:
+//   A <- U^H A U,  V <- V U,  U = diag(1, e^{-i phi}) [[c, s], [-s, c]] per pair.
+// Entry (i, j) of U^H A U depends only on the 2x2 block of A at the pairs
+// holding i and j, so a round is one pass over the blocks (a <= b) of pairs:
+// A'_ab = U_a^H A_ab U_b, with A'_ba = A'_ab^H written by the same thread.
+// That touches half of A, with all arithmetic on A in FP64.  The
+// eigenvectors accumulate in VT (FP64, or FP32 on the mixed-precision path,
+// whose wavefunctions are FP32), stored one eigenvector per row so that a
+// warp updates consecutive addresses.  Eigenvalues ascending go to
+// eig[item0 + j]; eigenvectors (columns) to C.
 // ---------------------------------------------------------------------------
+// pair k of round r in the circle schedule over ne positions (position 0
+// fixed, the others advance one place per round)
+__device__ __forceinline__ void rr_pair(int k, int r, int ne, int &p, int &q) {
+  const int m = ne - 1;
+  const int a = k == 0 ? 0 : 1 + (k - 1 + r) % m;
+  const int b = 1 + (ne - 2 - k + r) % m;
+  p = min(a, b);
+  q = max(a, b);
+}
+
+template <typename VT>
 __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
                                                 const double2 *__restrict__ Hs,
                                                 double2 *__restrict__ Cout,
                                                 const long long *__restrict__ mat_off,
                                                 double *__restrict__ eig,
                                                 double2 *__restrict__ scratch, int max_sweeps,
-                                                double tol, int v_in_smem,
+                                                double tol, int a_in_smem, int v_in_smem,
                                                 int *__restrict__ sweeps_out) {
+  using V2 = cplx<VT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ksi = ks_begin + blockIdx.x;
   const KSetDev &K = t.ks[ksi];
   if (!t.sys[K.sys].active) return;
   const int n = K.nb;
-  const int ne = n + (n & 1);  // even count for the tournament
+  const int ne = n + (n & 1);  // even count for the tournament; index n is a dummy
   const int np = ne / 2;
-  double2 *A = reinterpret_cast<double2 *>(smem_raw);
-  double2 *V = v_in_smem ? A + n * n : scratch + 2 * mat_off[ksi];
-  double *rc = reinterpret_cast<double *>(A + n * n + (v_in_smem ? n * n : 0));  // [np]
+  const int nblk = np * (np + 1) / 2;
+  unsigned char *sp = smem_raw;
+  double2 *A = a_in_smem ? reinterpret_cast<double2 *>(sp) : scratch + 2 * mat_off[ksi] + (long long)n * n;
+  if (a_in_smem) sp += (size_t)n * n * sizeof(double2);
+  V2 *Vt = v_in_smem ? reinterpret_cast<V2 *>(sp) : reinterpret_cast<V2 *>(scratch + 2 * mat_off[ksi]);
+  if (v_in_smem) sp += ((size_t)n * n * sizeof(V2) + 15) / 16 * 16;
+  double2 *rph = reinterpret_cast<double2 *>(sp);  // [np]
+  double *rc = reinterpret_cast<double *>(rph + np);
   double *rs = rc + np;
-  double2 *rph = reinterpret_cast<double2 *>(rs + np);  // [np]
-  int *pp = reinterpret_cast<int *>(rph + np);           // [np]
-  int *pq = pp + np;                                    // [np]
-  int *idx = pq + np;                                   // [ne]
+  int *pp = reinterpret_cast<int *>(rs + np);
+  int *pq = pp + np;
+  int *act = pq + np;
+  short2 *blk = reinterpret_cast<short2 *>(act + np);  // [nblk]: (a, b), a <= b
   __shared__ double red[256];
   __shared__ double red2[256];
   const double2 *Hb = Hs + mat_off[ksi];
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     A[e] = Hb[e];
     const int i = e / n, j = e % n;
-    V[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    V2 one;
+    one.x = (VT)(i == j ? 1 : 0);
+    one.y = (VT)0;
+    Vt[e] = one;
   }
-  for (int i = threadIdx.x; i < ne; i += blockDim.x) idx[i] = i;
+  for (int w = threadIdx.x; w < nblk; w += blockDim.x) {
+    // w -> (a, b) with a <= b, rows of the upper triangle in order
+    int a = 0, rem = w;
+    while (rem >= np - a) {
+      rem -= np - a;
+      ++a;
+    }
+    blk[w] = make_short2((short)a, (short)(a + rem));
+  }
   __syncthreads();
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
@@ -308,86 +344,121 @@ __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
       __syncthreads();
     }
     const bool done = red[0] <= tol * tol * red2[0];
+    // skip rotations whose element cannot matter for the convergence test
+    // (threshold Jacobi): |a_pq| below tol * ||A||_F / (4 n)
     const double skip = tol * sqrt(red2[0]) / (4.0 * n);
     __syncthreads();
     if (done) break;
     for (int round = 0; round < ne - 1; ++round) {
       for (int k = threadIdx.x; k < np; k += blockDim.x) {
-        int p = idx[k], q = idx[ne - 1 - k];
-        if (p > q) {
-          const int tmp = p;
-          p = q;
-          q = tmp;
-        }
+        int p, q;
+        rr_pair(k, round, ne, p, q);
         pp[k] = p;
         pq[k] = q;
         double c = 1.0, s = 0.0;
         double2 ph = make_double2(1.0, 0.0);
+        int on = 0;
         if (q < n) {
           const double a = A[p * n + p].x, d = A[q * n + q].x;
           const double2 b = A[p * n + q];
           const double e = hypot(b.x, b.y);
-          // skip rotations whose element cannot matter for the convergence
-          // test (threshold Jacobi): |a_pq| below tol * ||A||_F / n
           if (e > skip) {
             ph = make_double2(b.x / e, b.y / e);
             const double tau = (d - a) / (2.0 * e);
             const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
             c = 1.0 / sqrt(1.0 + tt * tt);
             s = tt * c;
+            on = 1;
           }
         }
         rc[k] = c;
         rs[k] = s;
         rph[k] = ph;
+        act[k] = on;
       }
       __syncthreads();
-      // rows: new p = c A_p - s ph A_q ; new q = s A_p + c ph A_q
-      for (int w = threadIdx.x; w < np * n; w += blockDim.x) {
-        const int k = w / n, col = w % n;
-        const int p = pp[k], q = pq[k];
-        if (q >= n || rs[k] == 0.0) continue;
-        const double c = rc[k], s = rs[k];
-        const double2 ph = rph[k];
-        const double2 ap = A[p * n + col], aq = A[q * n + col];
-        const double2 phq = zmul(ph, aq);
-        A[p * n + col] = make_double2(c * ap.x - s * phq.x, c * ap.y - s * phq.y);
-        A[q * n + col] = make_double2(s * ap.x + c * phq.x, s * ap.y + c * phq.y);
-      }
-      __syncthreads();
-      // columns of A and V: new p = c X_p - s conj(ph) X_q ; new q = s X_p + c conj(ph) X_q
-      for (int w = threadIdx.x; w < np * n; w += blockDim.x) {
-        const int k = w / n, row = w % n;
-        const int p = pp[k], q = pq[k];
-        if (q >= n || rs[k] == 0.0) continue;
-        const double c = rc[k], s = rs[k];
-        const double2 phc = make_double2(rph[k].x, -rph[k].y);
-        {
-          const double2 xp = A[row * n + p], xq = A[row * n + q];
-          const double2 t2 = zmul(phc, xq);
-          A[row * n + p] = make_double2(c * xp.x - s * t2.x, c * xp.y - s * t2.y);
-          A[row * n + q] = make_double2(s * xp.x + c * t2.x, s * xp.y + c * t2.y);
+      // blocks of A: left by U_a^H (new row p = c A_p - s ph A_q, new row
+      // q = s A_p + c ph A_q), right by U_b (new col p = c X_p - s conj(ph) X_q,
+      // new col q = s X_p + c conj(ph) X_q)
+      for (int w = threadIdx.x; w < nblk; w += blockDim.x) {
+        const short2 ab = blk[w];
+        const int ia = ab.x, ib = ab.y;
+        const int on_a = act[ia], on_b = act[ib];
+        if (!on_a && !on_b) continue;
+        const int pa = pp[ia], qa = pq[ia], pb = pp[ib], qb = pq[ib];
+        const bool qa_ok = qa < n, qb_ok = qb < n;
+        const double2 z = make_double2(0.0, 0.0);
+        double2 x00 = A[pa * n + pb];
+        double2 x01 = qb_ok ? A[pa * n + qb] : z;
+        double2 x10 = qa_ok ? A[qa * n + pb] : z;
+        double2 x11 = (qa_ok && qb_ok) ? A[qa * n + qb] : z;
+        if (on_a) {
+          const double c = rc[ia], s = rs[ia];
+          const double2 ph = rph[ia];
+          const double2 t0 = zmul(ph, x10), t1 = zmul(ph, x11);
+          const double2 n00 = make_double2(c * x00.x - s * t0.x, c * x00.y - s * t0.y);
+          const double2 n01 = make_double2(c * x01.x - s * t1.x, c * x01.y - s * t1.y);
+          x10 = make_double2(s * x00.x + c * t0.x, s * x00.y + c * t0.y);
+          x11 = make_double2(s * x01.x + c * t1.x, s * x01.y + c * t1.y);
+          x00 = n00;
+          x01 = n01;
         }
-        {
-          const double2 xp = V[row * n + p], xq = V[row * n + q];
-          const double2 t2 = zmul(phc, xq);
-          V[row * n + p] = make_double2(c * xp.x - s * t2.x, c * xp.y - s * t2.y);
-          V[row * n + q] = make_double2(s * xp.x + c * t2.x, s * xp.y + c * t2.y);
+        if (on_b) {
+          const double c = rc[ib], s = rs[ib];
+          const double2 phc = make_double2(rph[ib].x, -rph[ib].y);
+          const double2 t0 = zmul(phc, x01), t1 = zmul(phc, x11);
+          const double2 n00 = make_double2(c * x00.x - s * t0.x, c * x00.y - s * t0.y);
+          const double2 n10 = make_double2(c * x10.x - s * t1.x, c * x10.y - s * t1.y);
+          x01 = make_double2(s * x00.x + c * t0.x, s * x00.y + c * t0.y);
+          x11 = make_double2(s * x10.x + c * t1.x, s * x10.y + c * t1.y);
+          x00 = n00;
+          x10 = n10;
+        }
+        if (ia == ib) {
+          // the pair's own 2x2 block is now diagonal and real
+          A[pa * n + pa] = make_double2(x00.x, 0.0);
+          A[qa * n + qa] = make_double2(x11.x, 0.0);
+          A[pa * n + qa] = z;
+          A[qa * n + pa] = z;
+          continue;
+        }
+        A[pa * n + pb] = x00;
+        A[pb * n + pa] = make_double2(x00.x, -x00.y);
+        if (qb_ok) {
+          A[pa * n + qb] = x01;
+          A[qb * n + pa] = make_double2(x01.x, -x01.y);
+        }
+        if (qa_ok) {
+          A[qa * n + pb] = x10;
+          A[pb * n + qa] = make_double2(x10.x, -x10.y);
+        }
+        if (qa_ok && qb_ok) {
+          A[qa * n + qb] = x11;
+          A[qb * n + qa] = make_double2(x11.x, -x11.y);
         }
       }
-      __syncthreads();
-      // next tournament round: keep idx[0], rotate the rest by one
-      if (threadIdx.x == 0) {
-        const int last = idx[ne - 1];
-        for (int i = ne - 1; i > 1; --i) idx[i] = idx[i - 1];
-        idx[1] = last;
+      // eigenvectors: Vt[col][row], new col p = c X_p - s conj(ph) X_q,
+      // new col q = s X_p + c conj(ph) X_q
+      for (int w = threadIdx.x; w < np * n; w += blockDim.x) {
+        const int k = w / n, row = w - (w / n) * n;
+        if (!act[k]) continue;
+        const VT c = (VT)rc[k], s = (VT)rs[k];
+        const VT phx = (VT)rph[k].x, phy = (VT)-rph[k].y;
+        V2 &xp = Vt[pp[k] * n + row];
+        V2 &xq = Vt[pq[k] * n + row];
+        const V2 a = xp, b = xq;
+        const VT tx = phx * b.x - phy * b.y, ty = phx * b.y + phy * b.x;
+        xp.x = c * a.x - s * tx;
+        xp.y = c * a.y - s * ty;
+        xq.x = s * a.x + c * tx;
+        xq.y = s * a.y + c * ty;
       }
       __syncthreads();
     }
   }
   if (threadIdx.x == 0 && sweeps_out) sweeps_out[ksi] = sweep;
   // sort eigenvalues ascending (selection by rank; ties broken by index)
-  double *ev = rc;  // reuse: n entries needed, np*2 >= n available
+  double *ev = rc;  // reuse: np * 2 >= n entries (rc and rs are adjacent)
   for (int i = threadIdx.x; i < n; i += blockDim.x) ev[i] = A[i * n + i].x;
   __syncthreads();
   double2 *Cb = Cout + mat_off[ksi];
@@ -396,7 +467,10 @@ __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
     int rank = 0;
     for (int j = 0; j < n; ++j) rank += (ev[j] < vi) || (ev[j] == vi && j < i);
     eig[K.item0 + rank] = vi;
-    for (int r = 0; r < n; ++r) Cb[r * n + rank] = V[r * n + i];
+    for (int r = 0; r < n; ++r) {
+      const V2 v = Vt[i * n + r];
+      Cb[r * n + rank] = make_double2((double)v.x, (double)v.y);
+    }
   }
 }
 
@@ -431,11 +505,6 @@ void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_n
 }
 
 bool cholesky_fits_smem(int max_nb) { return 2 * (size_t)max_nb * max_nb * 16 <= 200 * 1024; }
-bool jacobi_v_fits_smem(int max_nb) {
-  // A and V (2 nb^2 complex FP64) plus the pair tables and 4 KB of reduction scratch
-  return 2 * (size_t)max_nb * max_nb * 16 + 48 * (size_t)max_nb + 4096 + 512 <= 232448;
-}
-
 void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *S,
                          double2 *C, const long long *mat_off, double2 *scratch, int *status,
                          cudaStream_t st) {
@@ -446,18 +515,33 @@ void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, con
   derek::note_launch(), k_cholesky_inv<<<nks, 256, sm, st>>>(t, ks_begin, S, C, mat_off, scratch, status, use_smem);
 }
 
+// shared memory of the Jacobi kernel: A (FP64) when it fits, the eigenvector
+// matrix when it also fits, and the pair and block tables
+static size_t jacobi_tables(int max_nb) {
+  const size_t np = (size_t)(max_nb + 1) / 2;
+  return np * (sizeof(double2) + 2 * sizeof(double) + 3 * sizeof(int)) + np * (np + 1) / 2 * 4 + 64;
+}
+constexpr size_t kJacobiSmem = 227 * 1024 - 4096;   // static reduction arrays take 4 KB
+
 void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
                    double2 *C, const long long *mat_off, double *eig, double2 *scratch,
-                   int max_sweeps, double tol, int *sweeps_out, cudaStream_t st) {
+                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st) {
   if (nks <= 0) return;
-  const int v_smem = jacobi_v_fits_smem(max_nb);
-  const int ne = max_nb + 1;
-  const size_t sm = (size_t)max_nb * max_nb * sizeof(double2) * (v_smem ? 2 : 1) +
-                    (size_t)ne / 2 * (2 * sizeof(double) + sizeof(double2) + 2 * sizeof(int)) +
-                    (size_t)(ne + 1) * sizeof(int) + 64;
-  cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  derek::note_launch(), k_jacobi<<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps, tol,
-                                 v_smem, sweeps_out);
+  const size_t nn = (size_t)max_nb * max_nb;
+  const size_t tab = jacobi_tables(max_nb);
+  const size_t vbytes = (nn * (fp32_vectors ? sizeof(float2) : sizeof(double2)) + 15) / 16 * 16;
+  const int a_smem = nn * sizeof(double2) + tab <= kJacobiSmem;
+  const int v_smem = a_smem && nn * sizeof(double2) + vbytes + tab <= kJacobiSmem;
+  const size_t sm = (a_smem ? nn * sizeof(double2) : 0) + (v_smem ? vbytes : 0) + tab;
+  if (fp32_vectors) {
+    cudaFuncSetAttribute(k_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    derek::note_launch(), k_jacobi<float><<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps,
+                                                                tol, a_smem, v_smem, sweeps_out);
+  } else {
+    cudaFuncSetAttribute(k_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    derek::note_launch(), k_jacobi<double><<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps,
+                                                                 tol, a_smem, v_smem, sweeps_out);
+  }
 }
 
 #define DEREK_INST(R)                                                                          \

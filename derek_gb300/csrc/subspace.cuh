@@ -29,13 +29,13 @@ template <typename R>
 void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, cplx<R> *X,
                    const double2 *C, const long long *mat_off, cudaStream_t st);
 bool cholesky_fits_smem(int max_nb);
-bool jacobi_v_fits_smem(int max_nb);
 void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *S,
                          double2 *C, const long long *mat_off, double2 *scratch, int *status,
                          cudaStream_t st);
+// fp32_vectors: accumulate the eigenvectors in FP32 (A stays FP64)
 void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
                    double2 *C, const long long *mat_off, double *eig, double2 *scratch,
-                   int max_sweeps, double tol, int *sweeps_out, cudaStream_t st);
+                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st);
 
 // Per-system SCF scalars kept on the device.
 constexpr int kMaxHist = 16;
