@@ -46,11 +46,11 @@ __global__ void k_to_float(long long n, const double *__restrict__ a, float *__r
 
 template <typename R>
 static void apply_h_class(derek_gpu *h, const Tables &t, int item_begin, int nitems, int nchunk,
-                          const int n[3], int max_my, const void *in, const void *prev, void *out,
+                          const int n[3], int max_yz, const void *in, const void *prev, void *out,
                           const Axpby *coef, const R *vloc) {
   launch_x_inv<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)in,
                   (cplx<R> *)h->d_abuf, nullptr, h->stream);
-  launch_plane<R>(t, item_begin, nitems, n[0], n[1], n[2], n[1], n[2], max_my, (cplx<R> *)h->d_abuf,
+  launch_plane<R>(t, item_begin, nitems, n[0], n[1], n[2], n[1], n[2], max_yz, (cplx<R> *)h->d_abuf,
                   vloc, h->stream);
   launch_x_fwd<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)h->d_abuf,
                   (const cplx<R> *)in, (const cplx<R> *)prev, (cplx<R> *)out, coef, h->stream);
@@ -65,14 +65,14 @@ static void apply_h_t(derek_gpu *h, const Tables &base, int item_begin, int nite
     for (const auto &c : h->classes) {
       Tables t = base;
       t.item_list = c.d_list;
-      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, c.max_my, in, prev, out, coef, vloc);
+      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, c.max_yz, in, prev, out, coef, vloc);
     }
     return;
   }
   const KSetDev &K = h->ks[h->item_ks[item_begin]];
   const SysDev &S = h->sys[K.sys];
   apply_h_class<R>(h, base, item_begin, nitems, (K.ncol + kColChunk - 1) / kColChunk, S.n,
-                   h->ks_max_my[h->item_ks[item_begin]], in, prev, out, coef, vloc);
+                   h->ks_max_yz[h->item_ks[item_begin]], in, prev, out, coef, vloc);
 }
 
 int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
@@ -103,7 +103,7 @@ template <typename R> static void density_t(derek_gpu *h, const void *psi) {
                     (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
   }
   launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
-                          h->min_n[2], h->max_my_all, (const cplx<R> *)h->d_abuf, h->d_occw,
+                          h->min_n[2], h->max_yz_all, (const cplx<R> *)h->d_abuf, h->d_occw,
                           h->d_partial, h->d_partial_off, h->stream);
 }
 
@@ -355,7 +355,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       for (int i = 0; i < npw; ++i) cols[{sp.my[i], sp.mz[i]}].push_back(i);
       K.ncol = (int)cols.size();
       K.ncol_pad = (K.ncol + 15) / 16 * 16;
-      int c = 0, e = 0, last_row = -1, max_my = 0;
+      int c = 0, e = 0, last_row = -1, max_yz = 0;
       std::vector<short> krows;
       for (auto &kv : cols) {
         const int iy = ((kv.first.first % nfine[1]) + nfine[1]) % nfine[1];
@@ -372,10 +372,10 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
           kin32.push_back((float)sp.kinetic[ref]);
           ++e;
         }
+        max_yz = std::max(max_yz, std::max(std::abs(kv.first.first), std::abs(kv.first.second)));
         if (kv.first.first != last_row) {
           krows.push_back((short)iy);
           last_row = kv.first.first;
-          max_my = std::max(max_my, std::abs(last_row));
         }
         ++c;
       }
@@ -384,8 +384,8 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       col_y.push_back(0);
       col_z.push_back(0);
       K.nrow = (int)krows.size();
-      h->ks_max_my.push_back(max_my);
-      h->max_my_all = std::max(h->max_my_all, max_my);
+      h->ks_max_yz.push_back(max_yz);
+      h->max_yz_all = std::max(h->max_yz_all, max_yz);
       rows.insert(rows.end(), krows.begin(), krows.end());
       for (int i = 0; i < npw; ++i) {
         const int ix = ((sp.mx[i] % nfine[0]) + nfine[0]) % nfine[0];
@@ -508,14 +508,14 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       const std::array<int, 3> key = {S.n[0], S.n[1], S.n[2]};
       groups[key].push_back(it);
       chunks[key] = std::max(chunks[key], (K.ncol + kColChunk - 1) / kColChunk);
-      mys[key] = std::max(mys[key], h->ks_max_my[h->item_ks[it]]);
+      mys[key] = std::max(mys[key], h->ks_max_yz[h->item_ks[it]]);
     }
     for (auto &g : groups) {
       derek_gpu::ItemClass c{};
       for (int i = 0; i < 3; ++i) c.n[i] = g.first[i];
       c.count = (int)g.second.size();
       c.nchunk = chunks[g.first];
-      c.max_my = mys[g.first];
+      c.max_yz = mys[g.first];
       c.d_list = nullptr;
       if (groups.size() > 1) CK(upload(&c.d_list, g.second));
       h->classes.push_back(c);
@@ -780,10 +780,10 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       Tables t = h->tab;
       t.item_list = c.d_list;
       if (h->prec == DEREK_PREC_FP64)
-        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_my,
+        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_yz,
                              (double2 *)h->d_abuf, h->d_vloc, h->stream);
       else
-        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_my,
+        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_yz,
                             (float2 *)h->d_abuf, h->d_vloc32, h->stream);
     }
     cudaEventRecord(ev[2], h->stream);

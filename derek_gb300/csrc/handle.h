@@ -97,12 +97,12 @@ struct derek_gpu {
     int n[3];
     int count;
     int nchunk;
-    int max_my;    // largest |centred Miller y| of a sphere column in the class
+    int max_yz;    // largest |centred Miller y or z| of a sphere column in the class
     int *d_list;   // nullptr when the class is the contiguous range of all items
   };
   std::vector<ItemClass> classes;
-  std::vector<int> ks_max_my;   // per k-set: largest |centred Miller y| of its columns
-  int max_my_all = 0;
+  std::vector<int> ks_max_yz;   // per k-set: largest |centred Miller y or z| of its columns
+  int max_yz_all = 0;
 
   cudaStream_t stream = nullptr;
   std::string last_error;

@@ -492,11 +492,11 @@ static bool try_plane_fixed(const Tables &t, int item_begin, int nitems, int max
 
 template <typename R>
 void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2, int max_n3,
-                  int min_n2, int min_n3, int max_my, cplx<R> *abuf, const R *vloc, cudaStream_t st) {
+                  int min_n2, int min_n3, int max_yz, cplx<R> *abuf, const R *vloc, cudaStream_t st) {
   if (nitems <= 0) return;
   if constexpr (std::is_same<R, float>::value) {
     if (max_n2 == max_n3 && min_n2 == max_n2 && min_n3 == max_n3 &&
-        launch_plane_reg(t, item_begin, nitems, max_n1, max_n2, max_my, abuf, vloc, st))
+        launch_plane_reg(t, item_begin, nitems, max_n1, max_n2, max_yz, abuf, vloc, st))
       return;
   }
   if (try_plane_fixed<R, 72>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
@@ -527,12 +527,12 @@ static bool try_density_fixed(const Tables &t, int ks_begin, int nks, int max_n1
 
 template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
-                          int min_n2, int min_n3, int max_my, const cplx<R> *abuf, const double *occ,
+                          int min_n2, int min_n3, int max_yz, const cplx<R> *abuf, const double *occ,
                           double *partial, const long long *partial_off, cudaStream_t st) {
   if (nks <= 0) return;
   if constexpr (std::is_same<R, float>::value) {
     if (max_n2 == max_n3 && min_n2 == max_n2 && min_n3 == max_n3 &&
-        launch_density_reg(t, ks_begin, nks, max_n1, max_n2, max_my, abuf, occ, partial, partial_off, st))
+        launch_density_reg(t, ks_begin, nks, max_n1, max_n2, max_yz, abuf, occ, partial, partial_off, st))
       return;
   }
   if (try_density_fixed<R, 72>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||

@@ -21,13 +21,13 @@
 #include "kernels.cuh"
 #include "regfft.cuh"
 
-#include <cstdlib>
-
 namespace derek {
 
 // Shared-memory layout of one plane (rows my in [-RY, RY]) and of one V(r)
 // plane.  The plane pitch PP is congruent to N mod 16 and the V pitch VP to N
 // mod 32, so a warp straddling two planes still reads consecutive banks.
+// kept(j): line index j (0 <= j < N) has a centred index within [-RY, RY];
+// the same bound holds for the z index of every sphere column.
 template <int N, int RY> struct RowsLayout {
   static_assert(RY >= 0 && 2 * RY + 1 <= N + 1, "row bound");
   static constexpr int NRW = 2 * RY + 1;
@@ -35,7 +35,7 @@ template <int N, int RY> struct RowsLayout {
   static constexpr int PP0 = NRW * PZ;
   static constexpr int PP = PP0 + ((N - PP0) % 16 + 16) % 16;
   static constexpr int VP = N * N + ((N - N * N) % 32 + 32) % 32;
-  // centred index of y row j (0 <= j < N)
+  // centred index of line index j (0 <= j < N)
   __host__ __device__ static constexpr int my_of(int j) { return j > N / 2 ? j - N : j; }
   __host__ __device__ static constexpr bool kept(int j) { return my_of(j) >= -RY && my_of(j) <= RY; }
   __host__ __device__ static constexpr int row_of(int j) { return my_of(j) + RY; }
@@ -82,7 +82,9 @@ __device__ __forceinline__ void load_column(float2 (&v)[N], const float2 *col) {
   });
 }
 
-// z transforms of the rows holding columns, planes [0, np)
+// z transforms of the rows holding columns, planes [0, np).  The backward
+// transform reads only the z positions a sphere column can occupy (the rest
+// of the row is zero); the forward one stores only those positions.
 template <int N, int RY, int SIGN>
 __device__ __forceinline__ void z_pass(float2 *P, int np, int nrow, const short *__restrict__ rows) {
   using Lay = RowsLayout<N, RY>;
@@ -92,9 +94,24 @@ __device__ __forceinline__ void z_pass(float2 *P, int np, int nrow, const short 
     const int l = tid - p * nrow;
     float2 *line = P + p * Lay::PP + Lay::row_of(rows[l]) * Lay::PZ;
     float2 v[N];
-    load_line<N>(v, line, 1);
-    reg_fft<N, SIGN, 0>(v);
-    store_line<N, 1>(v, line, 1);
+    if (SIGN > 0) {
+      static_for<0, N>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        if constexpr (Lay::kept(j))
+          v[j] = line[j];
+        else
+          v[j] = make_float2(0.f, 0.f);
+      });
+      reg_fft<N, SIGN, 0>(v);
+      store_line<N, 1>(v, line, 1);
+    } else {
+      load_line<N>(v, line, 1);
+      reg_fft<N, SIGN, 0>(v);
+      static_for<0, N>([&](auto mc) {
+        constexpr int m = decltype(mc)::value;
+        if constexpr (Lay::kept(m)) line[m] = v[line_slot<N>(m, 1)];
+      });
+    }
   }
 }
 
@@ -308,26 +325,10 @@ static void plane_rows_go_x(const Tables &t, int item_begin, int nitems, int max
   derek::note_launch(), kern<<<dim3(nitems, ng), NT, smem, st>>>(t, item_begin, abuf, vloc);
 }
 
-static int plane_variant() {
-  static int v = [] {
-    const char *e = getenv("DEREK_PLANE_VARIANT");
-    return e ? atoi(e) : 0;
-  }();
-  return v;
-}
-
 template <int N, int RY>
 static void plane_rows_go(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
                           const float *vloc, cudaStream_t st) {
   using Sh = RowsShape<N, RY, false>;
-  if (N == 72 && RY < N / 2) {
-    switch (plane_variant()) {
-      case 1: plane_rows_go_x<N, RY, 2, 2>(t, item_begin, nitems, max_n1, abuf, vloc, st); return;
-      case 2: plane_rows_go_x<N, RY, 1, 4>(t, item_begin, nitems, max_n1, abuf, vloc, st); return;
-      case 3: plane_rows_go_x<N, RY, 4, 1>(t, item_begin, nitems, max_n1, abuf, vloc, st); return;
-      default: break;
-    }
-  }
   plane_rows_go_x<N, RY, Sh::XP, 1>(t, item_begin, nitems, max_n1, abuf, vloc, st);
 }
 
@@ -343,50 +344,50 @@ static void density_rows_go(const Tables &t, int ks_begin, int nks, int max_n1, 
 }
 
 template <int N>
-static void plane_go(const Tables &t, int item_begin, int nitems, int max_n1, int max_my, float2 *abuf,
+static void plane_go(const Tables &t, int item_begin, int nitems, int max_n1, int max_yz, float2 *abuf,
                      const float *vloc, cudaStream_t st) {
-  if (max_my <= compact_ry<N>())
+  if (max_yz <= compact_ry<N>())
     plane_rows_go<N, compact_ry<N>()>(t, item_begin, nitems, max_n1, abuf, vloc, st);
   else
     plane_rows_go<N, N / 2>(t, item_begin, nitems, max_n1, abuf, vloc, st);
 }
 
 template <int N>
-static void density_go(const Tables &t, int ks_begin, int nks, int max_n1, int max_my, const float2 *abuf,
+static void density_go(const Tables &t, int ks_begin, int nks, int max_n1, int max_yz, const float2 *abuf,
                        const double *occ, double *partial, const long long *partial_off, cudaStream_t st) {
-  if (max_my <= compact_ry<N>())
+  if (max_yz <= compact_ry<N>())
     density_rows_go<N, compact_ry<N>()>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
   else
     density_rows_go<N, N / 2>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
 }
 
-bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_my,
+bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_yz,
                       float2 *abuf, const float *vloc, cudaStream_t st) {
   switch (n) {
-    case 72: plane_go<72>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
-    case 64: plane_go<64>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
-    case 54: plane_go<54>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
-    case 48: plane_go<48>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
-    case 36: plane_go<36>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
-    case 32: plane_go<32>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
-    case 27: plane_go<27>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
-    case 24: plane_go<24>(t, item_begin, nitems, max_n1, max_my, abuf, vloc, st); return true;
+    case 72: plane_go<72>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 64: plane_go<64>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 54: plane_go<54>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 48: plane_go<48>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 36: plane_go<36>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 32: plane_go<32>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 27: plane_go<27>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 24: plane_go<24>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
     default: return false;
   }
 }
 
-bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_my,
+bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_yz,
                         const float2 *abuf, const double *occ, double *partial,
                         const long long *partial_off, cudaStream_t st) {
   switch (n) {
-    case 72: density_go<72>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
-    case 64: density_go<64>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
-    case 54: density_go<54>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
-    case 48: density_go<48>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
-    case 36: density_go<36>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
-    case 32: density_go<32>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
-    case 27: density_go<27>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
-    case 24: density_go<24>(t, ks_begin, nks, max_n1, max_my, abuf, occ, partial, partial_off, st); return true;
+    case 72: density_go<72>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 64: density_go<64>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 54: density_go<54>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 48: density_go<48>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 36: density_go<36>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 32: density_go<32>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 27: density_go<27>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 24: density_go<24>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
     default: return false;
   }
 }
