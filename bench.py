@@ -17,10 +17,15 @@ value  : ground states/s with inputs resident on the device (handle reused,
 e2e    : the same through the C ABI with host buffers: each step uploads the
          external potential from pinned host memory, runs the SCF and copies
          eigenvalues, occupations and density back.
-roofline: the fused H.psi (three stage kernels over all 64 x 80 bands),
-         algorithmic bytes = psi in + H psi out (8 B per complex64 coefficient)
-         + the sphere index map (4 B per plane wave) + V(r) (4 B per point),
-         divided by its CUDA-event time, against MEASURED_PEAKS.json hbm_gbs.
+roofline: the fused H.psi (three stage kernels over all 64 k-points x 84
+         carried bands), algorithmic bytes = psi in + H psi out (8 B per
+         complex64 coefficient) + the sphere index map (4 B per plane wave) +
+         V(r) (4 B per point), divided by its CUDA-event time (events on the
+         library's stream), against MEASURED_PEAKS.json hbm_gbs.  traffic is
+         the DRAM bytes ncu counted for the three stage kernels on the
+         4-k-point case, per band item, times the items of one launch.  The
+         dominant stage, the (y,z)-plane pass, is bound by FP32 issue, not by
+         HBM: its FFT rate (5 n log2 n flops per line) is reported beside it.
 The working set (planes buffer ~7 GB) is far larger than L2, so no flush is
 needed between steps.
 
@@ -111,6 +116,14 @@ class Clocks:
                 "samples": len(sm)}
 
 
+# DRAM bytes per (k-point, band) item of one H.psi, summed over k_xinv_reg,
+# k_plane_rows and k_xfwd_reg, from one ncu capture of the 4-k-point case
+# (336 items: 143.1 + 256.6 + 236.0 MB).
+TRAFFIC_PER_ITEM = 635.7e6 / 336
+# nominal FP32 rate of a GB300: 152 SMs x 128 lanes x 2 flops x 2.07 GHz
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -131,6 +144,27 @@ def hpsi_bytes(h, specs, elem=8, real=4):
         for k in range(len(s.kpts)):
             npw = h.npw(si, k)
             total += 2 * elem * npw * nbi + 4 * npw
+    return total
+
+
+def plane_fft_flops(h, specs):
+    """FFT flops of one (y,z)-plane pass: per item and x-plane, the backward
+    and forward z transforms of the rows holding sphere columns and the
+    backward and forward y transforms of every z, 5 n log2 n flops each."""
+    import math
+    import numpy as np
+    total = 0.0
+    for si, s in enumerate(specs):
+        nf, _ = h.grid(si)
+        nbi = h.bands(si)[1]
+        for k in range(len(s.kpts)):
+            _, fidx, _ = h.gsphere(si, k)
+            iy = (np.asarray(fidx) // nf[2]) % nf[1]
+            nrow = len(np.unique(iy))
+            lines_z = 2 * nrow * nf[0]
+            lines_y = 2 * nf[2] * nf[0]
+            total += nbi * (lines_z * 5 * nf[2] * math.log2(nf[2]) +
+                            lines_y * 5 * nf[1] * math.log2(nf[1]))
     return total
 
 
@@ -212,16 +246,28 @@ def run_ours(args):
     # ---- roofline of the fused H.psi
     t_apply, stages = h.time_apply_h(nrep=5)
     nbytes = hpsi_bytes(h, specs)
+    nitems = sum(h.bands(si)[1] * len(s.kpts) for si, s in enumerate(specs))
     peak, src = measured_peaks()
     achieved = nbytes / (t_apply / 1e3) / 1e9
-    stage_names = ["inv_yz (scatter + backward z,y)", "vmul_x (backward x, V(r), forward x)",
-                   "fwd_yz (forward y,z + gather + kinetic)"]
+    stage_names = ["k_xinv_reg (scatter + backward x)",
+                   "k_plane_rows (backward z,y + V(r) + forward y,z)",
+                   "k_xfwd_reg (forward x + gather + kinetic + epilogue)"]
+    fft_tflops = plane_fft_flops(h, specs) / (stages[1] / 1e3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None,
-                "kernel": "fused H.psi, 3 stage kernels over 64 k x 80 bands",
+                "frac": round(achieved / peak, 4),
+                "traffic": round(TRAFFIC_PER_ITEM * nitems),
+                "traffic_source": "ncu dram__bytes_read+write of the 3 stage kernels, 4-k-point "
+                                  "case scaled by band items (profiles/hpsi_kpts64_k4_ncu.md)",
+                "kernel": f"fused H.psi, 3 stage kernels over {nitems} (k-point, band) items",
                 "bytes_per_launch": nbytes, "ms_per_launch": round(t_apply, 4),
                 "stage_ms": {n: round(x, 4) for n, x in zip(stage_names, stages)},
-                "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)"}
+                "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)",
+                "dominant_kernel": {
+                    "name": "k_plane_rows", "share_of_hpsi": round(stages[1] / sum(stages), 3),
+                    "bound": "fp32 issue", "fft_tflops": round(fft_tflops, 2),
+                    "fp32_peak_tflops": round(FP32_NOMINAL_TFLOPS, 1),
+                    "fp32_frac": round(fft_tflops / FP32_NOMINAL_TFLOPS, 3),
+                    "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz)"}}
     bands_per_gs = _hpsi_band_applications(specs, reps[-1], scf_opts)
 
     out.update({

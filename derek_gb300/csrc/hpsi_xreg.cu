@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kXCols, 4) k_xfwd_reg(Tables t, int item_begin
   const short *eix = t.ent_ix + K.ent_off;
   const float *kin = t.kin32 + K.ent_off;
   const long long off = K.psi_off + (long long)b * K.npw_pad;
-  const float inv_n = (float)(1.0 / (double)S.nr);
+  const float inv_n = 1.0f / (float)S.nr;
   float al = 1, be = 0, ga = 0, tk = 1;
   if (coef) {
     al = (float)coef[ksi].alpha;

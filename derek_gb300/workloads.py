@@ -8,6 +8,7 @@ uniform in the cell), spin-unpolarised, Fermi-Dirac smearing kT = 0.01 Ha:
                8 bands, 4 wells, Pulay alpha=0.3
   kpts64       L=16, Ecut=20, grid 72^3, 4x4x4 Monkhorst-Pack (64 k-points),
                64 electrons in 80 bands, 16 wells, Kerker + Pulay
+  kpts64_k4    kpts64 with its first 4 k-points only (profiler captures)
   adjoint9k    L=12, Ecut=15, grid 48^3, Gamma + 2x2x2 (9 k-points), 16
                electrons in 20 bands, 8 wells
   uneven256    256 systems, L ~ U[8,20], Ecut=15, {2,3}-smooth grids, 2..64
@@ -56,6 +57,16 @@ def kpts64(seed=2):
         dict(mix_alpha=0.3, kerker_q0=0.8)
 
 
+def kpts64_k4(seed=2):
+    """kpts64 cut to its first 4 k-points: the same kernels on a case small
+    enough for a full profiler capture."""
+    specs, mix = kpts64(seed)
+    specs[0].kpts = specs[0].kpts[:4].copy()
+    if specs[0].wk is not None:
+        specs[0].wk = specs[0].wk[:4].copy()
+    return specs, mix
+
+
 def adjoint9k(seed=3):
     rng = np.random.default_rng(seed)
     k = np.concatenate([[[0.0, 0.0, 0.0]], mp_grid((2, 2, 2))])
@@ -81,4 +92,5 @@ def uneven(count=256, seed=5):
     return specs, dict(mix_alpha=0.3, kerker_q0=0.8)
 
 
-WORKLOADS = {"gamma_8e": gamma_8e, "kpts64": kpts64, "adjoint9k": adjoint9k, "uneven256": uneven}
+WORKLOADS = {"gamma_8e": gamma_8e, "kpts64": kpts64, "kpts64_k4": kpts64_k4, "adjoint9k": adjoint9k,
+             "uneven256": uneven}
