@@ -16,13 +16,13 @@ void launch_overlap(const Tables &t, int ks_begin, int nks, int max_nb, int max_
 void launch_overlap_reduce(const Tables &t, int ks_begin, int nks, const double2 *part,
                            const long long *part_off, int ksplit, double2 *out,
                            const long long *mat_off, int hermitize, cudaStream_t st);
-// BF16x3 tcgen05 overlap (complex64 inputs, nb <= 128), same partial layout
+// split-BF16 tcgen05 overlap (complex64 inputs, nb <= 128), same partial layout
 size_t overlap_tc_smem(int max_nb);
 void launch_overlap_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, int ksplit,
                        const float2 *X, const float2 *Y, double2 *part, const long long *part_off,
                        double2 *out, const long long *mat_off, int hermitize, int *status,
                        cudaStream_t st);
-// BF16x3 tcgen05 rotation X <- X C (complex64, nb <= 128), in place
+// split-BF16 tcgen05 rotation X <- X C (complex64, nb <= 128), in place
 void launch_rotate_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, float2 *X,
                       const double2 *C, const long long *mat_off, int *status, cudaStream_t st);
 template <typename R>

@@ -1,4 +1,4 @@
-// Split-precision (BF16x3) overlap matrices on the 5th-generation tensor
+// Split-precision BF16 overlap matrices on the 5th-generation tensor
 // cores: S = X^H Y for every k-set, X, Y complex64 [nb][npw].
 //
 // Real form: with the interleaved (re, im) coefficients as the contraction
@@ -6,13 +6,18 @@
 //   Re S_ij = sum_K X_i[K] Y_j[K],   Im S_ij = sum_K X_i[K] (-i Y_j)[K]
 // where (-i y) interleaves (y_im, -y_re).  One GEMM with A = X (M = 128 rows,
 // bands padded) and B = [Y ; -iY] (N = 2 nb rounded to 16) yields both parts.
-// Each FP32 operand is split into bf16 hi + lo, and the three products
-// hi*hi + hi*lo + lo*hi accumulate in FP32 in tensor memory.
+// Each FP32 operand is split into bf16 hi + lo, and the four products
+// hi*hi + hi*lo + lo*hi + lo*lo accumulate in FP32 in tensor memory.  The
+// lo*lo term is kept: on a Gram diagonal sum_K x_K^2 it has one sign for
+// every K, so dropping it (the usual three-product split) biases |x|^2 low by
+// about 2^-18 relative, which shows up as an excess electron count and a
+// free-energy offset near 1e-6 Ha per electron; with it the remaining error
+// (rounding of lo) has random sign.
 //
 // One CTA owns one k-set's K-range (split-K).  Per 64-element K block the
 // 256 threads convert their share of X and Y into the canonical no-swizzle
 // K-major core-matrix layout (8 rows x 16 bytes per core matrix), one thread
-// issues the 12 tcgen05.mma (4 K-steps x 3 products) and commits them to the
+// issues the 16 tcgen05.mma (4 K-steps x 4 products) and commits them to the
 // stage's mbarrier; two stages overlap conversion with the MMAs.  The
 // accumulator is read back with tcgen05.ld and written as an FP64 partial
 // that k_overlap_reduce sums over the splits.
@@ -238,6 +243,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         mma_bf16(tmem, dah, dbh, idesc, (kb > 0 || ks > 0) ? 1u : 0u);
         mma_bf16(tmem, dah, dbl, idesc, 1u);
         mma_bf16(tmem, dal, dbh, idesc, 1u);
+        mma_bf16(tmem, dal, dbl, idesc, 1u);
       }
       mma_commit(&bars[s]);
     }
@@ -303,7 +309,8 @@ void launch_overlap_tc(const Tables &t, int ks_begin, int nks, int max_nb, int m
 }  // namespace derek
 
 // ---------------------------------------------------------------------------
-// Rotation X <- X C on the tensor cores (BF16x3), in place per 128-G tile.
+// Rotation X <- X C on the tensor cores (bf16 hi + lo split, four products),
+// in place per 128-G tile.
 //
 // Real form per coefficient G: with x_G = (Re X_0, Im X_0, Re X_1, ...) the
 // rotated row is y_G = M x_G, M = [[Re C, -Im C], [Im C, Re C]] per (i, j)
@@ -423,6 +430,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         mma_bf16(tmem, dah, dbh, idesc, (kb > 0 || ks > 0) ? 1u : 0u);
         mma_bf16(tmem, dah, dbl, idesc, 1u);
         mma_bf16(tmem, dal, dbh, idesc, 1u);
+        mma_bf16(tmem, dal, dbl, idesc, 1u);
       }
       mma_commit(&bars[s]);
     }

@@ -48,9 +48,11 @@ extern "C" {
 
 /* precision modes */
 #define DEREK_PREC_FP64   0   /* complex128 psi, FP64 FFTs and contractions */
-#define DEREK_PREC_MIXED  1   /* complex64 psi, FP32 FFTs and H.psi, BF16x3
-                                 tensor-core contractions; FP64 Cholesky,
-                                 Jacobi, occupations, densities, energies */
+#define DEREK_PREC_MIXED  1   /* complex64 psi, FP32 FFTs and H.psi, split-BF16
+                                 tensor-core contractions (hi + lo per operand,
+                                 four products, FP32 accumulation); FP64
+                                 Cholesky, Jacobi, occupations, densities,
+                                 energies */
 
 /* grid policies for n_fine = 0 */
 #define DEREK_GRID_REFERENCE 0  /* basis_prime_fact: {2,3,5,7,11,13}-smooth */
@@ -90,8 +92,9 @@ typedef struct {
   int    first_degree;     /* filter degree of those passes */
   uint64_t seed;           /* start-vector hash seed */
   int    use_graph;        /* capture each SCF iteration in a CUDA graph */
-  int    use_tensor_cores; /* mixed mode: 1 = tcgen05 BF16x3 overlaps,
-                              2 = overlaps and rotations, 0 = CUDA cores */
+  int    use_tensor_cores; /* mixed mode: 2 = tcgen05 split-BF16 overlaps and
+                              rotations (default), 1 = overlaps only,
+                              0 = CUDA cores */
   double density_tol;      /* also require max|n_out - n_in| < density_tol
                               (0 = energy criterion only, as the reference) */
   int    buffer_bands;     /* extra unreported bands carried by the filtered

@@ -217,12 +217,13 @@ def test_uneven_batch_apply_h(oracle):
 
 @pytest.mark.parametrize("nb", [6, 20, 88])
 def test_overlap_tensor_cores_match_fp64(oracle, nb):
-    """S = psi^H psi of complex64 wavefunctions: BF16x3 tcgen05 path and the
-    FP32 CUDA-core path against FP64 numpy on the same (FP32-rounded) data.
-    Tolerance relative to max|S|: 5e-5 for BF16x3 (hi*hi + hi*lo + lo*hi
-    leaves ~2^-16 per product and the tensor-core FP32 accumulation of a
-    2048-coefficient split adds to it; measured 1.6e-5), 5e-6 for FP32
-    (single-precision sums over npw ~ 1000 terms; measured 1.6e-6)."""
+    """S = psi^H psi of complex64 wavefunctions: split-BF16 tcgen05 path and
+    the FP32 CUDA-core path against FP64 numpy on the same (FP32-rounded)
+    data.  Tolerance relative to max|S|: 5e-5 for the tensor cores (the lo
+    part of each operand is itself rounded to bf16, ~2^-17 per product, and
+    the tensor-core FP32 accumulation of a 2048-coefficient split adds to
+    it), 5e-6 for FP32 (single-precision sums over npw ~ 1000 terms;
+    measured 1.6e-6)."""
     import derek_gb300 as dg
     L = 9.0 if nb < 50 else 12.0
     s, spec = make_pair(oracle, L=L, ecut=6.0, nb=nb, nelec=2.0)

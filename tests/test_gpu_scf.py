@@ -59,11 +59,9 @@ def test_scf_mixed_precision_accuracy(oracle, tc):
         rho = h.density()
     assert rep["converged"], rep
     per_electron = abs(rep["free_energy"] - d["free_energy"]) / float(d["nelec"])
-    # tc = 2 also rotates the subspace with BF16x3 tensor-core products; their
-    # ~2^-16 relative error leaves the orthonormality at ~1e-5 and the free
-    # energy at ~1e-6 Ha per electron (measured 1.05e-6), so the headline path
-    # keeps rotations in FP32 (tc = 1) and this mode is held to 2e-6
-    assert per_electron < (2e-6 if tc == 2 else 1e-6), per_electron
+    # the tensor-core products keep all four hi/lo terms, so the overlaps
+    # carry no sign-biased error and every mode meets the same target
+    assert per_electron < 1e-6, per_electron
     assert np.max(np.abs(eig - d["eig"])) < 1e-4
     rel = np.linalg.norm(rho - d["density"]) / np.linalg.norm(d["density"])
     assert rel < 1e-3, rel
