@@ -69,8 +69,13 @@ int cholqr_rr(derek_gpu *h) {
   int st = apply_h_items(h, 0, h->nitems, X, nullptr, h->d_HX, nullptr);
   if (st) return st;
   overlap_all(h, X, h->d_HX, h->d_Hs, 1);
+  // Off-diagonal Frobenius target relative to ||Hs||: 1e-14 on the FP64 path;
+  // on the mixed path Hs itself carries the FP32 H.psi error (~1e-7
+  // relative), so 1e-10 leaves eigenvalue errors of order 1e-20 / gap while
+  // saving about one of the four sweeps near convergence.
+  const double jtol = h->prec == DEREK_PREC_FP64 ? 1e-14 : 1e-10;
   launch_jacobi(h->tab, 0, h->nks, h->max_nb, h->d_Hs, h->d_C, h->d_mat_off, h->d_eig,
-                h->d_scratch, 30, 1e-14, 0, h->d_sweeps, h->stream);
+                h->d_scratch, 30, jtol, 0, h->d_sweeps, h->stream);
   rotate_all(h, X, h->d_C);
   return DEREK_OK;
 }
