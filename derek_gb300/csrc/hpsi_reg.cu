@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(NT, MINB) k_plane_rows(Tables t, int item_begi
   constexpr int PZ = Lay::PZ, PP = Lay::PP, VP = Lay::VP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *P = reinterpret_cast<float2 *>(smem_raw);
-  float *Vs = reinterpret_cast<float *>(P + XP * PP);
+  // V buffer 16-byte aligned for the 16-byte copies
+  float *Vs = reinterpret_cast<float *>(smem_raw + (((size_t)XP * PP * sizeof(float2) + 15) & ~(size_t)15));
   const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
   const int ksi = t.item_ks[item];
   const KSetDev &K = t.ks[ksi];
