@@ -1,8 +1,10 @@
 // FP32 (y,z)-plane passes with every line transform held in one thread's
 // registers (regfft.cuh).
 //
-// A block owns XP consecutive x-planes of one item (apply H) or of one k-set
-// (density).  Each plane sits in shared memory as the rows of centred Miller
+// A block works on XP consecutive x-planes: of one k-set, band after band
+// (density), or of a sequence of items (apply H, one block per SM keeping its
+// group of x-planes and its V(r) planes).  Each plane sits in shared memory
+// as the rows of centred Miller
 // index my in [-RY, RY] (row my + RY), PZ elements per row: the rows a
 // sphere's columns can occupy.  Every other y row of the plane is zero after
 // the backward z transforms and is not needed after the forward y
@@ -17,7 +19,7 @@
 // (y pass), so no shared-memory access has a bank conflict, and a whole line
 // costs one load and one store per element.  The V(r) planes of the block
 // are copied into shared memory with cp.async while the columns are gathered
-// and the z transforms run.
+// and the z transforms run, and stay there while the system is unchanged.
 #include "kernels.cuh"
 #include "regfft.cuh"
 
@@ -134,79 +136,209 @@ __device__ __forceinline__ void move_columns(float2 *P, float2 *a0, long long ld
   }
 }
 
-template <int N, int RY, int XP, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) k_plane_rows(Tables t, int item_begin, float2 *__restrict__ abuf,
-                                                      const float *__restrict__ vloc) {
-  using Lay = RowsLayout<N, RY>;
-  constexpr int PZ = Lay::PZ, PP = Lay::PP, VP = Lay::VP;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2 *P = reinterpret_cast<float2 *>(smem_raw);
-  // V buffer 16-byte aligned for the 16-byte copies
-  float *Vs = reinterpret_cast<float *>(smem_raw + (((size_t)XP * PP * sizeof(float2) + 15) & ~(size_t)15));
-  const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
-  const int ksi = t.item_ks[item];
-  const KSetDev &K = t.ks[ksi];
+// ---- H.psi (y,z) pass ----------------------------------------------------------
+// Block b keeps x-group g = b mod ng and walks the items r, r + R, ... with
+// r = b div ng, R = gridDim.x / ng.  Its V(r) planes stay in shared memory
+// while consecutive items belong to the same system.  While the forward z
+// transforms of a tile run (most threads idle), the threads without a z line
+// describe the next tile and stage its column and row offsets, so a tile
+// starts with one load round trip (its columns).
+struct PlaneTileSm {
+  long long a_base;    // offset of (band, x0) in the x-plane buffer
+  long long ld;        // x-plane buffer row pitch
+  long long vbase;     // offset of plane x0 in V(r)
+  int sys, ncol, nrow, np, valid, pad;
+};
+
+template <int N, int XP>
+__device__ __forceinline__ void plane_tile_describe(const Tables &t, int item_begin, int it, int g,
+                                                    PlaneTileSm &m) {
+  const int item = t.item_list ? t.item_list[it] : item_begin + it;
+  const KSetDev &K = t.ks[t.item_ks[item]];
   const SysDev &S = t.sys[K.sys];
-  if (!S.active) return;
   const int n1 = S.n[0];
-  const int x0 = blockIdx.y * XP;
-  if (x0 >= n1) return;
-  const int np = min(XP, n1 - x0);
+  const int x0 = g * XP;
+  m.valid = S.active && x0 < n1;
+  if (!m.valid) return;
   const int b = t.item_band[item];
-  const int tid = threadIdx.x;
-  // V(r) of the block's planes -> shared memory, in flight until the y pass
-  const float *vsrc = vloc + S.grid_off + (long long)x0 * N * N;
-  if (N % 4 == 0 && (reinterpret_cast<uintptr_t>(vsrc) & 15) == 0 &&
-      (reinterpret_cast<uintptr_t>(Vs) & 15) == 0) {
-    constexpr int Q = N * N / 4;
-    for (int i = tid; i < np * Q; i += NT) {
-      const int p = i / Q, r = i - p * Q;
-      cp_async16(Vs + p * VP + 4 * r, vsrc + (long long)p * N * N + 4 * r);
-    }
-  } else {
-    for (int i = tid; i < np * N * N; i += NT) {
-      const int p = i / (N * N), r = i - p * (N * N);
-      cp_async4(Vs + p * VP + r, vsrc + (long long)p * N * N + r);
-    }
-  }
-  cp_async_commit();
-  for (int i = tid; i < np * PP; i += NT) P[i] = make_float2(0.f, 0.f);
-  __syncthreads();
-  const long long ld = K.ncol_pad;
-  float2 *a0 = abuf + K.a_off + ((long long)b * n1 + x0) * ld;
+  m.sys = K.sys;
+  m.np = min(XP, n1 - x0);
+  m.ld = K.ncol_pad;
+  m.a_base = K.a_off + ((long long)b * n1 + x0) * K.ncol_pad;
+  m.vbase = S.grid_off + (long long)x0 * N * N;
+  m.ncol = K.ncol;
+  m.nrow = K.nrow;
+}
+
+// column offsets (row_of(y) PZ + z) and row offsets (row_of(y) PZ) of item
+// it's k-set, by the threads [t0, NT)
+template <int N, int RY, int NT>
+__device__ __forceinline__ void stage_offsets(const Tables &t, int item_begin, int it, int ncol, int nrow,
+                                              short *coff, short *roff, int t0) {
+  using Lay = RowsLayout<N, RY>;
+  const int tid = threadIdx.x - t0, nthr = NT - t0;
+  if (tid < 0) return;
+  const int item = t.item_list ? t.item_list[it] : item_begin + it;
+  const KSetDev &K = t.ks[t.item_ks[item]];
   const short *cy = t.col_y + K.col_off;
   const short *cz = t.col_z + K.col_off;
-  move_columns<N, RY, XP, NT, true>(P, a0, ld, np, K.ncol, cy, cz);
-  __syncthreads();
   const short *rows = t.rows + K.row_off;
-  z_pass<N, RY, +1>(P, np, K.nrow, rows);
-  cp_async_wait_all();
-  __syncthreads();
-  if (tid < np * N) {
-    const int p = tid / N;
-    const int z = tid - p * N;
-    float2 *col = P + p * PP + z;
-    const float *vz = Vs + p * VP + z;
-    float2 v[N];
-    load_column<N, RY>(v, col);
-    reg_fft<N, +1, 0>(v);
-    static_for<0, N>([&](auto mc) {
-      constexpr int m = decltype(mc)::value;
-      const float w = vz[m * N];
-      float2 &e = v[line_slot<N>(m, 1)];
-      e.x *= w;
-      e.y *= w;
-    });
-    reg_fft<N, -1, 1>(v);
-    static_for<0, N>([&](auto mc) {
-      constexpr int m = decltype(mc)::value;
-      if constexpr (Lay::kept(m)) col[Lay::row_of(m) * PZ] = v[line_slot<N>(m, 2)];
-    });
+  for (int c = tid; c < ncol; c += nthr) coff[c] = (short)(Lay::row_of(cy[c]) * Lay::PZ + cz[c]);
+  for (int l = tid; l < nrow; l += nthr) roff[l] = (short)(Lay::row_of(rows[l]) * Lay::PZ);
+}
+
+template <int N, int RY, int XP, int NT>
+__global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begin, int nitems, int ng,
+                                                         float2 *__restrict__ abuf,
+                                                         const float *__restrict__ vloc) {
+  using Lay = RowsLayout<N, RY>;
+  constexpr int PZ = Lay::PZ, PP = Lay::PP, VP = Lay::VP;
+  constexpr int MAXC = Lay::NRW * Lay::NRW, MAXR = Lay::NRW;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *P = reinterpret_cast<float2 *>(smem_raw);
+  float *Vs = reinterpret_cast<float *>(smem_raw + (((size_t)XP * PP * sizeof(float2) + 15) & ~(size_t)15));
+  short *offs = reinterpret_cast<short *>(Vs + XP * VP);   // [2][MAXC + MAXR]
+  __shared__ PlaneTileSm meta[2];
+  __shared__ int v_sys;   // system whose V(r) planes are in Vs (-1: none)
+  const int tid = threadIdx.x;
+  const int g = blockIdx.x % ng;
+  const int R = gridDim.x / ng;
+  int it = blockIdx.x / ng;
+  if (it >= nitems || blockIdx.x >= R * ng) return;   // whole block leaves together
+  if (tid == 0) {
+    plane_tile_describe<N, XP>(t, item_begin, it, g, meta[0]);
+    v_sys = -1;
   }
   __syncthreads();
-  z_pass<N, RY, -1>(P, np, K.nrow, rows);
-  __syncthreads();
-  move_columns<N, RY, XP, NT, false>(P, a0, ld, np, K.ncol, cy, cz);
+  if (meta[0].valid)
+    stage_offsets<N, RY, NT>(t, item_begin, it, meta[0].ncol, meta[0].nrow, offs, offs + MAXC, 0);
+  int cur = 0;
+  for (; it < nitems; it += R) {
+    const int valid = meta[cur].valid;
+    const short *coff = offs + cur * (MAXC + MAXR);
+    for (int i = tid; i < XP * PP; i += NT) P[i] = make_float2(0.f, 0.f);
+    __syncthreads();   // offsets staged, P zero
+    if (valid) {
+      const int sys = meta[cur].sys, np = meta[cur].np;
+      if (sys != v_sys) {   // uniform: new system, stage its V(r) planes
+        const float *vsrc = vloc + meta[cur].vbase;
+        if (N % 4 == 0 && (reinterpret_cast<uintptr_t>(vsrc) & 15) == 0) {
+          constexpr int Q = N * N / 4;
+          for (int i = tid; i < np * Q; i += NT) {
+            const int p = i / Q, r = i - p * Q;
+            cp_async16(Vs + p * VP + 4 * r, vsrc + (long long)p * N * N + 4 * r);
+          }
+        } else {
+          for (int i = tid; i < np * N * N; i += NT) {
+            const int p = i / (N * N), r = i - p * (N * N);
+            cp_async4(Vs + p * VP + r, vsrc + (long long)p * N * N + r);
+          }
+        }
+        cp_async_commit();
+      }
+      float2 *a0 = abuf + meta[cur].a_base;
+      const long long ld = meta[cur].ld;
+      const int ncol = meta[cur].ncol;
+#pragma unroll 4
+      for (int c = tid; c < ncol; c += NT) {
+        const int off = coff[c];
+#pragma unroll
+        for (int p = 0; p < XP; ++p)
+          if (p < np) P[p * PP + off] = a0[p * ld + c];
+      }
+    }
+    __syncthreads();
+    int zoff = -1, zthr = 0;
+    if (valid) {
+      const int nrow = meta[cur].nrow;
+      zthr = meta[cur].np * nrow;
+      if (tid < zthr) {
+        const int p = tid / nrow;
+        zoff = p * PP + coff[MAXC + tid - p * nrow];
+      }
+    }
+    if (zoff >= 0) {
+      float2 *line = P + zoff;
+      float2 v[N];
+      static_for<0, N>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        if constexpr (Lay::kept(j))
+          v[j] = line[j];
+        else
+          v[j] = make_float2(0.f, 0.f);
+      });
+      reg_fft<N, +1, 0>(v);
+      store_line<N, 1>(v, line, 1);
+    }
+    const int next = it + R;
+    if (tid == NT - 1) {
+      if (next < nitems)
+        plane_tile_describe<N, XP>(t, item_begin, next, g, meta[cur ^ 1]);
+      else
+        meta[cur ^ 1].valid = 0;
+      if (valid) v_sys = meta[cur].sys;
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (valid && tid < meta[cur].np * N) {
+      const int p = tid / N;
+      const int z = tid - p * N;
+      float2 *col = P + p * PP + z;
+      const float *vz = Vs + p * VP + z;
+      float2 v[N];
+      load_column<N, RY>(v, col);
+      reg_fft<N, +1, 0>(v);
+      static_for<0, N>([&](auto mc) {
+        constexpr int mm = decltype(mc)::value;
+        const float w = vz[mm * N];
+        float2 &e = v[line_slot<N>(mm, 1)];
+        e.x *= w;
+        e.y *= w;
+      });
+      reg_fft<N, -1, 1>(v);
+      static_for<0, N>([&](auto mc) {
+        constexpr int mm = decltype(mc)::value;
+        if constexpr (Lay::kept(mm)) col[Lay::row_of(mm) * PZ] = v[line_slot<N>(mm, 2)];
+      });
+    }
+    __syncthreads();   // the next tile's description is visible
+    if (zoff >= 0) {
+      float2 *line = P + zoff;
+      float2 v[N];
+      load_line<N>(v, line, 1);
+      reg_fft<N, -1, 0>(v);
+      static_for<0, N>([&](auto mc) {
+        constexpr int mm = decltype(mc)::value;
+        if constexpr (Lay::kept(mm)) line[mm] = v[line_slot<N>(mm, 1)];
+      });
+    }
+    if (meta[cur ^ 1].valid) {
+      // the next tile's offsets: staged by the threads without a z line
+      // (whole warps past the last z line) while the z transforms run, or by
+      // every thread after its z line when nearly all threads have one
+      const int t0 = zthr < NT - 32 ? (zthr + 31) / 32 * 32 : 0;
+      if (tid >= t0) {
+        short *nco = offs + (cur ^ 1) * (MAXC + MAXR);
+        stage_offsets<N, RY, NT>(t, item_begin, next, meta[cur ^ 1].ncol, meta[cur ^ 1].nrow, nco,
+                                 nco + MAXC, t0);
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      float2 *a0 = abuf + meta[cur].a_base;
+      const long long ld = meta[cur].ld;
+      const int ncol = meta[cur].ncol, np = meta[cur].np;
+#pragma unroll 4
+      for (int c = tid; c < ncol; c += NT) {
+        const int off = coff[c];
+#pragma unroll
+        for (int p = 0; p < XP; ++p)
+          if (p < np) a0[p * ld + c] = P[p * PP + off];
+      }
+    }
+    __syncthreads();   // every scatter read of P done before the next tile zeroes it
+    cur ^= 1;
+  }
 }
 
 // Density of one k-set over XP x-planes: loop over bands, accumulate
@@ -314,23 +446,34 @@ template <int N, int RY, bool DENSITY> struct RowsShape {
   static constexpr size_t SMEM = (size_t)XP * PLANE + 2 * N + 16;
 };
 
-template <int N, int RY, int XP, int MINB>
-static void plane_rows_go_x(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
-                            const float *vloc, cudaStream_t st) {
-  using Lay = RowsLayout<N, RY>;
-  constexpr int NT = (N * XP + 31) / 32 * 32;
-  const size_t smem = (size_t)XP * (Lay::PP * 8 + Lay::VP * 4) + 16;
-  auto kern = k_plane_rows<N, RY, XP, NT, MINB>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  const int ng = (max_n1 + XP - 1) / XP;
-  derek::note_launch(), kern<<<dim3(nitems, ng), NT, smem, st>>>(t, item_begin, abuf, vloc);
+static int sm_count() {
+  static int n = [] {
+    int dev = 0, c = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    return c > 0 ? c : 1;
+  }();
+  return n;
 }
 
 template <int N, int RY>
-static void plane_rows_go(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
-                          const float *vloc, cudaStream_t st) {
-  using Sh = RowsShape<N, RY, false>;
-  plane_rows_go_x<N, RY, Sh::XP, 1>(t, item_begin, nitems, max_n1, abuf, vloc, st);
+static void plane_persist_go(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
+                             const float *vloc, cudaStream_t st) {
+  using Lay = RowsLayout<N, RY>;
+  constexpr size_t OFFS = 2 * (size_t)(Lay::NRW * Lay::NRW + Lay::NRW) * sizeof(short);
+  constexpr int PLANE = Lay::PP * 8 + Lay::VP * 4;
+  constexpr int BYS = (int)((kSmemMax - 256 - OFFS) / PLANE);
+  constexpr int XP0 = BYS < kThreadsMax / N ? BYS : kThreadsMax / N;
+  constexpr int XP = XP0 < 1 ? 1 : XP0;
+  constexpr int NT = (N * XP + 31) / 32 * 32;
+  const size_t smem = (size_t)XP * PLANE + OFFS + 16;
+  auto kern = k_plane_persist<N, RY, XP, NT>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int ng = (max_n1 + XP - 1) / XP;
+  int R = sm_count() / ng;
+  if (R < 1) R = 1;
+  if (R > nitems) R = nitems;
+  derek::note_launch(), kern<<<ng * R, NT, smem, st>>>(t, item_begin, nitems, ng, abuf, vloc);
 }
 
 template <int N, int RY>
@@ -348,9 +491,9 @@ template <int N>
 static void plane_go(const Tables &t, int item_begin, int nitems, int max_n1, int max_yz, float2 *abuf,
                      const float *vloc, cudaStream_t st) {
   if (max_yz <= compact_ry<N>())
-    plane_rows_go<N, compact_ry<N>()>(t, item_begin, nitems, max_n1, abuf, vloc, st);
+    plane_persist_go<N, compact_ry<N>()>(t, item_begin, nitems, max_n1, abuf, vloc, st);
   else
-    plane_rows_go<N, N / 2>(t, item_begin, nitems, max_n1, abuf, vloc, st);
+    plane_persist_go<N, N / 2>(t, item_begin, nitems, max_n1, abuf, vloc, st);
 }
 
 template <int N>

@@ -137,3 +137,32 @@ def test_uneven_batch_scf_matches_single_systems():
         with dg.Handle(s, precision=dg.DEREK_PREC_FP64, density_tol=1e-9, **mix) as h1:
             r1 = h1.electronic_scf(max_scf=300, etol=1e-11)[0]
         assert abs(rb["free_energy"] - r1["free_energy"]) < 1e-9, (rb["free_energy"], r1["free_energy"])
+
+
+def test_mixed_batch_same_grid_matches_single_systems():
+    """Three systems sharing one 24^3 grid (one launch class) but with
+    different cells and wells: the FP32 plane pass keeps each block's V(r)
+    planes in shared memory while consecutive items belong to one system, so
+    a batched mixed-precision SCF must give each system the free energy it
+    gets alone."""
+    import derek_gb300 as dg
+    rng = np.random.default_rng(11)
+    specs = []
+    for i, L in enumerate((6.0, 6.4, 6.8)):
+        c = rng.random((3, 3))
+        wells = np.concatenate([c, rng.uniform(1.0, 3.0, (3, 1)), rng.uniform(0.8, 1.5, (3, 1))], axis=1)
+        # 4 k-points x 10 carried bands per system: 120 items, more than the
+        # blocks per x-group, so blocks walk items of several systems
+        kpts = [[0.0, 0.0, 0.0], [0.25, 0.25, -0.25], [-0.25, 0.25, 0.25], [0.25, -0.25, 0.25]]
+        specs.append(dg.SystemSpec(np.eye(3) * L, 5.0, kpts, 6, 4.0 + 2 * i, kT=0.01, wells=wells,
+                                   n_fine=(24, 24, 24)))
+    # CUDA-core overlaps: the batch and the single runs then follow the same
+    # arithmetic per system; etol sits above the FP32 noise floor (~1e-7 Ha)
+    opts = dict(mix_alpha=0.3, kerker_q0=0.0, density_tol=0.0, use_tensor_cores=0)
+    with dg.Handle(specs, precision=1, **opts) as h:
+        batch = h.electronic_scf(max_scf=100, etol=1e-6)
+    for s, rb in zip(specs, batch):
+        assert rb["converged"], rb
+        with dg.Handle(s, precision=1, **opts) as h1:
+            r1 = h1.electronic_scf(max_scf=100, etol=1e-6)[0]
+        assert abs(rb["free_energy"] - r1["free_energy"]) < 1e-5, (rb["free_energy"], r1["free_energy"])
