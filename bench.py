@@ -125,9 +125,9 @@ class Clocks:
 
 
 # DRAM bytes per (k-point, band) item of one H.psi, summed over k_xinv_reg,
-# k_plane_rows and k_xfwd_reg, from one ncu capture of the 4-k-point case
-# (336 items: 143.1 + 256.6 + 236.0 MB).
-TRAFFIC_PER_ITEM = 635.7e6 / 336
+# k_plane_persist and k_xfwd_reg, from one ncu capture of the 4-k-point case
+# (336 items: 144.7 + 256.8 + 236.5 MB).
+TRAFFIC_PER_ITEM = 638.0e6 / 336
 # nominal FP32 rate of a GB300: 152 SMs x 128 lanes x 2 flops x 2.07 GHz
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
@@ -258,7 +258,7 @@ def run_ours(args):
     peak, src = measured_peaks()
     achieved = nbytes / (t_apply / 1e3) / 1e9
     stage_names = ["k_xinv_reg (scatter + backward x)",
-                   "k_plane_rows (backward z,y + V(r) + forward y,z)",
+                   "k_plane_persist (backward z,y + V(r) + forward y,z)",
                    "k_xfwd_reg (forward x + gather + kinetic + epilogue)"]
     fft_tflops = plane_fft_flops(h, specs) / (stages[1] / 1e3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -271,7 +271,7 @@ def run_ours(args):
                 "stage_ms": {n: round(x, 4) for n, x in zip(stage_names, stages)},
                 "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)",
                 "dominant_kernel": {
-                    "name": "k_plane_rows", "share_of_hpsi": round(stages[1] / sum(stages), 3),
+                    "name": "k_plane_persist", "share_of_hpsi": round(stages[1] / sum(stages), 3),
                     "bound": "fp32 issue", "fft_tflops": round(fft_tflops, 2),
                     "fp32_peak_tflops": round(FP32_NOMINAL_TFLOPS, 1),
                     "fp32_frac": round(fft_tflops / FP32_NOMINAL_TFLOPS, 3),
