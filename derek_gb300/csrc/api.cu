@@ -46,13 +46,13 @@ __global__ void k_to_float(long long n, const double *__restrict__ a, float *__r
 
 template <typename R>
 static void apply_h_class(derek_gpu *h, const Tables &t, int item_begin, int nitems, int nchunk,
-                          const int n[3], int max_yz, const void *in, const void *prev, void *out,
+                          const int n[3], int max_m, const void *in, const void *prev, void *out,
                           const Axpby *coef, const R *vloc) {
-  launch_x_inv<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)in,
+  launch_x_inv<R>(t, item_begin, nitems, nchunk, n[0], n[0], max_m, (const cplx<R> *)in,
                   (cplx<R> *)h->d_abuf, nullptr, h->stream);
-  launch_plane<R>(t, item_begin, nitems, n[0], n[1], n[2], n[1], n[2], max_yz, (cplx<R> *)h->d_abuf,
+  launch_plane<R>(t, item_begin, nitems, n[0], n[1], n[2], n[1], n[2], max_m, (cplx<R> *)h->d_abuf,
                   vloc, h->stream);
-  launch_x_fwd<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)h->d_abuf,
+  launch_x_fwd<R>(t, item_begin, nitems, nchunk, n[0], n[0], max_m, (const cplx<R> *)h->d_abuf,
                   (const cplx<R> *)in, (const cplx<R> *)prev, (cplx<R> *)out, coef, h->stream);
 }
 
@@ -65,14 +65,14 @@ static void apply_h_t(derek_gpu *h, const Tables &base, int item_begin, int nite
     for (const auto &c : h->classes) {
       Tables t = base;
       t.item_list = c.d_list;
-      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, c.max_yz, in, prev, out, coef, vloc);
+      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, c.max_m, in, prev, out, coef, vloc);
     }
     return;
   }
   const KSetDev &K = h->ks[h->item_ks[item_begin]];
   const SysDev &S = h->sys[K.sys];
   apply_h_class<R>(h, base, item_begin, nitems, (K.ncol + kColChunk - 1) / kColChunk, S.n,
-                   h->ks_max_yz[h->item_ks[item_begin]], in, prev, out, coef, vloc);
+                   h->ks_max_m[h->item_ks[item_begin]], in, prev, out, coef, vloc);
 }
 
 int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
@@ -99,11 +99,11 @@ template <typename R> static void density_t(derek_gpu *h, const void *psi) {
   for (const auto &c : h->classes) {
     Tables t = h->tab;
     t.item_list = c.d_list;
-    launch_x_inv<R>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const cplx<R> *)psi,
+    launch_x_inv<R>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const cplx<R> *)psi,
                     (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
   }
   launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
-                          h->min_n[2], h->max_yz_all, (const cplx<R> *)h->d_abuf, h->d_occw,
+                          h->min_n[2], h->max_m_all, (const cplx<R> *)h->d_abuf, h->d_occw,
                           h->d_partial, h->d_partial_off, h->stream);
 }
 
@@ -185,7 +185,7 @@ const char *derek_gpu_last_error(derek_gpu_t *h) {
 int derek_gpu_destroy(derek_gpu_t *h) {
   if (!h) return DEREK_ERR_BAD_ARG;
   void *ptrs[] = {h->d_sys,   h->d_ks,      h->d_item_ks, h->d_item_band, h->d_ent_col,
-                  h->d_col_start, h->d_ent_ix, h->d_col_y, h->d_col_z, h->d_rows,  h->d_kin64,     h->d_kin32,
+                  h->d_col_start, h->d_ent_ix, h->d_col_y, h->d_col_z, h->d_col_x0, h->d_rows,  h->d_kin64,     h->d_kin32,
                   h->d_tw64,  h->d_tw32,    h->d_vext,    h->d_vloc,      h->d_vhxc,
                   h->d_vloc32, h->d_rho_in, h->d_rho_out, h->d_exc,       h->d_vxc,
                   h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
@@ -233,7 +233,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   h->nsys = nsys;
 
   std::vector<int> ent_col, col_start;
-  std::vector<short> ent_ix, col_y, col_z, rows;
+  std::vector<short> ent_ix, col_y, col_z, col_x0, rows;
   std::vector<float> kin32;
   std::vector<double> tw64;
   std::map<int, long long> tw_of;  // n -> offset
@@ -355,7 +355,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       for (int i = 0; i < npw; ++i) cols[{sp.my[i], sp.mz[i]}].push_back(i);
       K.ncol = (int)cols.size();
       K.ncol_pad = (K.ncol + 15) / 16 * 16;
-      int c = 0, e = 0, last_row = -1, max_yz = 0;
+      int c = 0, e = 0, last_row = -1, max_m = 0;
       std::vector<short> krows;
       for (auto &kv : cols) {
         const int iy = ((kv.first.first % nfine[1]) + nfine[1]) % nfine[1];
@@ -363,7 +363,9 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
         col_start.push_back(e);
         col_y.push_back((short)iy);
         col_z.push_back((short)iz);
+        col_x0.push_back((short)sp.mx[kv.second.front()]);
         for (int ref : kv.second) {
+          max_m = std::max(max_m, std::abs(sp.mx[ref]));
           const int ix = ((sp.mx[ref] % nfine[0]) + nfine[0]) % nfine[0];
           ent_col.push_back(c);
           ent_ix.push_back((short)ix);
@@ -372,7 +374,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
           kin32.push_back((float)sp.kinetic[ref]);
           ++e;
         }
-        max_yz = std::max(max_yz, std::max(std::abs(kv.first.first), std::abs(kv.first.second)));
+        max_m = std::max(max_m, std::max(std::abs(kv.first.first), std::abs(kv.first.second)));
         if (kv.first.first != last_row) {
           krows.push_back((short)iy);
           last_row = kv.first.first;
@@ -383,9 +385,10 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       // keep col_y / col_z aligned with col_start (ncol + 1 entries per k-set)
       col_y.push_back(0);
       col_z.push_back(0);
+      col_x0.push_back(0);
       K.nrow = (int)krows.size();
-      h->ks_max_yz.push_back(max_yz);
-      h->max_yz_all = std::max(h->max_yz_all, max_yz);
+      h->ks_max_m.push_back(max_m);
+      h->max_m_all = std::max(h->max_m_all, max_m);
       rows.insert(rows.end(), krows.begin(), krows.end());
       for (int i = 0; i < npw; ++i) {
         const int ix = ((sp.mx[i] % nfine[0]) + nfine[0]) % nfine[0];
@@ -429,6 +432,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   CK(upload(&h->d_col_start, col_start));
   CK(upload(&h->d_col_y, col_y));
   CK(upload(&h->d_col_z, col_z));
+  CK(upload(&h->d_col_x0, col_x0));
   CK(upload(&h->d_rows, rows));
   CK(upload(&h->d_kin64, h->kin_col));
   CK(upload(&h->d_kin32, kin32));
@@ -491,6 +495,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   h->tab.col_start = h->d_col_start;
   h->tab.col_y = h->d_col_y;
   h->tab.col_z = h->d_col_z;
+  h->tab.col_x0 = h->d_col_x0;
   h->tab.kin64 = h->d_kin64;
   h->tab.kin32 = h->d_kin32;
   h->tab.rows = h->d_rows;
@@ -508,14 +513,14 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       const std::array<int, 3> key = {S.n[0], S.n[1], S.n[2]};
       groups[key].push_back(it);
       chunks[key] = std::max(chunks[key], (K.ncol + kColChunk - 1) / kColChunk);
-      mys[key] = std::max(mys[key], h->ks_max_yz[h->item_ks[it]]);
+      mys[key] = std::max(mys[key], h->ks_max_m[h->item_ks[it]]);
     }
     for (auto &g : groups) {
       derek_gpu::ItemClass c{};
       for (int i = 0; i < 3; ++i) c.n[i] = g.first[i];
       c.count = (int)g.second.size();
       c.nchunk = chunks[g.first];
-      c.max_yz = mys[g.first];
+      c.max_m = mys[g.first];
       c.d_list = nullptr;
       if (groups.size() > 1) CK(upload(&c.d_list, g.second));
       h->classes.push_back(c);
@@ -769,10 +774,10 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       Tables t = h->tab;
       t.item_list = c.d_list;
       if (h->prec == DEREK_PREC_FP64)
-        launch_x_inv<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const double2 *)in,
+        launch_x_inv<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const double2 *)in,
                              (double2 *)h->d_abuf, nullptr, h->stream);
       else
-        launch_x_inv<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const float2 *)in,
+        launch_x_inv<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const float2 *)in,
                             (float2 *)h->d_abuf, nullptr, h->stream);
     }
     cudaEventRecord(ev[1], h->stream);
@@ -780,10 +785,10 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       Tables t = h->tab;
       t.item_list = c.d_list;
       if (h->prec == DEREK_PREC_FP64)
-        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_yz,
+        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_m,
                              (double2 *)h->d_abuf, h->d_vloc, h->stream);
       else
-        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_yz,
+        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_m,
                             (float2 *)h->d_abuf, h->d_vloc32, h->stream);
     }
     cudaEventRecord(ev[2], h->stream);
@@ -791,10 +796,10 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       Tables t = h->tab;
       t.item_list = c.d_list;
       if (h->prec == DEREK_PREC_FP64)
-        launch_x_fwd<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const double2 *)h->d_abuf,
+        launch_x_fwd<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const double2 *)h->d_abuf,
                              (const double2 *)in, nullptr, (double2 *)h->d_HX, nullptr, h->stream);
       else
-        launch_x_fwd<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const float2 *)h->d_abuf,
+        launch_x_fwd<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const float2 *)h->d_abuf,
                             (const float2 *)in, nullptr, (float2 *)h->d_HX, nullptr, h->stream);
     }
     cudaEventRecord(ev[3], h->stream);

@@ -41,7 +41,7 @@ struct derek_gpu {
   derek::KSetDev *d_ks = nullptr;
   int *d_item_ks = nullptr, *d_item_band = nullptr;
   int *d_ent_col = nullptr, *d_col_start = nullptr;
-  short *d_ent_ix = nullptr, *d_col_y = nullptr, *d_col_z = nullptr, *d_rows = nullptr;
+  short *d_ent_ix = nullptr, *d_col_y = nullptr, *d_col_z = nullptr, *d_col_x0 = nullptr, *d_rows = nullptr;
   double *d_kin64 = nullptr;
   float *d_kin32 = nullptr;
   double2 *d_tw64 = nullptr;
@@ -97,12 +97,12 @@ struct derek_gpu {
     int n[3];
     int count;
     int nchunk;
-    int max_yz;    // largest |centred Miller y or z| of a sphere column in the class
+    int max_m;     // largest |centred Miller index| (x, y or z) of a sphere entry in the class
     int *d_list;   // nullptr when the class is the contiguous range of all items
   };
   std::vector<ItemClass> classes;
-  std::vector<int> ks_max_yz;   // per k-set: largest |centred Miller y or z| of its columns
-  int max_yz_all = 0;
+  std::vector<int> ks_max_m;    // per k-set: largest |centred Miller index| of its sphere
+  int max_m_all = 0;
 
   cudaStream_t stream = nullptr;
   std::string last_error;

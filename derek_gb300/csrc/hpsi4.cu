@@ -431,12 +431,12 @@ static void x_inv_go(const Tables &t, int item_begin, int nitems, int max_nchunk
 // compile-time x length when every item has the same n1 in {32, 36, 48, 54, 64, 72}
 template <typename R>
 void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
+                  int min_n1, int max_m, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
                   cudaStream_t st) {
   if (nitems <= 0) return;
   if constexpr (std::is_same<R, float>::value) {
     if (max_n1 == min_n1 &&
-        launch_xinv_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, psi, abuf, occ_skip, st))
+        launch_xinv_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, max_m, psi, abuf, occ_skip, st))
       return;
   }
   const int n = max_n1 == min_n1 ? max_n1 : 0;
@@ -460,12 +460,12 @@ static void x_fwd_go(const Tables &t, int item_begin, int nitems, int max_nchunk
 
 template <typename R>
 void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  int min_n1, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
+                  int min_n1, int max_m, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
                   cplx<R> *out, const Axpby *coef, cudaStream_t st) {
   if (nitems <= 0) return;
   if constexpr (std::is_same<R, float>::value) {
     if (max_n1 == min_n1 &&
-        launch_xfwd_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, abuf, psi, prev, out, coef, st))
+        launch_xfwd_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, max_m, abuf, psi, prev, out, coef, st))
       return;
   }
   const int n = max_n1 == min_n1 ? max_n1 : 0;
@@ -492,11 +492,11 @@ static bool try_plane_fixed(const Tables &t, int item_begin, int nitems, int max
 
 template <typename R>
 void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2, int max_n3,
-                  int min_n2, int min_n3, int max_yz, cplx<R> *abuf, const R *vloc, cudaStream_t st) {
+                  int min_n2, int min_n3, int max_m, cplx<R> *abuf, const R *vloc, cudaStream_t st) {
   if (nitems <= 0) return;
   if constexpr (std::is_same<R, float>::value) {
     if (max_n2 == max_n3 && min_n2 == max_n2 && min_n3 == max_n3 &&
-        launch_plane_reg(t, item_begin, nitems, max_n1, max_n2, max_yz, abuf, vloc, st))
+        launch_plane_reg(t, item_begin, nitems, max_n1, max_n2, max_m, abuf, vloc, st))
       return;
   }
   if (try_plane_fixed<R, 72>(t, item_begin, nitems, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, vloc, st) ||
@@ -527,12 +527,12 @@ static bool try_density_fixed(const Tables &t, int ks_begin, int nks, int max_n1
 
 template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
-                          int min_n2, int min_n3, int max_yz, const cplx<R> *abuf, const double *occ,
+                          int min_n2, int min_n3, int max_m, const cplx<R> *abuf, const double *occ,
                           double *partial, const long long *partial_off, cudaStream_t st) {
   if (nks <= 0) return;
   if constexpr (std::is_same<R, float>::value) {
     if (max_n2 == max_n3 && min_n2 == max_n2 && min_n3 == max_n3 &&
-        launch_density_reg(t, ks_begin, nks, max_n1, max_n2, max_yz, abuf, occ, partial, partial_off, st))
+        launch_density_reg(t, ks_begin, nks, max_n1, max_n2, max_m, abuf, occ, partial, partial_off, st))
       return;
   }
   if (try_density_fixed<R, 72>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
@@ -548,11 +548,11 @@ void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, in
 }
 
 #define DEREK_INST(R)                                                                             \
-  template void launch_x_inv<R>(const Tables &, int, int, int, int, int, const cplx<R> *,        \
+  template void launch_x_inv<R>(const Tables &, int, int, int, int, int, int, const cplx<R> *,   \
                                 cplx<R> *, const double *, cudaStream_t);                         \
   template void launch_plane<R>(const Tables &, int, int, int, int, int, int, int, int, cplx<R> *, \
                                 const R *, cudaStream_t);                                         \
-  template void launch_x_fwd<R>(const Tables &, int, int, int, int, int, const cplx<R> *,        \
+  template void launch_x_fwd<R>(const Tables &, int, int, int, int, int, int, const cplx<R> *,   \
                                 const cplx<R> *, const cplx<R> *, cplx<R> *, const Axpby *,      \
                                 cudaStream_t);                                                    \
   template void launch_density_plane<R>(const Tables &, int, int, int, int, int, int, int, int,   \

@@ -488,50 +488,50 @@ static void density_rows_go(const Tables &t, int ks_begin, int nks, int max_n1, 
 }
 
 template <int N>
-static void plane_go(const Tables &t, int item_begin, int nitems, int max_n1, int max_yz, float2 *abuf,
+static void plane_go(const Tables &t, int item_begin, int nitems, int max_n1, int max_m, float2 *abuf,
                      const float *vloc, cudaStream_t st) {
-  if (max_yz <= compact_ry<N>())
+  if (max_m <= compact_ry<N>())
     plane_persist_go<N, compact_ry<N>()>(t, item_begin, nitems, max_n1, abuf, vloc, st);
   else
     plane_persist_go<N, N / 2>(t, item_begin, nitems, max_n1, abuf, vloc, st);
 }
 
 template <int N>
-static void density_go(const Tables &t, int ks_begin, int nks, int max_n1, int max_yz, const float2 *abuf,
+static void density_go(const Tables &t, int ks_begin, int nks, int max_n1, int max_m, const float2 *abuf,
                        const double *occ, double *partial, const long long *partial_off, cudaStream_t st) {
-  if (max_yz <= compact_ry<N>())
+  if (max_m <= compact_ry<N>())
     density_rows_go<N, compact_ry<N>()>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
   else
     density_rows_go<N, N / 2>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
 }
 
-bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_yz,
+bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_m,
                       float2 *abuf, const float *vloc, cudaStream_t st) {
   switch (n) {
-    case 72: plane_go<72>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
-    case 64: plane_go<64>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
-    case 54: plane_go<54>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
-    case 48: plane_go<48>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
-    case 36: plane_go<36>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
-    case 32: plane_go<32>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
-    case 27: plane_go<27>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
-    case 24: plane_go<24>(t, item_begin, nitems, max_n1, max_yz, abuf, vloc, st); return true;
+    case 72: plane_go<72>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
+    case 64: plane_go<64>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
+    case 54: plane_go<54>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
+    case 48: plane_go<48>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
+    case 36: plane_go<36>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
+    case 32: plane_go<32>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
+    case 27: plane_go<27>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
+    case 24: plane_go<24>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
     default: return false;
   }
 }
 
-bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_yz,
+bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_m,
                         const float2 *abuf, const double *occ, double *partial,
                         const long long *partial_off, cudaStream_t st) {
   switch (n) {
-    case 72: density_go<72>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
-    case 64: density_go<64>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
-    case 54: density_go<54>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
-    case 48: density_go<48>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
-    case 36: density_go<36>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
-    case 32: density_go<32>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
-    case 27: density_go<27>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
-    case 24: density_go<24>(t, ks_begin, nks, max_n1, max_yz, abuf, occ, partial, partial_off, st); return true;
+    case 72: density_go<72>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
+    case 64: density_go<64>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
+    case 54: density_go<54>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
+    case 48: density_go<48>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
+    case 36: density_go<36>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
+    case 32: density_go<32>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
+    case 27: density_go<27>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
+    case 24: density_go<24>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
     default: return false;
   }
 }

@@ -18,6 +18,7 @@ struct Tables {
   const int *col_start;   // per column: first entry (local), ncol + 1 per k-set
   const short *col_y;     // per column: FFT indices along y and z
   const short *col_z;
+  const short *col_x0;    // per column: centred Miller x of its first entry
   const short *rows;      // per k-set: the y rows holding columns
   const double2 *tw64;    // twiddle tables exp(-2 pi i t/n)
   const float2 *tw32;
@@ -43,35 +44,35 @@ struct Axpby {
 // Launch geometry: items [item_begin, item_begin + nitems) of the batch.
 template <typename R>
 void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
+                  int min_n1, int max_m, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
                   cudaStream_t st);
 // (y,z)-plane pass; a compile-time kernel is used when every system has
 // n2 = n3 = N for N in {32, 36, 48, 54, 64, 72}
-// max_yz: largest |centred Miller y or z| of a sphere column among the items
+// max_m: largest |centred Miller index| (x, y or z) of a sphere entry among the items
 template <typename R>
 void launch_plane(const Tables &t, int item_begin, int nitems, int max_n1, int max_n2, int max_n3,
-                  int min_n2, int min_n3, int max_yz, cplx<R> *abuf, const R *vloc, cudaStream_t st);
+                  int min_n2, int min_n3, int max_m, cplx<R> *abuf, const R *vloc, cudaStream_t st);
 template <typename R>
 void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
-                  int min_n1, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
+                  int min_n1, int max_m, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
                   cplx<R> *out, const Axpby *coef, cudaStream_t st);
 template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
-                          int min_n2, int min_n3, int max_yz, const cplx<R> *abuf, const double *occ,
+                          int min_n2, int min_n3, int max_m, const cplx<R> *abuf, const double *occ,
                           double *partial, const long long *partial_off, cudaStream_t st);
 constexpr int kColChunk = 64;   // columns per x-line chunk (kCC in hpsi4.cu)
 
 // FP32 (y,z)-plane passes with register-resident line transforms
 // (hpsi_reg.cu), for cubic-plane lengths n in {24, 27, 32, 36, 48, 54, 64, 72};
 // they return false for any other n.
-bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_yz,
+bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_m,
                       float2 *abuf, const float *vloc, cudaStream_t st);
-bool launch_xinv_reg(const Tables &t, int item_begin, int nitems, int max_ncol, int n, const float2 *psi,
-                     float2 *abuf, const double *occ_skip, cudaStream_t st);
-bool launch_xfwd_reg(const Tables &t, int item_begin, int nitems, int max_ncol, int n, const float2 *abuf,
-                     const float2 *psi, const float2 *prev, float2 *out, const Axpby *coef,
-                     cudaStream_t st);
-bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_yz,
+bool launch_xinv_reg(const Tables &t, int item_begin, int nitems, int max_ncol, int n, int max_m,
+                     const float2 *psi, float2 *abuf, const double *occ_skip, cudaStream_t st);
+bool launch_xfwd_reg(const Tables &t, int item_begin, int nitems, int max_ncol, int n, int max_m,
+                     const float2 *abuf, const float2 *psi, const float2 *prev, float2 *out,
+                     const Axpby *coef, cudaStream_t st);
+bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_m,
                         const float2 *abuf, const double *occ, double *partial,
                         const long long *partial_off, cudaStream_t st);
 

@@ -115,16 +115,16 @@ REG_LENGTHS = [24, 27, 32, 36, 48, 54, 64, 72]
 
 
 def reg_plane_pair(oracle, n, rows, kpts, nb, seed):
-    """Cubic cell on an n^3 grid whose sphere reaches max(|my|, |mz|) = N/4 + 1
-    ("compact": the FP32 plane kernels keep only those y rows and z
-    positions) or N/4 + 3 ("all": every row kept)."""
+    """Cubic cell on an n^3 grid whose sphere reaches max(|mx|, |my|, |mz|) =
+    N/4 + 1 ("compact": the FP32 kernels keep only those x, y and z line
+    positions) or N/4 + 3 ("all": every position kept)."""
     L = 8.0
     rmax = n // 4 + 1 if rows == "compact" else n // 4 + 3
     rho = rmax + 0.25   # Miller radius; k_y = 0.2 puts the extreme rows at +-rmax
     ecut = 0.5 * (rho * 2 * np.pi / L) ** 2
     s, spec = make_pair(oracle, L=L, ecut=ecut, nb=nb, kpts=kpts, seed=seed, n_fine=(n, n, n))
-    myz = np.concatenate([oracle.KBasis(s, ik).miller[:, 1:] for ik in range(len(kpts))])
-    assert int(np.abs(myz).max()) == rmax
+    mil = np.concatenate([oracle.KBasis(s, ik).miller for ik in range(len(kpts))])
+    assert int(np.abs(mil).max()) == rmax
     return s, spec
 
 
