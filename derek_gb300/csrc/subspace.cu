@@ -9,6 +9,8 @@
 
 #include "subspace.cuh"
 
+#include <cooperative_groups.h>
+
 namespace derek {
 
 // ---------------------------------------------------------------------------
@@ -475,6 +477,216 @@ __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
 }
 
 // ---------------------------------------------------------------------------
+// The same Jacobi eigensolver on a cluster of two CTAs per k-set, so the FP64
+// work of a round is split over two SMs.  Each CTA keeps a full copy of A and
+// computes every rotation (the two copies are equal, so both take the same
+// decisions); it updates half of the 2x2 blocks of a round and writes each
+// result into its own A and, through distributed shared memory, into its
+// partner's, then updates its half of the eigenvector rows.  One cluster
+// barrier per round makes the partner's writes visible before the next
+// round reads A.
+// ---------------------------------------------------------------------------
+template <typename VT>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
+    k_jacobi_pair(const Tables t, int ks_begin, const double2 *__restrict__ Hs,
+                  double2 *__restrict__ Cout, const long long *__restrict__ mat_off,
+                  double *__restrict__ eig, int max_sweeps, double tol, int *__restrict__ sweeps_out) {
+  using V2 = cplx<VT>;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int crank = (int)cluster.block_rank();
+  const int ksi = ks_begin + blockIdx.x / 2;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;   // both CTAs of the cluster leave together
+  const int n = K.nb;
+  const int ne = n + (n & 1);
+  const int np = ne / 2;
+  const int nblk = np * (np + 1) / 2;
+  const int hv = (n + 1) / 2;                  // eigenvector rows per CTA
+  const int r0 = crank * hv, r1 = min(n, r0 + hv);
+  unsigned char *sp = smem_raw;
+  double2 *A = reinterpret_cast<double2 *>(sp);
+  sp += (size_t)n * n * sizeof(double2);
+  V2 *Vt = reinterpret_cast<V2 *>(sp);          // [n][hv]: eigenvector i, rows r0..r1
+  sp += ((size_t)n * hv * sizeof(V2) + 15) / 16 * 16;
+  double2 *rph = reinterpret_cast<double2 *>(sp);
+  double *rc = reinterpret_cast<double *>(rph + np);
+  double *rs = rc + np;
+  int *pp = reinterpret_cast<int *>(rs + np);
+  int *pq = pp + np;
+  int *act = pq + np;
+  short2 *blk = reinterpret_cast<short2 *>(act + np);
+  __shared__ double red[256];
+  __shared__ double red2[256];
+  double2 *Ap = cluster.map_shared_rank(A, crank ^ 1);   // the partner's copy of A
+  const double2 *Hb = Hs + mat_off[ksi];
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = Hb[e];
+  for (int e = threadIdx.x; e < n * hv; e += blockDim.x) {
+    const int i = e / hv, r = r0 + e % hv;
+    V2 one;
+    one.x = (VT)(i == r ? 1 : 0);
+    one.y = (VT)0;
+    Vt[e] = one;
+  }
+  for (int w = threadIdx.x; w < nblk; w += blockDim.x) {
+    int a = 0, rem = w;
+    while (rem >= np - a) {
+      rem -= np - a;
+      ++a;
+    }
+    blk[w] = make_short2((short)a, (short)(a + rem));
+  }
+  cluster.sync();   // both CTAs running and initialised before any remote write
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    double off = 0, tot = 0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const double m2 = A[e].x * A[e].x + A[e].y * A[e].y;
+      tot += m2;
+      if (e / n != e % n) off += m2;
+    }
+    red[threadIdx.x] = off;
+    red2[threadIdx.x] = tot;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        red[threadIdx.x] += red[threadIdx.x + s];
+        red2[threadIdx.x] += red2[threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    const bool done = red[0] <= tol * tol * red2[0];
+    const double skip = tol * sqrt(red2[0]) / (4.0 * n);
+    __syncthreads();
+    if (done) break;
+    for (int round = 0; round < ne - 1; ++round) {
+      for (int k = threadIdx.x; k < np; k += blockDim.x) {
+        int p, q;
+        rr_pair(k, round, ne, p, q);
+        pp[k] = p;
+        pq[k] = q;
+        double c = 1.0, s = 0.0;
+        double2 ph = make_double2(1.0, 0.0);
+        int on = 0;
+        if (q < n) {
+          const double a = A[p * n + p].x, d = A[q * n + q].x;
+          const double2 b = A[p * n + q];
+          const double e = hypot(b.x, b.y);
+          if (e > skip) {
+            ph = make_double2(b.x / e, b.y / e);
+            const double tau = (d - a) / (2.0 * e);
+            const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + tt * tt);
+            s = tt * c;
+            on = 1;
+          }
+        }
+        rc[k] = c;
+        rs[k] = s;
+        rph[k] = ph;
+        act[k] = on;
+      }
+      __syncthreads();
+      for (int w = crank + 2 * (int)threadIdx.x; w < nblk; w += 2 * blockDim.x) {
+        const short2 ab = blk[w];
+        const int ia = ab.x, ib = ab.y;
+        const int on_a = act[ia], on_b = act[ib];
+        if (!on_a && !on_b) continue;
+        const int pa = pp[ia], qa = pq[ia], pb = pp[ib], qb = pq[ib];
+        const bool qa_ok = qa < n, qb_ok = qb < n;
+        const double2 z = make_double2(0.0, 0.0);
+        double2 x00 = A[pa * n + pb];
+        double2 x01 = qb_ok ? A[pa * n + qb] : z;
+        double2 x10 = qa_ok ? A[qa * n + pb] : z;
+        double2 x11 = (qa_ok && qb_ok) ? A[qa * n + qb] : z;
+        if (on_a) {
+          const double c = rc[ia], s = rs[ia];
+          const double2 ph = rph[ia];
+          const double2 t0 = zmul(ph, x10), t1 = zmul(ph, x11);
+          const double2 n00 = make_double2(c * x00.x - s * t0.x, c * x00.y - s * t0.y);
+          const double2 n01 = make_double2(c * x01.x - s * t1.x, c * x01.y - s * t1.y);
+          x10 = make_double2(s * x00.x + c * t0.x, s * x00.y + c * t0.y);
+          x11 = make_double2(s * x01.x + c * t1.x, s * x01.y + c * t1.y);
+          x00 = n00;
+          x01 = n01;
+        }
+        if (on_b) {
+          const double c = rc[ib], s = rs[ib];
+          const double2 phc = make_double2(rph[ib].x, -rph[ib].y);
+          const double2 t0 = zmul(phc, x01), t1 = zmul(phc, x11);
+          const double2 n00 = make_double2(c * x00.x - s * t0.x, c * x00.y - s * t0.y);
+          const double2 n10 = make_double2(c * x10.x - s * t1.x, c * x10.y - s * t1.y);
+          x01 = make_double2(s * x00.x + c * t0.x, s * x00.y + c * t0.y);
+          x11 = make_double2(s * x10.x + c * t1.x, s * x10.y + c * t1.y);
+          x00 = n00;
+          x10 = n10;
+        }
+        // each entry goes to both copies of A
+        auto put = [&](int idx, double2 v) {
+          A[idx] = v;
+          Ap[idx] = v;
+        };
+        if (ia == ib) {
+          put(pa * n + pa, make_double2(x00.x, 0.0));
+          put(qa * n + qa, make_double2(x11.x, 0.0));
+          put(pa * n + qa, z);
+          put(qa * n + pa, z);
+          continue;
+        }
+        put(pa * n + pb, x00);
+        put(pb * n + pa, make_double2(x00.x, -x00.y));
+        if (qb_ok) {
+          put(pa * n + qb, x01);
+          put(qb * n + pa, make_double2(x01.x, -x01.y));
+        }
+        if (qa_ok) {
+          put(qa * n + pb, x10);
+          put(pb * n + qa, make_double2(x10.x, -x10.y));
+        }
+        if (qa_ok && qb_ok) {
+          put(qa * n + qb, x11);
+          put(qb * n + qa, make_double2(x11.x, -x11.y));
+        }
+      }
+      // eigenvector rows r0..r1 of this CTA
+      const int nr = r1 - r0;
+      for (int w = threadIdx.x; w < np * nr; w += blockDim.x) {
+        const int k = w / nr, row = w - (w / nr) * nr;
+        if (!act[k]) continue;
+        const VT c = (VT)rc[k], s = (VT)rs[k];
+        const VT phx = (VT)rph[k].x, phy = (VT)-rph[k].y;
+        V2 &xp = Vt[pp[k] * hv + row];
+        V2 &xq = Vt[pq[k] * hv + row];
+        const V2 a = xp, b = xq;
+        const VT tx = phx * b.x - phy * b.y, ty = phx * b.y + phy * b.x;
+        xp.x = c * a.x - s * tx;
+        xp.y = c * a.y - s * ty;
+        xq.x = s * a.x + c * tx;
+        xq.y = s * a.y + c * ty;
+      }
+      cluster.sync();   // both halves of the round written into both copies of A
+    }
+  }
+  if (threadIdx.x == 0 && crank == 0 && sweeps_out) sweeps_out[ksi] = sweep;
+  double *ev = rc;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) ev[i] = A[i * n + i].x;
+  __syncthreads();
+  double2 *Cb = Cout + mat_off[ksi];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double vi = ev[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) rank += (ev[j] < vi) || (ev[j] == vi && j < i);
+    if (crank == 0) eig[K.item0 + rank] = vi;
+    for (int r = r0; r < r1; ++r) {
+      const V2 v = Vt[i * hv + (r - r0)];
+      Cb[r * n + rank] = make_double2((double)v.x, (double)v.y);
+    }
+  }
+  cluster.sync();   // neither CTA leaves while its partner could still address it
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 template <typename R>
@@ -533,6 +745,22 @@ void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const dou
   const int a_smem = nn * sizeof(double2) + tab <= kJacobiSmem;
   const int v_smem = a_smem && nn * sizeof(double2) + vbytes + tab <= kJacobiSmem;
   const size_t sm = (a_smem ? nn * sizeof(double2) : 0) + (v_smem ? vbytes : 0) + tab;
+  // two CTAs per k-set when A and half of the eigenvector rows fit
+  const size_t hv = (size_t)(max_nb + 1) / 2;
+  const size_t vhalf = ((size_t)max_nb * hv * (fp32_vectors ? sizeof(float2) : sizeof(double2)) + 15) / 16 * 16;
+  const size_t sm_pair = nn * sizeof(double2) + vhalf + tab;
+  if (sm_pair <= kJacobiSmem) {
+    if (fp32_vectors) {
+      cudaFuncSetAttribute(k_jacobi_pair<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pair);
+      derek::note_launch(), k_jacobi_pair<float><<<2 * nks, 256, sm_pair, st>>>(t, ks_begin, Hs, C, mat_off, eig,
+                                                                             max_sweeps, tol, sweeps_out);
+    } else {
+      cudaFuncSetAttribute(k_jacobi_pair<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pair);
+      derek::note_launch(), k_jacobi_pair<double><<<2 * nks, 256, sm_pair, st>>>(t, ks_begin, Hs, C, mat_off, eig,
+                                                                              max_sweeps, tol, sweeps_out);
+    }
+    return;
+  }
   if (fp32_vectors) {
     cudaFuncSetAttribute(k_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     derek::note_launch(), k_jacobi<float><<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps,
