@@ -187,6 +187,10 @@ __device__ __forceinline__ void stage_offsets(const Tables &t, int item_begin, i
   for (int l = tid; l < nrow; l += nthr) roff[l] = (short)(Lay::row_of(rows[l]) * Lay::PZ);
 }
 
+// values (columns x planes) per idle thread the persistent plane pass
+// prefetches for the next tile
+constexpr int kPrefetchValues = 32;
+
 template <int N, int RY, int XP, int NT>
 __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begin, int nitems, int ng,
                                                          float2 *__restrict__ abuf,
@@ -213,6 +217,12 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
   if (meta[0].valid)
     stage_offsets<N, RY, NT>(t, item_begin, it, meta[0].ncol, meta[0].nrow, offs, offs + MAXC, 0);
   int cur = 0;
+  // columns of the next tile loaded into registers by the threads idle in
+  // the forward z transforms: thread tid >= pf_t0 holds columns
+  // (tid - pf_t0) + j * (NT - pf_t0), j < kPrefetchCols, for every plane
+  constexpr int PFC = kPrefetchValues / XP > 0 ? kPrefetchValues / XP : 1;
+  float2 pf[PFC][XP];
+  int pf_t0 = -1;   // -1: this tile's columns were not prefetched
   for (; it < nitems; it += R) {
     const int valid = meta[cur].valid;
     const short *coff = offs + cur * (MAXC + MAXR);
@@ -236,17 +246,39 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
         }
         cp_async_commit();
       }
-      float2 *a0 = abuf + meta[cur].a_base;
-      const long long ld = meta[cur].ld;
       const int ncol = meta[cur].ncol;
-#pragma unroll 4
-      for (int c = tid; c < ncol; c += NT) {
-        const int off = coff[c];
+      if (pf_t0 >= 0) {
+        if (tid >= pf_t0) {
+          const int nthr = NT - pf_t0;
 #pragma unroll
-        for (int p = 0; p < XP; ++p)
-          if (p < np) P[p * PP + off] = a0[p * ld + c];
+          for (int j = 0; j < PFC; ++j) {
+            const int c = tid - pf_t0 + j * nthr;
+            if (c < ncol) {
+              const int off = coff[c];
+#pragma unroll
+              for (int p = 0; p < XP; ++p)
+                if (p < np) P[p * PP + off] = pf[j][p];
+            }
+          }
+        }
+      } else {
+        float2 *a0 = abuf + meta[cur].a_base;
+        const long long ld = meta[cur].ld;
+#pragma unroll 4
+        for (int c = tid; c < ncol; c += NT) {
+          const int off = coff[c];
+#pragma unroll
+          for (int p = 0; p < XP; ++p)
+            if (p < np) P[p * PP + off] = a0[p * ld + c];
+        }
       }
     }
+    // the prefetched values are consumed: end their live range before the
+    // transforms (they are reloaded after the forward z transforms)
+#pragma unroll
+    for (int j = 0; j < PFC; ++j)
+#pragma unroll
+      for (int p = 0; p < XP; ++p) pf[j][p] = make_float2(0.f, 0.f);
     __syncthreads();
     int zoff = -1, zthr = 0;
     if (valid) {
@@ -321,6 +353,28 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
         short *nco = offs + (cur ^ 1) * (MAXC + MAXR);
         stage_offsets<N, RY, NT>(t, item_begin, next, meta[cur ^ 1].ncol, meta[cur ^ 1].nrow, nco,
                                  nco + MAXC, t0);
+      }
+    }
+    // the next tile's columns into registers (threads past the z lines, when
+    // they can hold all of them)
+    pf_t0 = -1;
+    {
+      const int t0 = zthr < NT - 32 ? (zthr + 31) / 32 * 32 : 0;
+      if (t0 > 0 && meta[cur ^ 1].valid && meta[cur ^ 1].ncol <= PFC * (NT - t0)) {
+        pf_t0 = t0;
+        if (tid >= t0) {
+          const int nthr = NT - t0;
+          const float2 *a0n = abuf + meta[cur ^ 1].a_base;
+          const long long ldn = meta[cur ^ 1].ld;
+          const int ncn = meta[cur ^ 1].ncol, npn = meta[cur ^ 1].np;
+#pragma unroll
+          for (int j = 0; j < PFC; ++j) {
+            const int c = tid - t0 + j * nthr;
+#pragma unroll
+            for (int p = 0; p < XP; ++p)
+              pf[j][p] = (c < ncn && p < npn) ? a0n[p * ldn + c] : make_float2(0.f, 0.f);
+          }
+        }
       }
     }
     __syncthreads();
