@@ -70,6 +70,7 @@ struct derek_gpu {
   double2 *d_opart = nullptr;                  // overlap split-K partials
   long long *d_mat_off = nullptr, *d_opart_off = nullptr, *d_hist_off = nullptr;
   int *d_status = nullptr, *d_sweeps = nullptr;
+  unsigned char *d_rot_img = nullptr;   // tensor-core rotation operands (mixed path)
   derek::Axpby *d_coef_all = nullptr;
   int max_degree = 0;
   double *d_nin_hist = nullptr, *d_res_hist = nullptr;

@@ -49,7 +49,7 @@ int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int he
 int rotate_all(derek_gpu *h, void *X, const double2 *C) {
   if (use_tc(h) && h->opts.use_tensor_cores >= 2)
     launch_rotate_tc(h->tab, 0, h->nks, h->max_nb, h->max_npw, (float2 *)X, C, h->d_mat_off,
-                     h->d_status, h->stream);
+                     h->d_rot_img, h->d_status, h->stream);
   else if (h->prec == DEREK_PREC_FP64)
     launch_rotate<double>(h->tab, 0, h->nks, h->max_nb, h->max_npw, (double2 *)X, C, h->d_mat_off,
                           h->stream);
@@ -278,6 +278,7 @@ extern "C" int derek_scf_alloc(derek_gpu_t *h) {
   A(dalloc(&h->d_hist_off, hist_off.size()));
   A(dalloc(&h->d_status, h->nks));
   A(dalloc(&h->d_sweeps, h->nks));
+  if (use_tc(h)) A(dalloc(&h->d_rot_img, h->nks * rotate_tc_image_bytes(h->max_nb)));
   A(dalloc(&h->d_coef_all, (size_t)h->max_degree * h->nks));
   A(dalloc(&h->d_nin_hist, hoff));
   A(dalloc(&h->d_res_hist, hoff));
@@ -301,7 +302,7 @@ extern "C" void derek_scf_free(derek_gpu_t *h) {
   void *ptrs[] = {h->d_state,  h->d_S,      h->d_Hs,       h->d_C,        h->d_scratch,
                   h->d_opart,  h->d_mat_off, h->d_opart_off, h->d_hist_off, h->d_status,
                   h->d_sweeps, h->d_coef_all, h->d_nin_hist, h->d_res_hist, h->d_epart,
-                  h->d_gpart};
+                  h->d_gpart,  h->d_rot_img};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }

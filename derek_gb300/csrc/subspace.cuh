@@ -23,8 +23,12 @@ void launch_overlap_tc(const Tables &t, int ks_begin, int nks, int max_nb, int m
                        double2 *out, const long long *mat_off, int hermitize, int *status,
                        cudaStream_t st);
 // split-BF16 tcgen05 rotation X <- X C (complex64, nb <= 128), in place
+// img: rotate_tc_image_bytes(max_nb) bytes per k-set of scratch for the
+// converted B operand
+size_t rotate_tc_image_bytes(int max_nb);
 void launch_rotate_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, float2 *X,
-                      const double2 *C, const long long *mat_off, int *status, cudaStream_t st);
+                      const double2 *C, const long long *mat_off, unsigned char *img, int *status,
+                      cudaStream_t st);
 template <typename R>
 void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, cplx<R> *X,
                    const double2 *C, const long long *mat_off, cudaStream_t st);

@@ -321,9 +321,63 @@ void launch_overlap_tc(const Tables &t, int ks_begin, int nks, int max_nb, int m
 // ---------------------------------------------------------------------------
 namespace derek {
 
+namespace {
+__device__ __forceinline__ void cp_async16_tc(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+}  // namespace
+
+// bytes of one k-set's B operand image: per K block, bf16 hi then lo of M's
+// N rows in the core-matrix layout (2 x N x 64 x 2 bytes)
+size_t rotate_tc_image_bytes(int max_nb) {
+  const int N = ((2 * max_nb + 15) / 16) * 16;
+  const int nkb = (2 * max_nb + TC_KB - 1) / TC_KB;
+  return (size_t)nkb * 4 * N * TC_KB;
+}
+
+// The rotation's B operand (M built from the FP64 C) for every k-set,
+// converted once here instead of in every 128-G tile of the rotation.
+__global__ void __launch_bounds__(256) k_rotate_operand(const Tables t, int ks_begin, const double2 *__restrict__ C,
+                                                        const long long *__restrict__ mat_off,
+                                                        unsigned char *__restrict__ img, long long stride) {
+  const int ksi = ks_begin + blockIdx.y;
+  const KSetDev &K = t.ks[ksi];
+  if (!t.sys[K.sys].active) return;
+  const int nb = K.nb;
+  const int N = ((2 * nb + 15) / 16) * 16;
+  const int nkb = (2 * nb + TC_KB - 1) / TC_KB;
+  const double2 *Cb = C + mat_off[ksi];
+  unsigned char *base = img + (long long)blockIdx.y * stride;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nkb * N * 8; c += gridDim.x * blockDim.x) {
+    const int kb = c / (N * 8), rem = c - kb * (N * 8);
+    const int row = rem >> 3, k8 = rem & 7;
+    const int j = row >> 1, part = row & 1;
+    const int ib = kb * (TC_KB / 2);
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = ib + 4 * k8 + q;
+      double2 cij = make_double2(0.0, 0.0);
+      if (row < 2 * nb && i < nb) cij = Cb[(long long)i * nb + j];
+      if (part == 0) {
+        v[2 * q] = (float)cij.x;
+        v[2 * q + 1] = (float)(-cij.y);
+      } else {
+        v[2 * q] = (float)cij.y;
+        v[2 * q + 1] = (float)cij.x;
+      }
+    }
+    uint4 hi, lo;
+    split8(v, hi, lo);
+    unsigned char *blk = base + (size_t)kb * 4 * N * TC_KB;
+    *reinterpret_cast<uint4 *>(blk + core_off(row, k8)) = hi;
+    *reinterpret_cast<uint4 *>(blk + (size_t)2 * N * TC_KB + core_off(row, k8)) = lo;
+  }
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_rotate_tc(const Tables t, int ks_begin, float2 *__restrict__ X, const double2 *__restrict__ C,
-                const long long *__restrict__ mat_off, int *__restrict__ status) {
+    k_rotate_tc(const Tables t, int ks_begin, float2 *__restrict__ X, const unsigned char *__restrict__ img,
+                long long img_stride, int *__restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[3];
   __shared__ uint32_t tmem_slot;
@@ -359,7 +413,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = tmem_slot;
   const uint32_t idesc = idesc_bf16(TC_M, N);
   float2 *Xb = X + K.psi_off;
-  const double2 *Cb = C + mat_off[ksi];
+  const unsigned char *Bimg = img + (long long)blockIdx.y * img_stride;
   const int nkb = (KT + TC_KB - 1) / TC_KB;
   bool ok = true;
   for (int kb = 0; kb < nkb; ++kb) {
@@ -375,6 +429,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     unsigned char *A_hi = stage[s], *A_lo = A_hi + a_bytes, *B_hi = A_lo + a_bytes,
                   *B_lo = B_hi + b_bytes;
     const int ib = kb * (TC_KB / 2);  // first band of this K block
+    // B: this K block's hi and lo parts, contiguous in the image, copied as is
+    {
+      const unsigned char *src = Bimg + (size_t)kb * 2 * b_bytes;
+      for (int i = tid; i < (int)(2 * b_bytes / 16); i += TC_THREADS) cp_async16_tc(B_hi + 16 * i, src + 16 * i);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
     // A: row g, chunk k8 holds bands ib + 4 k8 .. +3 as (re, im) pairs
     for (int c = tid; c < TC_M * 8; c += TC_THREADS) {
       const int row = c % TC_M, k8 = c / TC_M;
@@ -393,29 +453,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       *reinterpret_cast<uint4 *>(A_hi + core_off(row, k8)) = hi;
       *reinterpret_cast<uint4 *>(A_lo + core_off(row, k8)) = lo;
     }
-    // B: row n = 2 j + part, chunk k8 holds bands ib + 4 k8 .. +3
-    for (int c = tid; c < N * 8; c += TC_THREADS) {
-      const int row = c >> 3, k8 = c & 7;
-      const int j = row >> 1, part = row & 1;
-      float v[8];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i = ib + 4 * k8 + q;
-        double2 cij = make_double2(0.0, 0.0);
-        if (row < 2 * nb && i < nb) cij = Cb[(long long)i * nb + j];
-        if (part == 0) {
-          v[2 * q] = (float)cij.x;
-          v[2 * q + 1] = (float)(-cij.y);
-        } else {
-          v[2 * q] = (float)cij.y;
-          v[2 * q + 1] = (float)cij.x;
-        }
-      }
-      uint4 hi, lo;
-      split8(v, hi, lo);
-      *reinterpret_cast<uint4 *>(B_hi + core_off(row, k8)) = hi;
-      *reinterpret_cast<uint4 *>(B_lo + core_off(row, k8)) = lo;
-    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -472,12 +510,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 void launch_rotate_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, float2 *X,
-                      const double2 *C, const long long *mat_off, int *status, cudaStream_t st) {
+                      const double2 *C, const long long *mat_off, unsigned char *img, int *status,
+                      cudaStream_t st) {
   if (nks <= 0) return;
+  const long long stride = (long long)rotate_tc_image_bytes(max_nb);
+  derek::note_launch(), k_rotate_operand<<<dim3(4, nks), 256, 0, st>>>(t, ks_begin, C, mat_off, img, stride);
   const size_t sm = overlap_tc_smem(max_nb);
   cudaFuncSetAttribute(k_rotate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((max_npw + TC_M - 1) / TC_M, nks);
-  derek::note_launch(), k_rotate_tc<<<grid, TC_THREADS, sm, st>>>(t, ks_begin, X, C, mat_off, status);
+  derek::note_launch(), k_rotate_tc<<<grid, TC_THREADS, sm, st>>>(t, ks_begin, X, img, stride, status);
 }
 
 }  // namespace derek
