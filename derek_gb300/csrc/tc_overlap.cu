@@ -176,6 +176,55 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int nkb = (k1 - k0 + TC_KB - 1) / TC_KB;
   bool ok = true;
 
+  // Jobs per K block: A rows j < nb (chunk (j, k8) of X) and B rows j < nb
+  // (chunk (j, k8) of Y, which also gives row nb + j = -i Y_j); job q of
+  // thread tid is c = tid + q TC_THREADS.  The raw chunks of the next K block
+  // are loaded into registers while the current one is converted.
+  constexpr int QJ = 2 * TC_M * 8 / TC_THREADS;   // jobs per thread at nb = 128
+  const int njobs = 2 * nb * 8;
+  // rows no job writes stay zero: A rows >= nb, B rows >= 2 nb (both stages)
+  for (int s2 = 0; s2 < 2; ++s2) {
+    unsigned char *A_hi = stage[s2], *A_lo = A_hi + a_bytes, *B_hi = A_lo + a_bytes,
+                  *B_lo = B_hi + b_bytes;
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    for (int c = tid; c < (TC_M - nb) * 8; c += TC_THREADS) {
+      const int row = nb + (c >> 3), k8 = c & 7;
+      *reinterpret_cast<uint4 *>(A_hi + core_off(row, k8)) = z;
+      *reinterpret_cast<uint4 *>(A_lo + core_off(row, k8)) = z;
+    }
+    for (int c = tid; c < (N - 2 * nb) * 8; c += TC_THREADS) {
+      const int row = 2 * nb + (c >> 3), k8 = c & 7;
+      *reinterpret_cast<uint4 *>(B_hi + core_off(row, k8)) = z;
+      *reinterpret_cast<uint4 *>(B_lo + core_off(row, k8)) = z;
+    }
+  }
+  float4 nxt[QJ][2];
+  auto load_block = [&](int kb) {
+    const int kbase = k0 + kb * TC_KB;
+#pragma unroll
+    for (int q = 0; q < QJ; ++q) {
+      const int c = tid + q * TC_THREADS;
+      if (c < njobs) {
+        const bool isB = c >= nb * 8;
+        const int cc = isB ? c - nb * 8 : c;
+        const int row = cc >> 3, k8 = cc & 7;
+        const int kk = kbase + k8 * 8;
+        const float *src = (isB ? Yb : Xb) + row * ld + kk;
+        if (kk + 8 <= k1) {
+          nxt[q][0] = *reinterpret_cast<const float4 *>(src);
+          nxt[q][1] = *reinterpret_cast<const float4 *>(src + 4);
+        } else {
+          float w[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) w[i] = kk + i < k1 ? src[i] : 0.0f;
+          nxt[q][0] = make_float4(w[0], w[1], w[2], w[3]);
+          nxt[q][1] = make_float4(w[4], w[5], w[6], w[7]);
+        }
+      }
+    }
+  };
+  if (nkb > 0) load_block(0);
+
   for (int kb = 0; kb < nkb; ++kb) {
     const int s = kb & 1;
     if (kb >= 2) {
@@ -189,45 +238,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     unsigned char *A_hi = stage[s], *A_lo = A_hi + a_bytes, *B_hi = A_lo + a_bytes,
                   *B_lo = B_hi + b_bytes;
-    const int kbase = k0 + kb * TC_KB;
-    // A: 128 rows x 8 chunks of 8 reals
-    for (int c = tid; c < TC_M * 8; c += TC_THREADS) {
-      const int row = c >> 3, k8 = c & 7;
-      float v[8];
-      const int kk = kbase + k8 * 8;
+    float4 cur[QJ][2];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] = (row < nb && kk + i < k1) ? Xb[row * ld + kk + i] : 0.0f;
-      uint4 hi, lo;
-      split8(v, hi, lo);
-      *reinterpret_cast<uint4 *>(A_hi + core_off(row, k8)) = hi;
-      *reinterpret_cast<uint4 *>(A_lo + core_off(row, k8)) = lo;
+    for (int q = 0; q < QJ; ++q) {
+      cur[q][0] = nxt[q][0];
+      cur[q][1] = nxt[q][1];
     }
-    // B: rows j < nb -> Y_j; nb <= j < 2nb -> -i Y_{j-nb} = (y_im, -y_re); rest zero
-    for (int c = tid; c < N * 8; c += TC_THREADS) {
-      const int row = c >> 3, k8 = c & 7;
-      float v[8];
-      const int kk = kbase + k8 * 8;
-      if (row < nb) {
+    if (kb + 1 < nkb) load_block(kb + 1);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = (kk + i < k1) ? Yb[row * ld + kk + i] : 0.0f;
-      } else if (row < 2 * nb) {
-        const int r = row - nb;
-#pragma unroll
-        for (int i = 0; i < 8; i += 2) {
-          const bool in = kk + i < k1;
-          const float re = in ? Yb[r * ld + kk + i] : 0.0f;
-          const float im = in ? Yb[r * ld + kk + i + 1] : 0.0f;
-          v[i] = im;
-          v[i + 1] = -re;
+    for (int q = 0; q < QJ; ++q) {
+      const int c = tid + q * TC_THREADS;
+      if (c < njobs) {
+        const bool isB = c >= nb * 8;
+        const int cc = isB ? c - nb * 8 : c;
+        const int row = cc >> 3, k8 = cc & 7;
+        const float v[8] = {cur[q][0].x, cur[q][0].y, cur[q][0].z, cur[q][0].w,
+                            cur[q][1].x, cur[q][1].y, cur[q][1].z, cur[q][1].w};
+        uint4 hi, lo;
+        split8(v, hi, lo);
+        if (!isB) {
+          *reinterpret_cast<uint4 *>(A_hi + core_off(row, k8)) = hi;
+          *reinterpret_cast<uint4 *>(A_lo + core_off(row, k8)) = lo;
+        } else {
+          *reinterpret_cast<uint4 *>(B_hi + core_off(row, k8)) = hi;
+          *reinterpret_cast<uint4 *>(B_lo + core_off(row, k8)) = lo;
+          // row nb + j: -i Y_j interleaves (y_im, -y_re)
+          const float w[8] = {v[1], -v[0], v[3], -v[2], v[5], -v[4], v[7], -v[6]};
+          split8(w, hi, lo);
+          *reinterpret_cast<uint4 *>(B_hi + core_off(nb + row, k8)) = hi;
+          *reinterpret_cast<uint4 *>(B_lo + core_off(nb + row, k8)) = lo;
         }
-      } else {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = 0.0f;
       }
-      uint4 hi, lo;
-      split8(v, hi, lo);
-      *reinterpret_cast<uint4 *>(B_hi + core_off(row, k8)) = hi;
-      *reinterpret_cast<uint4 *>(B_lo + core_off(row, k8)) = lo;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
