@@ -141,13 +141,14 @@ __device__ __forceinline__ void move_columns(float2 *P, float2 *a0, long long ld
 // r = b div ng, R = gridDim.x / ng.  Its V(r) planes stay in shared memory
 // while consecutive items belong to the same system.  While the forward z
 // transforms of a tile run (most threads idle), the threads without a z line
-// describe the next tile and stage its column and row offsets, so a tile
-// starts with one load round trip (its columns).
+// load the next tile's columns into registers and, when its k-set differs
+// from the one whose offsets their buffer holds, stage its column and row
+// offsets (per k-set data: consecutive tiles of a block mostly share one).
 struct PlaneTileSm {
   long long a_base;    // offset of (band, x0) in the x-plane buffer
   long long ld;        // x-plane buffer row pitch
   long long vbase;     // offset of plane x0 in V(r)
-  int sys, ncol, nrow, np, valid, pad;
+  int sys, ncol, nrow, np, valid, ks;
 };
 
 template <int N, int XP>
@@ -162,6 +163,7 @@ __device__ __forceinline__ void plane_tile_describe(const Tables &t, int item_be
   if (!m.valid) return;
   const int b = t.item_band[item];
   m.sys = K.sys;
+  m.ks = t.item_ks[item];
   m.np = min(XP, n1 - x0);
   m.ld = K.ncol_pad;
   m.a_base = K.a_off + ((long long)b * n1 + x0) * K.ncol_pad;
@@ -183,6 +185,7 @@ __device__ __forceinline__ void stage_offsets(const Tables &t, int item_begin, i
   const short *cy = t.col_y + K.col_off;
   const short *cz = t.col_z + K.col_off;
   const short *rows = t.rows + K.row_off;
+#pragma unroll 4
   for (int c = tid; c < ncol; c += nthr) coff[c] = (short)(Lay::row_of(cy[c]) * Lay::PZ + cz[c]);
   for (int l = tid; l < nrow; l += nthr) roff[l] = (short)(Lay::row_of(rows[l]) * Lay::PZ);
 }
@@ -203,7 +206,8 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
   float *Vs = reinterpret_cast<float *>(smem_raw + (((size_t)XP * PP * sizeof(float2) + 15) & ~(size_t)15));
   short *offs = reinterpret_cast<short *>(Vs + XP * VP);   // [2][MAXC + MAXR]
   __shared__ PlaneTileSm meta[2];
-  __shared__ int v_sys;   // system whose V(r) planes are in Vs (-1: none)
+  __shared__ int v_sys;      // system whose V(r) planes are in Vs (-1: none)
+  __shared__ int offs_ks[2];   // k-set whose offsets each offset buffer holds
   const int tid = threadIdx.x;
   const int g = blockIdx.x % ng;
   const int R = gridDim.x / ng;
@@ -212,6 +216,8 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
   if (tid == 0) {
     plane_tile_describe<N, XP>(t, item_begin, it, g, meta[0]);
     v_sys = -1;
+    offs_ks[0] = meta[0].valid ? meta[0].ks : -1;
+    offs_ks[1] = -1;
   }
   __syncthreads();
   if (meta[0].valid)
@@ -344,17 +350,6 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
         if constexpr (Lay::kept(mm)) line[mm] = v[line_slot<N>(mm, 1)];
       });
     }
-    if (meta[cur ^ 1].valid) {
-      // the next tile's offsets: staged by the threads without a z line
-      // (whole warps past the last z line) while the z transforms run, or by
-      // every thread after its z line when nearly all threads have one
-      const int t0 = zthr < NT - 32 ? (zthr + 31) / 32 * 32 : 0;
-      if (tid >= t0) {
-        short *nco = offs + (cur ^ 1) * (MAXC + MAXR);
-        stage_offsets<N, RY, NT>(t, item_begin, next, meta[cur ^ 1].ncol, meta[cur ^ 1].nrow, nco,
-                                 nco + MAXC, t0);
-      }
-    }
     // the next tile's columns into registers (threads past the z lines, when
     // they can hold all of them)
     pf_t0 = -1;
@@ -377,7 +372,21 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
         }
       }
     }
+    // the next tile's offsets, unless its offset buffer already holds its
+    // k-set: staged by the threads without a z line (whole warps past the
+    // last z line) while the z transforms run, or by every thread after its
+    // z line when nearly all threads have one
+    const bool restage = meta[cur ^ 1].valid && offs_ks[cur ^ 1] != meta[cur ^ 1].ks;
+    if (restage) {
+      const int t0 = zthr < NT - 32 ? (zthr + 31) / 32 * 32 : 0;
+      if (tid >= t0) {
+        short *nco = offs + (cur ^ 1) * (MAXC + MAXR);
+        stage_offsets<N, RY, NT>(t, item_begin, next, meta[cur ^ 1].ncol, meta[cur ^ 1].nrow, nco,
+                                 nco + MAXC, t0);
+      }
+    }
     __syncthreads();
+    if (tid == 0 && restage) offs_ks[cur ^ 1] = meta[cur ^ 1].ks;
     if (valid) {
       float2 *a0 = abuf + meta[cur].a_base;
       const long long ld = meta[cur].ld;
