@@ -25,6 +25,16 @@ namespace derek {
 constexpr int kXThreads = 128;   // columns (threads) per block
 
 template <int N> __host__ __device__ constexpr int mx_of(int j) { return j > N / 2 ? j - N : j; }
+
+// L2 prefetch of [p, p + bytes) on 16-byte boundaries: the start rounded
+// down (the buffers start on 256-byte boundaries), the end rounded down so
+// the range never passes the end of the run
+__device__ __forceinline__ void prefetch_l2(const void *p, int bytes) {
+  const unsigned long long a = reinterpret_cast<unsigned long long>(p);
+  const unsigned long long lo = a & ~15ull, hi = (a + (unsigned)bytes) & ~15ull;
+  if (hi > lo)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
+}
 template <int N, int RX> __host__ __device__ constexpr bool x_kept(int j) {
   return mx_of<N>(j) >= -RX && mx_of<N>(j) <= RX;
 }
@@ -78,6 +88,14 @@ __global__ void __launch_bounds__(kXThreads, 3) k_xfwd_reg(Tables t, int item_be
   if (!S.active) return;
   const int b = t.item_band[item];
   const long long ld = K.ncol_pad;
+  const int *cs = t.col_start + K.col_off;
+  const int e0 = cs[c], cnt = cs[c + 1] - e0, x0 = t.col_x0[K.col_off + c];
+  const long long off = K.psi_off + (long long)b * K.npw_pad + e0;
+  const float *kin = t.kin32 + K.ent_off + e0;
+  // the epilogue's runs into L2 while the x-line loads and the transform run
+  prefetch_l2(psi + off, cnt * (int)sizeof(float2));
+  if (prev) prefetch_l2(prev + off, cnt * (int)sizeof(float2));
+  prefetch_l2(kin, cnt * (int)sizeof(float));
   const float2 *src = abuf + K.a_off + (long long)b * N * ld + c;
   float2 v[N];
   static_for<0, N>([&](auto jc) {
@@ -85,10 +103,6 @@ __global__ void __launch_bounds__(kXThreads, 3) k_xfwd_reg(Tables t, int item_be
     v[j] = src[j * ld];
   });
   reg_fft<N, -1, 0>(v);
-  const int *cs = t.col_start + K.col_off;
-  const int e0 = cs[c], cnt = cs[c + 1] - e0, x0 = t.col_x0[K.col_off + c];
-  const long long off = K.psi_off + (long long)b * K.npw_pad + e0;
-  const float *kin = t.kin32 + K.ent_off + e0;
   const float inv_n = 1.0f / (float)S.nr;
   float al = 1, be = 0, ga = 0, tk = 1;
   if (coef) {
