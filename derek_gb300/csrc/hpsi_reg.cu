@@ -20,121 +20,9 @@
 // costs one load and one store per element.  The V(r) planes of the block
 // are copied into shared memory with cp.async while the columns are gathered
 // and the z transforms run, and stay there while the system is unchanged.
-#include "kernels.cuh"
-#include "regfft.cuh"
+#include "planes.cuh"
 
 namespace derek {
-
-// Shared-memory layout of one plane (rows my in [-RY, RY]) and of one V(r)
-// plane.  The plane pitch PP is congruent to N mod 16 and the V pitch VP to N
-// mod 32, so a warp straddling two planes still reads consecutive banks.
-// kept(j): line index j (0 <= j < N) has a centred index within [-RY, RY];
-// the same bound holds for the z index of every sphere column.
-template <int N, int RY> struct RowsLayout {
-  static_assert(RY >= 0 && 2 * RY + 1 <= N + 1, "row bound");
-  static constexpr int NRW = 2 * RY + 1;
-  static constexpr int PZ = N | 1;
-  static constexpr int PP0 = NRW * PZ;
-  static constexpr int PP = PP0 + ((N - PP0) % 16 + 16) % 16;
-  static constexpr int VP = N * N + ((N - N * N) % 32 + 32) % 32;
-  // centred index of line index j (0 <= j < N)
-  __host__ __device__ static constexpr int my_of(int j) { return j > N / 2 ? j - N : j; }
-  __host__ __device__ static constexpr bool kept(int j) { return my_of(j) >= -RY && my_of(j) <= RY; }
-  __host__ __device__ static constexpr int row_of(int j) { return my_of(j) + RY; }
-};
-
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-template <int N>
-__device__ __forceinline__ void load_line(float2 (&v)[N], const float2 *p, int stride) {
-  static_for<0, N>([&](auto jc) {
-    constexpr int j = decltype(jc)::value;
-    v[j] = p[j * stride];
-  });
-}
-
-// store X[m] (slot line_slot(m, L)) to p[m * stride]
-template <int N, int L>
-__device__ __forceinline__ void store_line(const float2 (&v)[N], float2 *p, int stride) {
-  static_for<0, N>([&](auto mc) {
-    constexpr int m = decltype(mc)::value;
-    p[m * stride] = v[line_slot<N>(m, L)];
-  });
-}
-
-// column z of a plane: the kept rows from shared memory, zeros elsewhere
-template <int N, int RY>
-__device__ __forceinline__ void load_column(float2 (&v)[N], const float2 *col) {
-  using Lay = RowsLayout<N, RY>;
-  static_for<0, N>([&](auto jc) {
-    constexpr int j = decltype(jc)::value;
-    if constexpr (Lay::kept(j))
-      v[j] = col[Lay::row_of(j) * Lay::PZ];
-    else
-      v[j] = make_float2(0.f, 0.f);
-  });
-}
-
-// z transforms of the rows holding columns, planes [0, np).  The backward
-// transform reads only the z positions a sphere column can occupy (the rest
-// of the row is zero); the forward one stores only those positions.
-template <int N, int RY, int SIGN>
-__device__ __forceinline__ void z_pass(float2 *P, int np, int nrow, const short *__restrict__ rows) {
-  using Lay = RowsLayout<N, RY>;
-  const int tid = threadIdx.x;
-  if (tid < np * nrow) {
-    const int p = tid / nrow;
-    const int l = tid - p * nrow;
-    float2 *line = P + p * Lay::PP + Lay::row_of(rows[l]) * Lay::PZ;
-    float2 v[N];
-    if (SIGN > 0) {
-      static_for<0, N>([&](auto jc) {
-        constexpr int j = decltype(jc)::value;
-        if constexpr (Lay::kept(j))
-          v[j] = line[j];
-        else
-          v[j] = make_float2(0.f, 0.f);
-      });
-      reg_fft<N, SIGN, 0>(v);
-      store_line<N, 1>(v, line, 1);
-    } else {
-      load_line<N>(v, line, 1);
-      reg_fft<N, SIGN, 0>(v);
-      static_for<0, N>([&](auto mc) {
-        constexpr int m = decltype(mc)::value;
-        if constexpr (Lay::kept(m)) line[m] = v[line_slot<N>(m, 1)];
-      });
-    }
-  }
-}
-
-// columns of the item's sphere into (IN) or out of the planes
-template <int N, int RY, int XP, int NT, bool IN>
-__device__ __forceinline__ void move_columns(float2 *P, float2 *a0, long long ld, int np, int ncol,
-                                             const short *__restrict__ cy, const short *__restrict__ cz) {
-  using Lay = RowsLayout<N, RY>;
-  for (int c = threadIdx.x; c < ncol; c += NT) {
-    const int off = Lay::row_of(cy[c]) * Lay::PZ + cz[c];
-#pragma unroll
-    for (int p = 0; p < XP; ++p) {
-      if (p < np) {
-        if (IN)
-          P[p * Lay::PP + off] = a0[p * ld + c];
-        else
-          a0[p * ld + c] = P[p * Lay::PP + off];
-      }
-    }
-  }
-}
 
 // ---- H.psi (y,z) pass ----------------------------------------------------------
 // Block b keeps x-group g = b mod ng and walks the items r, r + R, ... with
@@ -404,121 +292,7 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
   }
 }
 
-// Density of one k-set over XP x-planes: loop over bands, accumulate
-// f_b |psi_b(r)|^2 per point in FP32 for up to kFlush bands, then add that
-// sum into the FP64 per-k-set partial grid (each point owned by one thread).
-constexpr int kFlush = 8;
-
-template <int N, int RY, int XP, int NT>
-__global__ void __launch_bounds__(NT, 1) k_density_rows(Tables t, int ks_begin, const float2 *__restrict__ abuf,
-                                                        const double *__restrict__ occ,
-                                                        double *__restrict__ partial,
-                                                        const long long *__restrict__ partial_off) {
-  using Lay = RowsLayout<N, RY>;
-  constexpr int PZ = Lay::PZ, PP = Lay::PP;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2 *P = reinterpret_cast<float2 *>(smem_raw);
-  float *acc = reinterpret_cast<float *>(P + XP * PP);
-  short *rows_s = reinterpret_cast<short *>(acc + XP * N * N);
-  const int ksi = ks_begin + blockIdx.x;
-  const KSetDev &K = t.ks[ksi];
-  const SysDev &S = t.sys[K.sys];
-  if (!S.active) return;
-  const int n1 = S.n[0];
-  const int x0 = blockIdx.y * XP;
-  if (x0 >= n1) return;
-  const int np = min(XP, n1 - x0);
-  const int tid = threadIdx.x;
-  for (int i = tid; i < np * PP; i += NT) P[i] = make_float2(0.f, 0.f);
-  const bool owner = tid < np * N;
-  const int p = owner ? tid / N : 0;
-  const int z = owner ? tid - p * N : 0;
-  float *accz = acc + p * N * N + z;
-  if (owner)
-    static_for<0, N>([&](auto mc) { accz[decltype(mc)::value * N] = 0.f; });
-  double *dst = partial + partial_off[ksi] + (long long)(x0 + p) * N * N + z;
-  const int nrow = K.nrow;
-  const long long ld = K.ncol_pad;
-  const short *cy = t.col_y + K.col_off;
-  const short *cz = t.col_z + K.col_off;
-  const short *rows = t.rows + K.row_off;
-  for (int l = tid; l < nrow; l += NT) rows_s[l] = (short)Lay::row_of(rows[l]);
-  int pending = 0;     // bands summed in acc since the last flush
-  bool first = true;   // dst not yet written
-  for (int b = 0; b < K.nb; ++b) {
-    const double w = occ[K.item0 + b];
-    if (w == 0.0) continue;
-    __syncthreads();   // previous band's column reads done; P's rows are zero again
-    float2 *a0 = const_cast<float2 *>(abuf) + K.a_off + ((long long)b * n1 + x0) * ld;
-    move_columns<N, RY, XP, NT, true>(P, a0, ld, np, K.ncol, cy, cz);
-    __syncthreads();
-    z_pass<N, RY, +1>(P, np, nrow, rows);
-    __syncthreads();
-    if (owner) {
-      float2 *col = P + p * PP + z;
-      float2 v[N];
-      load_column<N, RY>(v, col);
-      // clear this column's rows for the next band's gather
-      for (int l = 0; l < nrow; ++l) col[rows_s[l] * PZ] = make_float2(0.f, 0.f);
-      reg_fft<N, +1, 0>(v);
-      const float wf = (float)w;
-      static_for<0, N>([&](auto mc) {
-        constexpr int m = decltype(mc)::value;
-        const float2 e = v[line_slot<N>(m, 1)];
-        accz[m * N] += wf * (e.x * e.x + e.y * e.y);
-      });
-      if (++pending == kFlush) {
-        static_for<0, N>([&](auto mc) {
-          constexpr int m = decltype(mc)::value;
-          const double s = (double)accz[m * N];
-          dst[m * N] = first ? s : dst[m * N] + s;
-          accz[m * N] = 0.f;
-        });
-        first = false;
-        pending = 0;
-      }
-    }
-  }
-  if (owner && (pending || first)) {
-    static_for<0, N>([&](auto mc) {
-      constexpr int m = decltype(mc)::value;
-      const double s = (double)accz[m * N];
-      dst[m * N] = first ? s : dst[m * N] + s;
-    });
-  }
-}
-
 // ---- launch shapes -----------------------------------------------------------
-// Row bound of the compact kernels: a fine grid of N points along y holds the
-// sphere's |my| <= N / 4 + 1 whenever the grid is about twice the sphere's
-// diameter (the density cutoff); other spheres use every row (RY = N / 2).
-template <int N> constexpr int compact_ry() { return N / 4 + 1; }
-
-constexpr int kSmemMax = 227 * 1024;
-constexpr int kThreadsMax = 384;
-
-// planes per block: as many as fit the shared memory and kThreadsMax threads
-template <int N, int RY, bool DENSITY> struct RowsShape {
-  using Lay = RowsLayout<N, RY>;
-  static constexpr int PLANE = Lay::PP * 8 + (DENSITY ? N * N * 4 : Lay::VP * 4);
-  static constexpr int BY_SMEM = (kSmemMax - 2 * N - 16) / PLANE;
-  static constexpr int BY_THREADS = kThreadsMax / N;
-  static constexpr int XP0 = BY_SMEM < BY_THREADS ? BY_SMEM : BY_THREADS;
-  static constexpr int XP = XP0 < 1 ? 1 : XP0;
-  static constexpr int NT = (N * XP + 31) / 32 * 32;
-  static constexpr size_t SMEM = (size_t)XP * PLANE + 2 * N + 16;
-};
-
-static int sm_count() {
-  static int n = [] {
-    int dev = 0, c = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
-    return c > 0 ? c : 1;
-  }();
-  return n;
-}
-
 template <int N, int RY>
 static void plane_persist_go(const Tables &t, int item_begin, int nitems, int max_n1, float2 *abuf,
                              const float *vloc, cudaStream_t st) {
@@ -539,33 +313,19 @@ static void plane_persist_go(const Tables &t, int item_begin, int nitems, int ma
   derek::note_launch(), kern<<<ng * R, NT, smem, st>>>(t, item_begin, nitems, ng, abuf, vloc);
 }
 
-template <int N, int RY>
-static void density_rows_go(const Tables &t, int ks_begin, int nks, int max_n1, const float2 *abuf,
-                            const double *occ, double *partial, const long long *partial_off,
-                            cudaStream_t st) {
-  using Sh = RowsShape<N, RY, true>;
-  auto kern = k_density_rows<N, RY, Sh::XP, Sh::NT>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM);
-  const int ng = (max_n1 + Sh::XP - 1) / Sh::XP;
-  derek::note_launch(), kern<<<dim3(nks, ng), Sh::NT, Sh::SMEM, st>>>(t, ks_begin, abuf, occ, partial, partial_off);
-}
-
 template <int N>
 static void plane_go(const Tables &t, int item_begin, int nitems, int max_n1, int max_m, float2 *abuf,
                      const float *vloc, cudaStream_t st) {
+  if constexpr (tight_ry<N>() > 0) {
+    if (max_m <= tight_ry<N>()) {
+      plane_persist_go<N, tight_ry<N>()>(t, item_begin, nitems, max_n1, abuf, vloc, st);
+      return;
+    }
+  }
   if (max_m <= compact_ry<N>())
     plane_persist_go<N, compact_ry<N>()>(t, item_begin, nitems, max_n1, abuf, vloc, st);
   else
     plane_persist_go<N, N / 2>(t, item_begin, nitems, max_n1, abuf, vloc, st);
-}
-
-template <int N>
-static void density_go(const Tables &t, int ks_begin, int nks, int max_n1, int max_m, const float2 *abuf,
-                       const double *occ, double *partial, const long long *partial_off, cudaStream_t st) {
-  if (max_m <= compact_ry<N>())
-    density_rows_go<N, compact_ry<N>()>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
-  else
-    density_rows_go<N, N / 2>(t, ks_begin, nks, max_n1, abuf, occ, partial, partial_off, st);
 }
 
 bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, int n, int max_m,
@@ -579,22 +339,6 @@ bool launch_plane_reg(const Tables &t, int item_begin, int nitems, int max_n1, i
     case 32: plane_go<32>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
     case 27: plane_go<27>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
     case 24: plane_go<24>(t, item_begin, nitems, max_n1, max_m, abuf, vloc, st); return true;
-    default: return false;
-  }
-}
-
-bool launch_density_reg(const Tables &t, int ks_begin, int nks, int max_n1, int n, int max_m,
-                        const float2 *abuf, const double *occ, double *partial,
-                        const long long *partial_off, cudaStream_t st) {
-  switch (n) {
-    case 72: density_go<72>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
-    case 64: density_go<64>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
-    case 54: density_go<54>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
-    case 48: density_go<48>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
-    case 36: density_go<36>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
-    case 32: density_go<32>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
-    case 27: density_go<27>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
-    case 24: density_go<24>(t, ks_begin, nks, max_n1, max_m, abuf, occ, partial, partial_off, st); return true;
     default: return false;
   }
 }

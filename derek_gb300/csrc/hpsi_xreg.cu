@@ -135,8 +135,10 @@ __global__ void __launch_bounds__(kXThreads, 3) k_xfwd_reg(Tables t, int item_be
   });
 }
 
-// |Miller x| bound of the compact kernels (as the planes' row bound)
+// |Miller x| bounds of the compact and tight kernels (as the planes' row
+// bounds; no tight kernels below N = 48)
 template <int N> constexpr int compact_rx() { return N / 4 + 1; }
+template <int N> constexpr int tight_rx() { return N >= 48 ? N / 4 - 2 : 0; }
 
 template <int N, int RX>
 static void xinv_go(const Tables &t, int item_begin, int nitems, int max_ncol, const float2 *psi,
@@ -155,6 +157,12 @@ static void xfwd_go(const Tables &t, int item_begin, int nitems, int max_ncol, c
 template <int N>
 static void xinv_n(const Tables &t, int item_begin, int nitems, int max_ncol, int max_m, const float2 *psi,
                    float2 *abuf, const double *occ_skip, cudaStream_t st) {
+  if constexpr (tight_rx<N>() > 0) {
+    if (max_m <= tight_rx<N>()) {
+      xinv_go<N, tight_rx<N>()>(t, item_begin, nitems, max_ncol, psi, abuf, occ_skip, st);
+      return;
+    }
+  }
   if (max_m <= compact_rx<N>())
     xinv_go<N, compact_rx<N>()>(t, item_begin, nitems, max_ncol, psi, abuf, occ_skip, st);
   else
@@ -164,6 +172,12 @@ static void xinv_n(const Tables &t, int item_begin, int nitems, int max_ncol, in
 template <int N>
 static void xfwd_n(const Tables &t, int item_begin, int nitems, int max_ncol, int max_m, const float2 *abuf,
                    const float2 *psi, const float2 *prev, float2 *out, const Axpby *coef, cudaStream_t st) {
+  if constexpr (tight_rx<N>() > 0) {
+    if (max_m <= tight_rx<N>()) {
+      xfwd_go<N, tight_rx<N>()>(t, item_begin, nitems, max_ncol, abuf, psi, prev, out, coef, st);
+      return;
+    }
+  }
   if (max_m <= compact_rx<N>())
     xfwd_go<N, compact_rx<N>()>(t, item_begin, nitems, max_ncol, abuf, psi, prev, out, coef, st);
   else

@@ -116,10 +116,11 @@ REG_LENGTHS = [24, 27, 32, 36, 48, 54, 64, 72]
 
 def reg_plane_pair(oracle, n, rows, kpts, nb, seed):
     """Cubic cell on an n^3 grid whose sphere reaches max(|mx|, |my|, |mz|) =
-    N/4 + 1 ("compact": the FP32 kernels keep only those x, y and z line
-    positions) or N/4 + 3 ("all": every position kept)."""
+    N/4 - 2 ("tight": from N = 48 on, kernels that keep only those x, y and z
+    line positions), N/4 + 1 ("compact") or N/4 + 3 ("all": every position
+    kept)."""
     L = 8.0
-    rmax = n // 4 + 1 if rows == "compact" else n // 4 + 3
+    rmax = {"tight": n // 4 - 2, "compact": n // 4 + 1, "all": n // 4 + 3}[rows]
     rho = rmax + 0.25   # Miller radius; k_y = 0.2 puts the extreme rows at +-rmax
     ecut = 0.5 * (rho * 2 * np.pi / L) ** 2
     s, spec = make_pair(oracle, L=L, ecut=ecut, nb=nb, kpts=kpts, seed=seed, n_fine=(n, n, n))
@@ -128,7 +129,7 @@ def reg_plane_pair(oracle, n, rows, kpts, nb, seed):
     return s, spec
 
 
-@pytest.mark.parametrize("rows", ["compact", "all"])
+@pytest.mark.parametrize("rows", ["tight", "compact", "all"])
 @pytest.mark.parametrize("n", REG_LENGTHS)
 def test_apply_h_register_planes(oracle, n, rows):
     """FP32 H.psi through the register-line plane kernels at every compiled
@@ -146,7 +147,7 @@ def test_apply_h_register_planes(oracle, n, rows):
     assert rel_err(got, oracle.apply_h(s, kb, v, psi)) < FP32_TOL
 
 
-@pytest.mark.parametrize("rows", ["compact", "all"])
+@pytest.mark.parametrize("rows", ["tight", "compact", "all"])
 @pytest.mark.parametrize("n", REG_LENGTHS)
 def test_density_register_planes(oracle, n, rows):
     """FP32 density through the register-line plane kernels (band loop with
