@@ -52,6 +52,13 @@ __global__ void __launch_bounds__(NT, 1) k_density_rows(Tables t, int ks_begin, 
     if (w == 0.0) continue;
     __syncthreads();   // previous band's column reads done; P's rows are zero again
     float2 *a0 = const_cast<float2 *>(abuf) + K.a_off + ((long long)b * n1 + x0) * ld;
+    if (tid == 0 && b + 1 < K.nb) {
+      // the next band's x-plane rows (np consecutive rows of ld columns,
+      // 128-byte aligned, ld a multiple of 16) into L2 while this band runs
+      const float2 *nxt = a0 + (long long)n1 * ld;
+      const unsigned bytes = (unsigned)((long long)np * ld * sizeof(float2));
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nxt), "r"(bytes) : "memory");
+    }
     move_columns<N, RY, XP, NT, true>(P, a0, ld, np, K.ncol, cy, cz);
     __syncthreads();
     z_pass<N, RY, +1>(P, np, nrow, rows);
