@@ -50,14 +50,15 @@ METRIC = "converged ground states/sec at |dE|<1e-6 Ha/e vs FP64 path"
 UNIT = "ground_states/s"
 WORKLOAD = "kpts64: L=16 bohr, Ecut=20 Ha, 72^3 grid, 4x4x4 MP (64 k), 64 e / 80 bands, 16 wells"
 ETOL_PER_E = 1e-7    # Ha per electron: SCF stops at |F - F_prev| < ETOL_PER_E * N_e
-# Solver options of both arms: Chebyshev filter degree 6 per iteration and a
-# first iteration of 2 filter passes of degree 12 from the random start (the
-# fastest setting of a sweep over degrees 5-8 and 1-4 first passes of degree
-# 8-16 on kpts64; every setting met the accuracy gate).
-SOLVER = dict(cheb_degree=6, first_passes=2, first_degree=12)
+# Solver options of both arms: Chebyshev filter degree 6 per iteration, start
+# vectors on the lowest plane waves of each k-point and a first iteration of
+# one filter pass of degree 12 (the fastest setting of sweeps over degrees
+# 5-8, 0-4 first passes of degree 6-16 and random or plane-wave starts on
+# kpts64; every setting met the accuracy gate).
+SOLVER = dict(cheb_degree=6, first_passes=1, first_degree=12, init_vectors=1)
 # SCF iterations the GPU solver takes on kpts64 with SOLVER (its runs are
 # bit-deterministic); the reference arm scales its sample to this count.
-KPTS64_ITERATIONS = 11
+KPTS64_ITERATIONS = 12
 FP64_TOL = 1e-6      # Ha per electron: |F_mixed - F_FP64| / N_e must stay below
 
 

@@ -50,6 +50,7 @@ class ScfOpts(ctypes.Structure):
         ("cheb_degree", _i), ("first_passes", _i), ("first_degree", _i),
         ("seed", ctypes.c_uint64), ("use_graph", _i), ("use_tensor_cores", _i),
         ("density_tol", _d), ("buffer_bands", _i), ("etol_per_electron", _i),
+        ("init_vectors", _i),
     ]
 
 

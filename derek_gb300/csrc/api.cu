@@ -161,6 +161,7 @@ void derek_gpu_default_opts(derek_scf_opts *o) {
   o->density_tol = 0.0;
   o->buffer_bands = -1;
   o->etol_per_electron = 0;
+  o->init_vectors = 0;
 }
 
 const char *derek_gpu_strerror(int s) {
@@ -185,7 +186,7 @@ const char *derek_gpu_last_error(derek_gpu_t *h) {
 int derek_gpu_destroy(derek_gpu_t *h) {
   if (!h) return DEREK_ERR_BAD_ARG;
   void *ptrs[] = {h->d_sys,   h->d_ks,      h->d_item_ks, h->d_item_band, h->d_ent_col,
-                  h->d_col_start, h->d_ent_ix, h->d_col_y, h->d_col_z, h->d_col_x0, h->d_rows,  h->d_kin64,     h->d_kin32,
+                  h->d_col_start, h->d_ent_ix, h->d_col_y, h->d_col_z, h->d_col_x0, h->d_rows, h->d_pw_entry, h->d_kin64,     h->d_kin32,
                   h->d_tw64,  h->d_tw32,    h->d_vext,    h->d_vloc,      h->d_vhxc,
                   h->d_vloc32, h->d_rho_in, h->d_rho_out, h->d_exc,       h->d_vxc,
                   h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
@@ -234,6 +235,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
 
   std::vector<int> ent_col, col_start;
   std::vector<short> ent_ix, col_y, col_z, col_x0, rows;
+  std::vector<int> pw_entry;
   std::vector<float> kin32;
   std::vector<double> tw64;
   std::map<int, long long> tw_of;  // n -> offset
@@ -406,6 +408,17 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       a_off += (long long)nbi * nfine[0] * K.ncol_pad;
       partial_off.push_back(part_off);
       part_off += S.nr;
+      {
+        // plane-wave start vectors: the nbi lowest kinetic energies of the
+        // k-point (ties by entry index), entries in column order
+        std::vector<int> order(npw);
+        for (int i = 0; i < npw; ++i) order[i] = i;
+        const double *kc = h->kin_col.data() + K.ent_off;
+        std::partial_sort(order.begin(), order.begin() + nbi, order.end(), [kc](int a, int b) {
+          return kc[a] < kc[b] || (kc[a] == kc[b] && a < b);
+        });
+        for (int b = 0; b < nbi; ++b) pw_entry.push_back(order[b]);
+      }
       for (int b = 0; b < nbi; ++b) {
         h->item_ks.push_back((int)h->ks.size());
         h->item_band.push_back(b);
@@ -434,6 +447,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   CK(upload(&h->d_col_z, col_z));
   CK(upload(&h->d_col_x0, col_x0));
   CK(upload(&h->d_rows, rows));
+  CK(upload(&h->d_pw_entry, pw_entry));
   CK(upload(&h->d_kin64, h->kin_col));
   CK(upload(&h->d_kin32, kin32));
   {

@@ -42,6 +42,7 @@ struct derek_gpu {
   int *d_item_ks = nullptr, *d_item_band = nullptr;
   int *d_ent_col = nullptr, *d_col_start = nullptr;
   short *d_ent_ix = nullptr, *d_col_y = nullptr, *d_col_z = nullptr, *d_col_x0 = nullptr, *d_rows = nullptr;
+  int *d_pw_entry = nullptr;   // per item: entry of its band's start plane wave
   double *d_kin64 = nullptr;
   float *d_kin32 = nullptr;
   double2 *d_tw64 = nullptr;

@@ -141,10 +141,11 @@ int scf_start(derek_gpu *h, double etol) {
                    h->d_vext, h->d_vhxc, h->d_vloc, h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vloc32,
                    h->d_epart, h->d_state, 1, h->stream);
   h->cur = 0;
+  const int *pw = h->opts.init_vectors == 1 ? h->d_pw_entry : nullptr;
   if (h->prec == DEREK_PREC_FP64)
-    launch_init_psi<double>(h->tab, h->nitems, h->d_X, h->opts.seed, h->stream);
+    launch_init_psi<double>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
   else
-    launch_init_psi<float>(h->tab, h->nitems, h->d_X, h->opts.seed, h->stream);
+    launch_init_psi<float>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
   DEREK_CUDA(h, cudaGetLastError());
   int s = cholqr_rr(h);
   if (s) return s;

@@ -57,7 +57,8 @@ __device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
 }
 
 template <typename R>
-__global__ void k_init_psi(const Tables t, cplx<R> *__restrict__ X, unsigned long long seed) {
+__global__ void k_init_psi(const Tables t, cplx<R> *__restrict__ X, unsigned long long seed,
+                           const int *__restrict__ pw_entry) {
   const int item = blockIdx.x;
   const int ksi = t.item_ks[item];
   const KSetDev &K = t.ks[ksi];
@@ -65,11 +66,14 @@ __global__ void k_init_psi(const Tables t, cplx<R> *__restrict__ X, unsigned lon
   const unsigned long long key = (seed * 0x100000001B3ULL) ^ ((unsigned long long)K.sys << 40) ^
                                  ((unsigned long long)K.kidx << 24);
   cplx<R> *dst = X + K.psi_off + (long long)b * K.npw_pad;
+  // plane-wave start: one entry 1, the rest a small perturbation
+  const int e1 = pw_entry ? pw_entry[item] : -1;
+  const double amp = pw_entry ? 1e-3 : 1.0;
   for (int g = threadIdx.x; g < K.npw_pad; g += blockDim.x) {
     R v = 0;
     if (g < K.npw) {
       const unsigned long long h = splitmix64(key + (unsigned long long)b * (1ULL << 20) + g);
-      v = (R)((double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5);
+      v = (R)(amp * ((double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5) + (g == e1 ? 1.0 : 0.0));
     }
     dst[g] = mk<R>(v, 0);
   }
@@ -541,11 +545,12 @@ __global__ void __launch_bounds__(256) k_uniform_density(const Tables t, double 
 
 // ---------------------------------------------------------------------------
 template <typename R>
-void launch_init_psi(const Tables &t, int nitems, void *X, unsigned long long seed, cudaStream_t st) {
-  derek::note_launch(), k_init_psi<R><<<nitems, 256, 0, st>>>(t, (cplx<R> *)X, seed);
+void launch_init_psi(const Tables &t, int nitems, void *X, unsigned long long seed, const int *pw_entry,
+                     cudaStream_t st) {
+  derek::note_launch(), k_init_psi<R><<<nitems, 256, 0, st>>>(t, (cplx<R> *)X, seed, pw_entry);
 }
-template void launch_init_psi<float>(const Tables &, int, void *, unsigned long long, cudaStream_t);
-template void launch_init_psi<double>(const Tables &, int, void *, unsigned long long, cudaStream_t);
+template void launch_init_psi<float>(const Tables &, int, void *, unsigned long long, const int *, cudaStream_t);
+template void launch_init_psi<double>(const Tables &, int, void *, unsigned long long, const int *, cudaStream_t);
 
 void launch_filter_coef(const Tables &t, int nks, const double *eig, const SysState *st, Axpby *coef,
                         int m, cudaStream_t s) {

@@ -8,7 +8,10 @@
 namespace derek {
 
 template <typename R>
-void launch_init_psi(const Tables &t, int nitems, void *X, unsigned long long seed, cudaStream_t st);
+// start vectors: hashed random entries, or (pw_entry non-null) band b of item
+// i on entry pw_entry[i] plus a small hashed perturbation
+void launch_init_psi(const Tables &t, int nitems, void *X, unsigned long long seed, const int *pw_entry,
+                     cudaStream_t st);
 void launch_filter_coef(const Tables &t, int nks, const double *eig, const SysState *st, Axpby *coef,
                         int m, cudaStream_t s);
 void launch_occupations(const Tables &t, int nsys, const double *eig, double *occ, double *occw,

@@ -101,6 +101,9 @@ typedef struct {
                               subspace (-1 = max(4, nbands/20)) */
   int    etol_per_electron;/* 1: scf_run's etol is per electron (each system
                               stops at |dF| < etol * nelec) */
+  int    init_vectors;     /* start vectors: 0 = hashed random entries; 1 = band
+                              b on the b-th lowest-kinetic-energy plane wave of
+                              its k-point, plus a 1e-3 hashed perturbation */
 } derek_scf_opts;
 
 /* Per-system SCF report (Source/electronic.f90:143-146 table row). */

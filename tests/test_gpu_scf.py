@@ -32,10 +32,13 @@ def make_handle(oracle, d, precision=0, **opts):
     return dg.Handle(spec, precision=precision, **kw)
 
 
+@pytest.mark.parametrize("init", [0, 1])
 @pytest.mark.parametrize("name", ["scf_c1", "scf_kpts"])
-def test_scf_fp64_matches_oracle(oracle, name):
+def test_scf_fp64_matches_oracle(oracle, name, init):
+    """From hashed random start vectors (init 0) or from the lowest plane
+    waves (init 1) the SCF reaches the oracle's ground state."""
     d = load(name)
-    with make_handle(oracle, d) as h:
+    with make_handle(oracle, d, init_vectors=init) as h:
         rep = h.electronic_scf(max_scf=300, etol=1e-12)[0]
         eig = h.eigenvalues()
         rho = h.density()
