@@ -267,6 +267,27 @@ __global__ void __launch_bounds__(256) k_cholesky_inv(const Tables t, int ks_beg
 // ---------------------------------------------------------------------------
 // pair k of round r in the circle schedule over ne positions (position 0
 // fixed, the others advance one place per round)
+// Rotation that zeroes the Hermitian 2x2 block [[a, b], [conj(b), d]]: the
+// phase ph = b / |b|, then the real symmetric rotation (c, s) of
+// [[a, |b|], [|b|, d]] with t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
+// tau = (d - a) / (2 |b|), c = 1 / sqrt(1 + t^2), s = t c (Rutishauser).
+// Written as one reciprocal of |b|, one division and three square roots (the
+// last a reciprocal square root): the dependent FP64 chain every Jacobi
+// round waits on.  The entries are bounded by the matrix norm, so |b| needs
+// no hypot scaling.  False (no rotation) when |b| <= skip.
+__device__ __forceinline__ bool jacobi_rotation(double a, double d, double2 b, double skip, double &c,
+                                                double &s, double2 &ph) {
+  const double e2 = b.x * b.x + b.y * b.y;
+  if (!(e2 > skip * skip)) return false;
+  const double ie = 1.0 / sqrt(e2);
+  ph = make_double2(b.x * ie, b.y * ie);
+  const double tau = (d - a) * (0.5 * ie);
+  const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+  c = rsqrt(1.0 + tt * tt);
+  s = tt * c;
+  return true;
+}
+
 __device__ __forceinline__ void rr_pair(int k, int r, int ne, int &p, int &q) {
   const int m = ne - 1;
   const int a = k == 0 ? 0 : 1 + (k - 1 + r) % m;
@@ -361,17 +382,7 @@ __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
         double2 ph = make_double2(1.0, 0.0);
         int on = 0;
         if (q < n) {
-          const double a = A[p * n + p].x, d = A[q * n + q].x;
-          const double2 b = A[p * n + q];
-          const double e = hypot(b.x, b.y);
-          if (e > skip) {
-            ph = make_double2(b.x / e, b.y / e);
-            const double tau = (d - a) / (2.0 * e);
-            const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            c = 1.0 / sqrt(1.0 + tt * tt);
-            s = tt * c;
-            on = 1;
-          }
+          on = jacobi_rotation(A[p * n + p].x, A[q * n + q].x, A[p * n + q], skip, c, s, ph) ? 1 : 0;
         }
         rc[k] = c;
         rs[k] = s;
@@ -570,17 +581,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
         double2 ph = make_double2(1.0, 0.0);
         int on = 0;
         if (q < n) {
-          const double a = A[p * n + p].x, d = A[q * n + q].x;
-          const double2 b = A[p * n + q];
-          const double e = hypot(b.x, b.y);
-          if (e > skip) {
-            ph = make_double2(b.x / e, b.y / e);
-            const double tau = (d - a) / (2.0 * e);
-            const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            c = 1.0 / sqrt(1.0 + tt * tt);
-            s = tt * c;
-            on = 1;
-          }
+          on = jacobi_rotation(A[p * n + p].x, A[q * n + q].x, A[p * n + q], skip, c, s, ph) ? 1 : 0;
         }
         rc[k] = c;
         rs[k] = s;
