@@ -271,15 +271,14 @@ __global__ void __launch_bounds__(256) k_cholesky_inv(const Tables t, int ks_beg
 // phase ph = b / |b|, then the real symmetric rotation (c, s) of
 // [[a, |b|], [|b|, d]] with t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
 // tau = (d - a) / (2 |b|), c = 1 / sqrt(1 + t^2), s = t c (Rutishauser).
-// Written as one reciprocal of |b|, one division and three square roots (the
-// last a reciprocal square root): the dependent FP64 chain every Jacobi
-// round waits on.  The entries are bounded by the matrix norm, so |b| needs
+// Written as two reciprocal square roots, one square root and one division:
+// the dependent FP64 chain every Jacobi round waits on.  The entries are bounded by the matrix norm, so |b| needs
 // no hypot scaling.  False (no rotation) when |b| <= skip.
 __device__ __forceinline__ bool jacobi_rotation(double a, double d, double2 b, double skip, double &c,
                                                 double &s, double2 &ph) {
   const double e2 = b.x * b.x + b.y * b.y;
   if (!(e2 > skip * skip)) return false;
-  const double ie = 1.0 / sqrt(e2);
+  const double ie = rsqrt(e2);
   ph = make_double2(b.x * ie, b.y * ie);
   const double tau = (d - a) * (0.5 * ie);
   const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
