@@ -58,7 +58,7 @@ ETOL_PER_E = 1e-7    # Ha per electron: SCF stops at |F - F_prev| < ETOL_PER_E *
 SOLVER = dict(cheb_degree=6, first_passes=1, first_degree=12, init_vectors=1)
 # SCF iterations the GPU solver takes on kpts64 with SOLVER (its runs are
 # bit-deterministic); the reference arm scales its sample to this count.
-KPTS64_ITERATIONS = 12
+KPTS64_ITERATIONS = 11
 FP64_TOL = 1e-6      # Ha per electron: |F_mixed - F_FP64| / N_e must stay below
 
 
