@@ -291,6 +291,117 @@ class Handle:
         _check(lib.derek_gpu_get_density(self._h, sys, _dptr(rho)), self._h, "density")
         return rho
 
+    # ---- files and restart
+    def set_start_density(self, rho, sys=0):
+        """The next electronic_scf starts system sys from this density (None:
+        the uniform start again)."""
+        if rho is None:
+            _check(lib.derek_gpu_set_start_density(self._h, sys, None), self._h, "set_start_density")
+            return
+        rho = np.ascontiguousarray(np.asarray(rho, dtype=np.float64))
+        _check(lib.derek_gpu_set_start_density(self._h, sys, _dptr(rho)), self._h, "set_start_density")
+
+    def wavefunction_box(self, sys=0):
+        """All wavefunctions in the reference's wavefunction%coeff layout:
+        (n_std product, nk, nbands, 2) complex128, the sphere's coefficients
+        at their box rows (Source/basis.f90:125-149 order), zeros elsewhere
+        and in the second spinor component (Source/wave.f90:164)."""
+        s = self.systems[sys]
+        _, ns = self.grid(sys)
+        nbox = int(np.prod(ns))
+        c = np.zeros((nbox, len(s.kpts), s.nbands, 2), dtype=np.complex128, order="F")
+        for k in range(len(s.kpts)):
+            rows, _, _ = self.gsphere(sys, k)
+            c[rows, k, :, 0] = self.get_wfn(sys, k).T
+        return c
+
+    def write_state(self, seed, sys=0):
+        """seed.den, seed.pot, seed.potex and seed.wvfn of system sys as the
+        reference writes them (Source/state.f90:203-232 and the type-bound
+        writers): the last density, the local potential and the external
+        potential on the spin diagonal, and the wavefunctions."""
+        nf, ns = self.grid(sys)
+        nr = int(np.prod(nf))
+        write_den(seed + ".den", ns, self.density(sys).astype(np.complex128))
+        for ext, v in ((".pot", self.get_vloc(sys)), (".potex", self.get_vext(sys))):
+            nc = np.zeros((nr, 2, 2), dtype=np.complex128, order="F")
+            nc[:, 0, 0] = v
+            nc[:, 1, 1] = v
+            write_pot(seed + ext, ns, nc)
+        write_wvfn(seed + ".wvfn", ns, self.wavefunction_box(sys))
+
+    def restart_density(self, path, sys=0):
+        """Start the next SCF of system sys from the charge in a .den file."""
+        nf, ns = self.grid(sys)
+        charge, _ = read_den(path, ns, int(np.prod(nf)))
+        self.set_start_density(charge.real, sys)
+
+
+# ---- the reference's files (host only)
+def _ns(n_std):
+    return (ctypes.c_int * 3)(*[int(x) for x in n_std])
+
+
+def _cplx(a, shape):
+    a = np.asarray(a, dtype=np.complex128).reshape(shape, order="F")
+    return np.ascontiguousarray(a.ravel(order="F").view(np.float64))
+
+
+def write_den(path, n_std, charge, spin=None):
+    """Binary .den (Source/density.f90:128-160): charge (nr,) and spin (nr, 3)."""
+    nr = int(np.size(charge))
+    c = _cplx(charge, (nr,))
+    sp = None if spin is None else _dptr(_cplx(spin, (nr, 3)))
+    _check(lib.derek_io_write_den(str(path).encode(), _ns(n_std), nr, _dptr(c), sp), None, "write_den")
+
+
+def read_den(path, n_std, nr):
+    c = np.zeros(2 * nr)
+    sp = np.zeros(6 * nr)
+    _check(lib.derek_io_read_den(str(path).encode(), _ns(n_std), int(nr), _dptr(c), _dptr(sp)), None,
+           "read_den")
+    return c.view(np.complex128), sp.view(np.complex128).reshape((nr, 3), order="F")
+
+
+def write_pot(path, n_std, nc_pot):
+    """Binary .pot / .potex (Source/pot.f90:194-224): nc_pot (nr, 2, 2)."""
+    nr = np.asarray(nc_pot).shape[0]
+    v = _cplx(nc_pot, (nr, 2, 2))
+    _check(lib.derek_io_write_pot(str(path).encode(), _ns(n_std), nr, _dptr(v)), None, "write_pot")
+
+
+def read_pot(path, n_std, nr):
+    v = np.zeros(8 * nr)
+    _check(lib.derek_io_read_pot(str(path).encode(), _ns(n_std), int(nr), _dptr(v)), None, "read_pot")
+    return v.view(np.complex128).reshape((nr, 2, 2), order="F")
+
+
+def write_wvfn(path, n_std, coeff):
+    """Binary .wvfn (Source/wave.f90:893-921): coeff (nbox, nk, nbands, nspinor)."""
+    shape = np.asarray(coeff).shape
+    c = _cplx(coeff, shape)
+    _check(lib.derek_io_write_wvfn(str(path).encode(), _ns(n_std), shape[0], shape[1], shape[2], shape[3],
+                                   _dptr(c)), None, "write_wvfn")
+
+
+def read_wvfn(path, n_std, nbox, nk, nb, nspinor=2):
+    c = np.zeros(2 * nbox * nk * nb * nspinor)
+    _check(lib.derek_io_read_wvfn(str(path).encode(), _ns(n_std), int(nbox), int(nk), int(nb), int(nspinor),
+                                  _dptr(c)), None, "read_wvfn")
+    return c.view(np.complex128).reshape((nbox, nk, nb, nspinor), order="F")
+
+
+def write_xsf(path, cell, n_fine, data):
+    """XSF grid file of real values (Source/xsf.f90:67-128)."""
+    cm = (ctypes.c_double * 9)(*np.asarray(cell, dtype=np.float64).reshape(3, 3).ravel(order="F"))
+    d = np.ascontiguousarray(np.asarray(data, dtype=np.float64))
+    _check(lib.derek_io_write_xsf(str(path).encode(), cm, _ns(n_fine), _dptr(d)), None, "write_xsf")
+
+
+def set_subrecord_limit(nbytes=0):
+    """Largest Fortran subrecord written (0: gfortran's 2^31 - 9 bytes)."""
+    _check(lib.derek_io_set_subrecord_limit(int(nbytes)), None, "subrecord_limit")
+
 
 def launch_count() -> int:
     """Kernels launched by the library in this process (graph replays included)."""

@@ -100,6 +100,15 @@ SIGNATURES = {
     "derek_gpu_stream": (_vp, [_vp]),
     "derek_gpu_launch_count": (ctypes.c_ulonglong, []),
     "derek_gpu_time_apply_h": (_i, [_vp, _i, _pd, _pd]),
+    "derek_gpu_set_start_density": (_i, [_vp, _i, _pd]),
+    "derek_io_write_den": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd, _pd]),
+    "derek_io_read_den": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd, _pd]),
+    "derek_io_write_pot": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd]),
+    "derek_io_read_pot": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd]),
+    "derek_io_write_wvfn": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _i, _i, _i, _pd]),
+    "derek_io_read_wvfn": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _i, _i, _i, _pd]),
+    "derek_io_write_xsf": (_i, [ctypes.c_char_p, ctypes.POINTER(_d), ctypes.POINTER(_i), _pd]),
+    "derek_io_set_subrecord_limit": (_i, [ctypes.c_longlong]),
     "derek_host_prime_fact": (_i, [_i]),
     "derek_host_grid_sizes": (_i, [ctypes.POINTER(_d), _d, _d, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "derek_host_gsphere": (_i, [ctypes.POINTER(_d), _d, ctypes.POINTER(_d), ctypes.POINTER(_i), _i, _vp,

@@ -616,6 +616,18 @@ int derek_gpu_set_vloc(derek_gpu_t *h, int s, const double *v) {
   return DEREK_OK;
 }
 
+int derek_gpu_set_start_density(derek_gpu_t *h, int s, const double *rho) {
+  if (!check_sys(h, s)) return DEREK_ERR_BAD_ARG;
+  if ((int)h->start_rho.size() < h->nsys) h->start_rho.resize(h->nsys);
+  if (!rho) {
+    h->start_rho[s].clear();
+    return DEREK_OK;
+  }
+  const SysDev &S = h->sys[s];
+  h->start_rho[s].assign(rho, rho + S.nr);
+  return DEREK_OK;
+}
+
 int derek_gpu_get_vloc(derek_gpu_t *h, int s, double *v) {
   if (!check_sys(h, s) || !v) return DEREK_ERR_BAD_ARG;
   const SysDev &S = h->sys[s];

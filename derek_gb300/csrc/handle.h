@@ -52,6 +52,7 @@ struct derek_gpu {
   double *d_vext = nullptr, *d_vloc = nullptr, *d_vhxc = nullptr;
   float *d_vloc32 = nullptr;
   double *d_rho_in = nullptr, *d_rho_out = nullptr;
+  std::vector<std::vector<double>> start_rho;   // per system: SCF start density (empty = uniform)
   double *d_exc = nullptr, *d_vxc = nullptr;
   double2 *d_cgrid = nullptr;      // complex work grid
   double *d_partial = nullptr;     // per-k-set density partials

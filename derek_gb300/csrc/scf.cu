@@ -137,6 +137,11 @@ int scf_start(derek_gpu *h, double etol) {
                                 cudaMemcpyHostToDevice, h->stream));
   DEREK_CUDA(h, cudaMemsetAsync(h->d_status, 0, h->nks * sizeof(int), h->stream));
   launch_uniform_density(h->tab, h->nsys, (int)h->max_nr, h->d_rho_in, h->stream);
+  for (int s = 0; s < h->nsys && s < (int)h->start_rho.size(); ++s)
+    if (!h->start_rho[s].empty())
+      DEREK_CUDA(h, cudaMemcpyAsync(h->d_rho_in + h->sys[s].grid_off, h->start_rho[s].data(),
+                                    h->start_rho[s].size() * sizeof(double), cudaMemcpyHostToDevice,
+                                    h->stream));
   launch_potential(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_in, h->d_cgrid,
                    h->d_vext, h->d_vhxc, h->d_vloc, h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vloc32,
                    h->d_epart, h->d_state, 1, h->stream);

@@ -240,6 +240,41 @@ int derek_gpu_get_eigenvalues(derek_gpu_t *h, int sys, double *eig /* nk*nb */);
 int derek_gpu_get_occupations(derek_gpu_t *h, int sys, double *occ /* nk*nb */);
 int derek_gpu_get_density(derek_gpu_t *h, int sys, double *rho /* nr */);
 
+/* Restart: the next scf_run starts system `sys` from this density (nr FP64
+ * values, the reference's flat z-fastest order) instead of the uniform one;
+ * NULL clears it.  Pairs with derek_io_read_den for a .den restart
+ * (Source/state.f90 state_restart, which the reference leaves disabled at
+ * Source/derek.f90:71-74). */
+int derek_gpu_set_start_density(derek_gpu_t *h, int sys, const double *rho);
+
+/* The reference's output files, host only (no GPU needed).  Binary files are
+ * one big-endian Fortran sequential record each (gfortran with
+ * -fconvert=big-endian, Source/Makefile:86; 4-byte length markers,
+ * subrecords past 2^31 - 9 bytes with negated continuation markers):
+ *   .den   n_std(3), charge(nr), spin(nr,3), .true.  Source/density.f90:128-160
+ *   .pot   n_std(3), nc_pot(nr,2,2), .true.          Source/pot.f90:194-224
+ *   .potex as .pot (the external potential)          Source/state.f90:203-232
+ *   .wvfn  n_std(3), coeff(nbox,nk,nb,nspinor), nbands, kpts, .true.
+ *                                                     Source/wave.f90:893-921
+ * Complex arrays are interleaved (re, im) doubles, column-major; n_std is
+ * the standard grid written in the header (the readers require it to
+ * match, as pot_read does at Source/pot.f90:329-331); nr is the number of
+ * fine-grid points.  NULL spin writes zeros; NULL outputs skip a field. */
+int derek_io_write_den(const char *path, const int n_std[3], long long nr, const double *charge,
+                       const double *spin);
+int derek_io_read_den(const char *path, const int n_std[3], long long nr, double *charge, double *spin);
+int derek_io_write_pot(const char *path, const int n_std[3], long long nr, const double *nc_pot);
+int derek_io_read_pot(const char *path, const int n_std[3], long long nr, double *nc_pot);
+int derek_io_write_wvfn(const char *path, const int n_std[3], long long nbox, int nk, int nb, int nspinor,
+                        const double *coeff);
+int derek_io_read_wvfn(const char *path, const int n_std[3], long long nbox, int nk, int nb, int nspinor,
+                       double *coeff);
+/* XSF grid file (Source/xsf.f90:67-128): cell rows in F20.10, one value per
+ * line in E20.10, in the array's flat order as the reference writes it. */
+int derek_io_write_xsf(const char *path, const double cell[9], const int n_fine[3], const double *data);
+/* Test hook: largest subrecord in bytes (0 = gfortran's 2147483639). */
+int derek_io_set_subrecord_limit(long long bytes);
+
 /* Host-only helpers (no GPU needed): the grid and sphere rules the handle
  * uses, exposed so drivers and tests can check them on any machine. */
 int derek_host_prime_fact(int n);  /* Source/basis.f90:257-309 */

@@ -169,3 +169,39 @@ def test_mixed_batch_same_grid_matches_single_systems():
         with dg.Handle(s, precision=1, **opts) as h1:
             r1 = h1.electronic_scf(max_scf=100, etol=1e-6)[0]
         assert abs(rb["free_energy"] - r1["free_energy"]) < 1e-5, (rb["free_energy"], r1["free_energy"])
+
+
+def test_restart_from_written_density(oracle, tmp_path):
+    """write_state writes the reference's .den/.pot/.potex/.wvfn; a new
+    handle started from the written .den reaches the same ground state in
+    fewer iterations (Source/state.f90 restart, disabled in the reference)."""
+    import derek_gb300 as dg
+    from oracle import fortran_records as F
+    d = load("scf_c1")
+    seed = str(tmp_path / "c1")
+    with make_handle(oracle, d) as h:
+        rep = h.electronic_scf(max_scf=300, etol=1e-12)[0]
+        h.write_state(seed)
+        nf, ns = h.grid()
+        rho = h.density()
+        vloc = h.get_vloc()
+        wfn = [h.get_wfn(0, k) for k in range(len(d["kpts"]))]
+        rows = [h.gsphere(0, k)[0] for k in range(len(d["kpts"]))]
+    nr = int(np.prod(nf))
+    with open(seed + ".den", "rb") as f:
+        n_std, charge, spin, alloc = F.parse_den(F.read_record(f.read())[0], nr)
+    assert n_std == tuple(ns) and alloc == 1 and not spin.any()
+    assert np.array_equal(charge.real, rho) and not charge.imag.any()
+    pot = dg.read_pot(seed + ".pot", ns, nr)
+    assert np.array_equal(pot[:, 0, 0].real, vloc) and np.array_equal(pot[:, 1, 1], pot[:, 0, 0])
+    nbox = int(np.prod(ns))
+    c = dg.read_wvfn(seed + ".wvfn", ns, nbox, len(d["kpts"]), int(d["nbands"]), 2)
+    for k in range(len(d["kpts"])):
+        assert np.array_equal(c[rows[k], k, :, 0], wfn[k].T)
+    assert not c[..., 1].any()
+    with make_handle(oracle, d) as h2:
+        h2.restart_density(seed + ".den")
+        rep2 = h2.electronic_scf(max_scf=300, etol=1e-12)[0]
+    assert rep2["converged"], rep2
+    assert abs(rep2["free_energy"] - d["free_energy"]) < 1e-8
+    assert rep2["iterations"] < rep["iterations"], (rep2["iterations"], rep["iterations"])
