@@ -291,6 +291,24 @@ class Handle:
         _check(lib.derek_gpu_get_density(self._h, sys, _dptr(rho)), self._h, "density")
         return rho
 
+    # ---- bandstructure and dos (non-self-consistent)
+    def nscf(self, max_iter=200, eig_tol=1e-9):
+        """Eigenvalues (nk, nbands) per system in the potential set with
+        set_vloc, converged to eig_tol Ha; returns (eigenvalues list,
+        iterations)."""
+        it = ctypes.c_int()
+        _check(lib.derek_gpu_nscf_run(self._h, int(max_iter), float(eig_tol), ctypes.byref(it)), self._h,
+               "nscf_run")
+        return [self.eigenvalues(s) for s in range(len(self.systems))], it.value
+
+    def dos(self, energies, sigma=0.01, sys=0):
+        """Density of states per Ha (both spins) of the last eigenvalues:
+        sum_k w_k sum_b 2 g_sigma(E - e_kb), Gaussian of width sigma Ha."""
+        s = self.systems[sys]
+        eig = self.eigenvalues(sys)
+        wk = np.full(len(s.kpts), 1.0 / len(s.kpts)) if s.wk is None else np.asarray(s.wk)
+        return dos_gaussian(eig, wk, energies, sigma)
+
     # ---- files and restart
     def set_start_density(self, rho, sys=0):
         """The next electronic_scf starts system sys from this density (None:
@@ -335,6 +353,13 @@ class Handle:
         nf, ns = self.grid(sys)
         charge, _ = read_den(path, ns, int(np.prod(nf)))
         self.set_start_density(charge.real, sys)
+
+
+def dos_gaussian(eig, wk, energies, sigma):
+    """sum_k w_k sum_b 2 exp(-(E - e_kb)^2 / (2 sigma^2)) / (sigma sqrt(2 pi))."""
+    e = np.asarray(energies, dtype=np.float64)[:, None, None]
+    g = np.exp(-0.5 * ((e - np.asarray(eig)[None]) / sigma) ** 2) / (sigma * np.sqrt(2 * np.pi))
+    return 2.0 * np.einsum("ekb,k->e", g, np.asarray(wk, dtype=np.float64))
 
 
 # ---- the reference's files (host only)

@@ -12,6 +12,7 @@
 // with every scalar kept on the device, so a steady-state iteration is one
 // CUDA graph launch followed by a small state read-back.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "handle.h"
@@ -351,6 +352,66 @@ int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
   for (const auto &x : st)
     if (x.status) return x.status;
   return DEREK_OK;
+}
+
+int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterations) {
+  if (!h || max_iter <= 0 || !(eig_tol > 0)) return DEREK_ERR_BAD_ARG;
+  // frozen potential: the filter's upper bound from max V_loc of each system
+  for (auto &s : h->sys) s.active = 1;
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
+  std::vector<SysState> st(h->nsys);
+  for (int s = 0; s < h->nsys; ++s) {
+    std::memset(&st[s], 0, sizeof(SysState));
+    st[s].slot = -1;
+    std::vector<double> v(h->sys[s].nr);
+    DEREK_CUDA(h, cudaMemcpy(v.data(), h->d_vloc + h->sys[s].grid_off, v.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost));
+    st[s].vmax = *std::max_element(v.begin(), v.end());
+  }
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_state, st.data(), st.size() * sizeof(SysState),
+                                cudaMemcpyHostToDevice, h->stream));
+  DEREK_CUDA(h, cudaMemsetAsync(h->d_status, 0, h->nks * sizeof(int), h->stream));
+  h->cur = 0;
+  const int *pw = h->opts.init_vectors == 1 ? h->d_pw_entry : nullptr;
+  if (h->prec == DEREK_PREC_FP64)
+    launch_init_psi<double>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
+  else
+    launch_init_psi<float>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
+  int s = cholqr_rr(h);
+  if (s) return s;
+  // reported bands of every k-set (the buffer bands converge more slowly)
+  std::vector<double> eig(h->nitems), prev;
+  auto status = [&]() -> int {
+    std::vector<int> stat(h->nks);
+    DEREK_CUDA(h, cudaMemcpy(stat.data(), h->d_status, stat.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int x : stat)
+      if (x) return x;
+    return DEREK_OK;
+  };
+  int it = 0;
+  bool converged = false;
+  for (; it < max_iter; ++it) {
+    s = subspace_step(h, h->opts.cheb_degree);
+    if (s) return s;
+    DEREK_CUDA(h, cudaMemcpyAsync(eig.data(), h->d_eig, eig.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                  h->stream));
+    DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if ((s = status())) return s;
+    if (!prev.empty()) {
+      double d = 0;
+      for (const auto &K : h->ks)
+        for (int b = 0; b < K.nbr; ++b) d = std::max(d, std::fabs(eig[K.item0 + b] - prev[K.item0 + b]));
+      if (d < eig_tol) {
+        converged = true;
+        ++it;
+        break;
+      }
+    }
+    prev = eig;
+  }
+  if (iterations) *iterations = it;
+  return converged ? DEREK_OK : DEREK_ERR_NOT_CONVERGED;
 }
 
 int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol, derek_scf_report *rep) {

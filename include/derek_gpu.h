@@ -240,6 +240,16 @@ int derek_gpu_get_eigenvalues(derek_gpu_t *h, int sys, double *eig /* nk*nb */);
 int derek_gpu_get_occupations(derek_gpu_t *h, int sys, double *occ /* nk*nb */);
 int derek_gpu_get_density(derek_gpu_t *h, int sys, double *rho /* nr */);
 
+/* Non-self-consistent eigenvalues (the bandstructure and dos tasks, whose
+ * routines are empty in the reference: Source/spectral.f90:33-44; task
+ * keys Source/io.f90:519-527, DOS grid key dos_kpt_mp_grid io.f90:111):
+ * Chebyshev-filtered subspace iterations of degree cheb_degree in the
+ * potential set with derek_gpu_set_vloc (e.g. a converged one), from the
+ * start vectors of init_vectors, until no reported eigenvalue of any
+ * k-point moves by eig_tol between iterations.  Eigenvalues through
+ * derek_gpu_get_eigenvalues.  *iterations may be NULL. */
+int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterations);
+
 /* Restart: the next scf_run starts system `sys` from this density (nr FP64
  * values, the reference's flat z-fastest order) instead of the uniform one;
  * NULL clears it.  Pairs with derek_io_read_den for a .den restart
