@@ -292,13 +292,13 @@ class Handle:
         return rho
 
     # ---- bandstructure and dos (non-self-consistent)
-    def nscf(self, max_iter=200, eig_tol=1e-9):
+    def nscf(self, max_iter=200, eig_tol=1e-9, nconv=0):
         """Eigenvalues (nk, nbands) per system in the potential set with
-        set_vloc, converged to eig_tol Ha; returns (eigenvalues list,
-        iterations)."""
+        set_vloc, the lowest nconv bands (0: all) converged to eig_tol Ha;
+        returns (eigenvalues list, iterations)."""
         it = ctypes.c_int()
-        _check(lib.derek_gpu_nscf_run(self._h, int(max_iter), float(eig_tol), ctypes.byref(it)), self._h,
-               "nscf_run")
+        _check(lib.derek_gpu_nscf_run(self._h, int(max_iter), float(eig_tol), int(nconv), ctypes.byref(it)),
+               self._h, "nscf_run")
         return [self.eigenvalues(s) for s in range(len(self.systems))], it.value
 
     def dos(self, energies, sigma=0.01, sys=0):

@@ -101,7 +101,7 @@ SIGNATURES = {
     "derek_gpu_launch_count": (ctypes.c_ulonglong, []),
     "derek_gpu_time_apply_h": (_i, [_vp, _i, _pd, _pd]),
     "derek_gpu_set_start_density": (_i, [_vp, _i, _pd]),
-    "derek_gpu_nscf_run": (_i, [_vp, _i, _d, ctypes.POINTER(_i)]),
+    "derek_gpu_nscf_run": (_i, [_vp, _i, _d, _i, ctypes.POINTER(_i)]),
     "derek_io_write_den": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd, _pd]),
     "derek_io_read_den": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd, _pd]),
     "derek_io_write_pot": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd]),

@@ -354,8 +354,8 @@ int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
   return DEREK_OK;
 }
 
-int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterations) {
-  if (!h || max_iter <= 0 || !(eig_tol > 0)) return DEREK_ERR_BAD_ARG;
+int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, int *iterations) {
+  if (!h || max_iter <= 0 || !(eig_tol > 0) || nconv < 0) return DEREK_ERR_BAD_ARG;
   // frozen potential: the filter's upper bound from max V_loc of each system
   for (auto &s : h->sys) s.active = 1;
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
@@ -380,7 +380,9 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterat
     launch_init_psi<float>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
   int s = cholqr_rr(h);
   if (s) return s;
-  // reported bands of every k-set (the buffer bands converge more slowly)
+  // the lowest nconv reported bands of every k-set (0: all reported): a band
+  // close below the subspace's top converges slowly under the filter, whose
+  // damped interval reaches up to Ecut + max V
   std::vector<double> eig(h->nitems), prev;
   auto status = [&]() -> int {
     std::vector<int> stat(h->nks);
@@ -391,6 +393,8 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterat
   };
   int it = 0;
   bool converged = false;
+  double last = -1.0;   // largest change of the last iteration
+  int last_ks = -1, last_b = -1;
   for (; it < max_iter; ++it) {
     s = subspace_step(h, h->opts.cheb_degree);
     if (s) return s;
@@ -400,8 +404,18 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterat
     if ((s = status())) return s;
     if (!prev.empty()) {
       double d = 0;
-      for (const auto &K : h->ks)
-        for (int b = 0; b < K.nbr; ++b) d = std::max(d, std::fabs(eig[K.item0 + b] - prev[K.item0 + b]));
+      for (int q = 0; q < h->nks; ++q) {
+        const auto &K = h->ks[q];
+        for (int b = 0; b < (nconv > 0 ? std::min(nconv, K.nbr) : K.nbr); ++b) {
+          const double x = std::fabs(eig[K.item0 + b] - prev[K.item0 + b]);
+          if (x > d) {
+            d = x;
+            last_ks = q;
+            last_b = b;
+          }
+        }
+      }
+      last = d;
       if (d < eig_tol) {
         converged = true;
         ++it;
@@ -411,6 +425,9 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterat
     prev = eig;
   }
   if (iterations) *iterations = it;
+  if (!converged)
+    h->last_error = "largest eigenvalue change " + std::to_string(last) + " Ha after " + std::to_string(it) +
+                    " iterations (k-set " + std::to_string(last_ks) + ", band " + std::to_string(last_b) + ")";
   return converged ? DEREK_OK : DEREK_ERR_NOT_CONVERGED;
 }
 

@@ -245,10 +245,16 @@ int derek_gpu_get_density(derek_gpu_t *h, int sys, double *rho /* nr */);
  * keys Source/io.f90:519-527, DOS grid key dos_kpt_mp_grid io.f90:111):
  * Chebyshev-filtered subspace iterations of degree cheb_degree in the
  * potential set with derek_gpu_set_vloc (e.g. a converged one), from the
- * start vectors of init_vectors, until no reported eigenvalue of any
- * k-point moves by eig_tol between iterations.  Eigenvalues through
+ * start vectors of init_vectors, until none of the lowest nconv reported
+ * eigenvalues (0: all reported) of any k-point moves by eig_tol between
+ * iterations.  Bands just below the top of the carried subspace converge
+ * slowly (raise buffer_bands for them).  On the mixed path the split-BF16
+ * tensor-core products (about 16 significant bits per operand) make the
+ * Ritz values move by ~1e-5 relative between iterations; use_tensor_cores
+ * = 0 (FP32 CUDA-core products, ~1e-7) allows tighter eig_tol.  On failure
+ * the last error names the largest remaining change.  Eigenvalues through
  * derek_gpu_get_eigenvalues.  *iterations may be NULL. */
-int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int *iterations);
+int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, int *iterations);
 
 /* Restart: the next scf_run starts system `sys` from this density (nr FP64
  * values, the reference's flat z-fastest order) instead of the uniform one;
