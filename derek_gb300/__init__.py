@@ -44,6 +44,28 @@ class SystemSpec:
         self.grid_policy = int(grid_policy)
         self.g_fine_scale = float(g_fine_scale)
 
+    @classmethod
+    def from_info(cls, path):
+        """The system a .info file describes (read_info), with the
+        reference's own grid rule (Source/basis.f90:87-105) and its
+        Monkhorst-Pack k-points (Source/io.f90:2016-2031).  A gaussian_pot
+        block's rows (centre, height, width) become this build's Gaussian
+        wells of depth `height`; the reference evaluates that potential to
+        zero (Source/pot.f90:165-166).  kT must be positive here (Fermi
+        smearing), so electronic_temp 0, the reference default, is refused."""
+        p = read_info(path)
+        if not p["electronic_temp"] > 0:
+            raise ValueError("electronic_temp must be > 0 (the SCF uses Fermi-Dirac occupations)")
+        from .workloads import mp_grid
+        wells = None
+        if p["external_pot"] == "gaussian_pot" and p["n_pots"] > 0:
+            n = p["n_pots"]
+            c = np.asarray(p["pot_centres"][:3 * n]).reshape(n, 3)
+            wells = np.column_stack([c, p["pot_heights"][:n], p["pot_widths"][:n]])
+        return cls(np.asarray(p["cell"]).reshape(3, 3, order="F"), p["cut_off_energy"],
+                   mp_grid(p["kpt_mp_grid"]), p["nbands"], float(p["n_electrons"]), kT=p["electronic_temp"],
+                   wells=wells, grid_policy=DEREK_GRID_REFERENCE, g_fine_scale=p["g_fine_scale"])
+
     def to_desc(self, keep):
         d = _abi.SysDesc()
         # column-major storage of cell(3,3): cell[3*j+i] = cell(i+1, j+1)
@@ -360,6 +382,29 @@ def dos_gaussian(eig, wk, energies, sigma):
     e = np.asarray(energies, dtype=np.float64)[:, None, None]
     g = np.exp(-0.5 * ((e - np.asarray(eig)[None]) / sigma) ** 2) / (sigma * np.sqrt(2 * np.pi))
     return 2.0 * np.einsum("ekb,k->e", g, np.asarray(wk, dtype=np.float64))
+
+
+def read_info(path):
+    """A .info parameter file read as the reference reads it (derek_info_read):
+    every parameter by name, in Ha and bohr after the unit conversions;
+    'corrected' lists the keys the spell check corrected.  Raises DerekError
+    with the reference's message on a bad file."""
+    p = _abi.InfoParams()
+    msg = ctypes.create_string_buffer(512)
+    st = lib.derek_info_read(str(path).encode(), ctypes.byref(p), msg, 512)
+    if st != 0:
+        raise DerekError(st, f"read_info: {msg.value.decode()}")
+    out = {}
+    for name, t in _abi.InfoParams._fields_:
+        v = getattr(p, name)
+        if t is _abi._c32:
+            out[name] = bytes(v).split(b"\0", 1)[0].decode()
+        elif hasattr(v, "__len__"):
+            out[name] = list(v)
+        else:
+            out[name] = v
+    out["corrected"] = msg.value.decode()
+    return out
 
 
 # ---- the reference's files (host only)

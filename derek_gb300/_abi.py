@@ -44,6 +44,30 @@ class SysDesc(ctypes.Structure):
     ]
 
 
+_c32 = ctypes.c_char * 32
+
+
+class InfoParams(ctypes.Structure):
+    """derek_info (include/derek_gpu.h)."""
+    _fields_ = (
+        [(n, _i) for n in ("check", "debugging", "n_electrons", "max_scf", "conduction_bands", "nbands",
+                           "iprint", "random_seed", "write_wvfn", "soc", "write_density", "write_potential",
+                           "write_state", "write_spec", "write_memory", "write_formatted_potential",
+                           "write_potex", "write_formatted_density", "restart", "write_formatted_potex",
+                           "write_xsf")]
+        + [(n, _i * 3) for n in ("kpt_mp_grid", "periodic_pot_grid", "dos_kpt_mp_grid")]
+        + [(n, _d) for n in ("energy_tol", "cut_off_energy", "g_fine_scale", "electronic_temp",
+                             "finite_barrier_height")]
+        + [("finite_barrier_width", _d * 3), ("periodic_pot_amp", _d), ("ext_efield", _d * 3),
+           ("ext_bfield", _d * 3)]
+        + [(n, _c32) for n in ("xc_functional", "task", "scf_method", "external_pot", "output_level",
+                               "unit_energy", "unit_length", "unit_efield", "unit_bfield", "out_energy_unit",
+                               "out_len_unit", "out_efield_unit", "out_bfield_unit")]
+        + [("cell", _d * 9), ("n_pots", _i), ("pot_centres", _d * 192), ("pot_heights", _d * 64),
+           ("pot_widths", _d * 64), ("n_corrected", _i)]
+    )
+
+
 class ScfOpts(ctypes.Structure):
     _fields_ = [
         ("precision", _i), ("mix_alpha", _d), ("kerker_q0", _d), ("pulay_history", _i),
@@ -101,6 +125,7 @@ SIGNATURES = {
     "derek_gpu_launch_count": (ctypes.c_ulonglong, []),
     "derek_gpu_time_apply_h": (_i, [_vp, _i, _pd, _pd]),
     "derek_gpu_set_start_density": (_i, [_vp, _i, _pd]),
+    "derek_info_read": (_i, [ctypes.c_char_p, ctypes.POINTER(InfoParams), ctypes.c_char_p, _i]),
     "derek_gpu_nscf_run": (_i, [_vp, _i, _d, _i, ctypes.POINTER(_i)]),
     "derek_io_write_den": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd, _pd]),
     "derek_io_read_den": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _pd, _pd]),

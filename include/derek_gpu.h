@@ -291,6 +291,36 @@ int derek_io_write_xsf(const char *path, const double cell[9], const int n_fine[
 /* Test hook: largest subrecord in bytes (0 = gfortran's 2147483639). */
 int derek_io_set_subrecord_limit(long long bytes);
 
+/* A .info parameter file read as the reference reads it (Source/io.f90
+ * io_read_param 360-830, io_freeform_read 836-882, io_block_parse
+ * 1765-1937, spell check 2545-2630, io_initialise 299-353 with
+ * Source/units.f90 and CODATA 2018, Source/constants.f90:70-104): every key
+ * of io.f90:116-162 with its default, the lattice and gaussian_pot /
+ * lorentzian_pot blocks, keys within Levenshtein distance 1-2 corrected,
+ * output_level's write flags, and the unit conversions.  Units accepted:
+ * length bohr m cm mm mum nm A pm; energy Ha mHa eV meV Ry mRy J Hz MHz GHz
+ * THz cm-1; K; fields Ha/Bohr/e eV/A/e N/C T G agr.  On error the message
+ * holds the reference's error text; on success the keys it corrected. */
+typedef struct {
+  int    check, debugging, n_electrons, max_scf, conduction_bands, nbands, iprint, random_seed;
+  int    write_wvfn, soc, write_density, write_potential, write_state, write_spec, write_memory,
+         write_formatted_potential, write_potex, write_formatted_density, restart,
+         write_formatted_potex, write_xsf;
+  int    kpt_mp_grid[3], periodic_pot_grid[3], dos_kpt_mp_grid[3];
+  double energy_tol, cut_off_energy, g_fine_scale;       /* Ha, Ha, - */
+  double electronic_temp;                                /* kT in Ha */
+  double finite_barrier_height, finite_barrier_width[3], periodic_pot_amp;   /* Ha, bohr, Ha */
+  double ext_efield[3], ext_bfield[3];                   /* atomic units */
+  char   xc_functional[32], task[32], scf_method[32], external_pot[32], output_level[32],
+         unit_energy[32], unit_length[32], unit_efield[32], unit_bfield[32],
+         out_energy_unit[32], out_len_unit[32], out_efield_unit[32], out_bfield_unit[32];
+  double cell[9];          /* bohr, column-major cell(3,3), cell(i,:) lattice vector i */
+  int    n_pots;           /* rows of a gaussian_pot / lorentzian_pot block (<= 64) */
+  double pot_centres[3 * 64], pot_heights[64], pot_widths[64];   /* fractional, Ha, bohr */
+  int    n_corrected;      /* keys corrected by the spell check */
+} derek_info;
+int derek_info_read(const char *path, derek_info *out, char *message, int message_len);
+
 /* Host-only helpers (no GPU needed): the grid and sphere rules the handle
  * uses, exposed so drivers and tests can check them on any machine. */
 int derek_host_prime_fact(int n);  /* Source/basis.f90:257-309 */
