@@ -44,6 +44,7 @@ ERRORS = {
     "no_separator": "max_scf 4\n" + LATTICE,
     "lattice_key": "lattice : 3\n" + LATTICE,
     "unit": "unit_energy : furlong\n" + LATTICE,
+    "short_list": "kpt_mp_grid : 2 2\n" + LATTICE,   # fewer values than the array and no '/' 
 }
 
 
