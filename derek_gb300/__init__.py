@@ -28,7 +28,7 @@ class SystemSpec:
 
     def __init__(self, cell, ecut, kpts, nbands, nelec, kT=0.01, wk=None, vext=None,
                  wells=None, n_fine=None, grid_policy=DEREK_GRID_SMOOTH23, g_fine_scale=2.0,
-                 inv_cell=None):
+                 inv_cell=None, nspinor=1):
         self.cell = np.asarray(cell, dtype=np.float64).reshape(3, 3)
         self.inv_cell = None if inv_cell is None else np.asarray(inv_cell, dtype=np.float64).reshape(3, 3)
         self.ecut = float(ecut)
@@ -43,6 +43,7 @@ class SystemSpec:
         self.n_fine = (0, 0, 0) if n_fine is None else tuple(int(x) for x in n_fine)
         self.grid_policy = int(grid_policy)
         self.g_fine_scale = float(g_fine_scale)
+        self.nspinor = int(nspinor)
 
     @classmethod
     def from_info(cls, path):
@@ -86,7 +87,7 @@ class SystemSpec:
             keep.append(self.wk)
             d.wk = self.wk.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         d.nbands = self.nbands
-        d.nspinor = 1
+        d.nspinor = self.nspinor
         d.nelec = self.nelec
         d.kT = self.kT
         if self.vext is not None:
@@ -200,17 +201,22 @@ class Handle:
         _check(lib.derek_gpu_set_wfn(self._h, sys, k, psi.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
                self._h, "set_wfn")
 
+    def _wfn_shape(self, sys, k):
+        """(nbands, npw), or (2, nbands, npw) = coeff(gvec, band, spinor) of
+        one k-point for a spinor system (Source/wave.f90:30)."""
+        s = self.systems[sys]
+        shape = (s.nbands, self.npw(sys, k))
+        return shape if s.nspinor == 1 else (2,) + shape
+
     def get_wfn(self, sys=0, k=0):
-        nb = self.systems[sys].nbands
-        psi = np.zeros((nb, self.npw(sys, k)), dtype=np.complex128)
+        psi = np.zeros(self._wfn_shape(sys, k), dtype=np.complex128)
         _check(lib.derek_gpu_get_wfn(self._h, sys, k, psi.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
                self._h, "get_wfn")
         return psi
 
     def pot_apply_wfn(self, sys=0, k=0):
         """H psi of the stored wavefunctions (pot_apply_wfn + kinetic)."""
-        nb = self.systems[sys].nbands
-        out = np.zeros((nb, self.npw(sys, k)), dtype=np.complex128)
+        out = np.zeros(self._wfn_shape(sys, k), dtype=np.complex128)
         _check(lib.derek_gpu_apply_h(self._h, sys, k, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
                self._h, "apply_h")
         return out
@@ -223,6 +229,36 @@ class Handle:
         rho = np.zeros(int(np.prod(nf)))
         _check(lib.derek_gpu_density(self._h, sys, _dptr(occ), _dptr(rho)), self._h, "density")
         return rho
+
+    def density_spinor(self, occ, sys=0):
+        """(n, m) of a spinor system: n(r) and the magnetisation m = (mx, my,
+        mz)(r), shape (3, nr), the reference's den%charge / den%spin
+        (Source/density.f90:63-64)."""
+        s = self.systems[sys]
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.float64).reshape(len(s.kpts), s.nbands))
+        nf, _ = self.grid(sys)
+        nr = int(np.prod(nf))
+        rho = np.zeros(nr)
+        mag = np.zeros((3, nr))
+        _check(lib.derek_gpu_density_spinor(self._h, sys, _dptr(occ), _dptr(rho), _dptr(mag)),
+               self._h, "density_spinor")
+        return rho, mag
+
+    def set_nc_pot(self, nc_pot, sys=0):
+        """The 2x2 potential of a spinor system, nc_pot[n, i, j] (nr, 2, 2)
+        complex as Source/pot.f90:33 holds it: V I + mu_B sigma.B."""
+        a = np.asarray(nc_pot, dtype=np.complex128)
+        f = np.ascontiguousarray(a.reshape(-1, 2, 2).transpose(2, 1, 0))   # [j][i][n]: n fastest
+        _check(lib.derek_gpu_set_nc_pot(self._h, sys, f.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+               self._h, "set_nc_pot")
+
+    def get_nc_pot(self, sys=0):
+        nf, _ = self.grid(sys)
+        nr = int(np.prod(nf))
+        f = np.zeros((2, 2, nr), dtype=np.complex128)
+        _check(lib.derek_gpu_get_nc_pot(self._h, sys, f.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+               self._h, "get_nc_pot")
+        return np.ascontiguousarray(f.transpose(2, 1, 0))
 
     def xc_lda(self, rho):
         rho = np.ascontiguousarray(np.asarray(rho, dtype=np.float64))

@@ -202,6 +202,7 @@ using namespace derek;
 extern "C" int derek_gpu_grad_density_loss(derek_gpu_t *h, int s, const double *n_target,
                                            double *loss, double *grad, int max_iter, double tol) {
   if (!h || s < 0 || s >= h->nsys || !n_target || !grad) return DEREK_ERR_BAD_ARG;
+  if (reject_spinor(h, "grad_density_loss")) return DEREK_ERR_UNSUPPORTED;
   if (h->prec != DEREK_PREC_FP64 || h->nsys != 1) {
     h->last_error = "the adjoint gradient needs an FP64 handle over one system";
     return DEREK_ERR_UNSUPPORTED;

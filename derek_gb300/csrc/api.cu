@@ -119,6 +119,70 @@ int density_items(derek_gpu *h, const void *psi, double *rho) {
   return DEREK_OK;
 }
 
+// H.psi of every band of k-set ki of a spinor system: x-line passes per
+// component, the 2x2 plane pass per band
+template <typename R> static void apply_spinor_t(derek_gpu *h, int ki, const void *in, void *out) {
+  const KSetDev &K = h->ks[ki];
+  const SysDev &S = h->sys[K.sys];
+  const int nchunk = (K.ncol + kColChunk - 1) / kColChunk;
+  const cplx<R> *vnc;
+  if constexpr (std::is_same<R, double>::value)
+    vnc = h->d_vnc64;
+  else
+    vnc = h->d_vnc32;
+  launch_x_inv_lines<R>(h->tab, K.item0, K.nb, nchunk, S.n[0], S.n[0], (const cplx<R> *)in,
+                        (cplx<R> *)h->d_abuf, nullptr, h->stream);
+  launch_plane_spinor<R>(h->tab, K.item0, K.nb, S.n, (cplx<R> *)h->d_abuf, vnc, h->stream);
+  launch_x_fwd_lines<R>(h->tab, K.item0, K.nb, nchunk, S.n[0], S.n[0], (const cplx<R> *)h->d_abuf,
+                        (const cplx<R> *)in, nullptr, (cplx<R> *)out, nullptr, h->stream);
+}
+
+int apply_spinor_items(derek_gpu *h, int ki, const void *in, void *out) {
+  if (h->prec == DEREK_PREC_FP64)
+    apply_spinor_t<double>(h, ki, in, out);
+  else
+    apply_spinor_t<float>(h, ki, in, out);
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+// n and m of every active spinor system from psi and per-item weights
+// h->d_occw: rho gets n, h->d_mag the three components of m
+template <typename R> static void density_spinor_t(derek_gpu *h, const void *psi) {
+  for (const auto &c : h->classes) {
+    Tables t = h->tab;
+    t.item_list = c.d_list;
+    launch_x_inv_lines<R>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], (const cplx<R> *)psi,
+                          (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
+  }
+  launch_density_spinor<R>(h->tab, h->nks, h->max_n, (const cplx<R> *)h->d_abuf, h->d_occw,
+                           h->d_partial, h->d_partial_off, h->stream);
+}
+
+int density_spinor_items(derek_gpu *h, const void *psi, double *rho) {
+  if (h->prec == DEREK_PREC_FP64)
+    density_spinor_t<double>(h, psi);
+  else
+    density_spinor_t<float>(h, psi);
+  for (int s = 0; s < h->nsys; ++s) {
+    const SysDev &S = h->sys[s];
+    if (S.nspinor != 2) continue;
+    for (int c = 0; c < 4; ++c)
+      derek::note_launch(),
+          k_reduce_partials<<<152, 256, 0, h->stream>>>(h->d_sys, h->d_ks, s, h->d_partial + c * (long long)S.nr,
+                                                       h->d_partial_off,
+                                                       c == 0 ? rho : h->d_mag + (c - 1) * h->total_grid);
+  }
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+bool reject_spinor(derek_gpu *h, const char *what) {
+  if (!h->any_spinor) return false;
+  h->last_error = std::string(what) + ": spinor (nspinor = 2) systems support H.psi, overlaps and densities only";
+  return true;
+}
+
 int refresh_vloc32(derek_gpu *h) {
   if (h->prec != DEREK_PREC_FP64)
     derek::note_launch(), k_to_float<<<152 * 4, 256, 0, h->stream>>>(h->total_grid, h->d_vloc, h->d_vloc32);
@@ -192,7 +256,7 @@ int derek_gpu_destroy(derek_gpu_t *h) {
                   h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
                   h->d_Yp,    h->d_HX,      h->d_abuf,    h->d_occw,      h->d_eig,
                   h->d_occ,   h->d_coef,    h->d_cells,   h->d_wells,     h->d_well_off,
-                  h->d_hfpart, h->d_hfgrad};
+                  h->d_hfpart, h->d_hfgrad, h->d_vnc64, h->d_vnc32, h->d_mag};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (auto &c : h->classes)
@@ -245,10 +309,11 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
             part_off = 0;
   for (int s = 0; s < nsys; ++s) {
     const derek_sys_desc &d = desc[s];
-    if (d.nspinor != 1) FAIL(DEREK_ERR_UNSUPPORTED, "nspinor must be 1");
+    if (d.nspinor != 1 && d.nspinor != 2) FAIL(DEREK_ERR_UNSUPPORTED, "nspinor must be 1 or 2");
     if (d.nk <= 0 || !d.kpts || d.nbands <= 0 || d.ecut <= 0 || !(d.kT > 0) || d.nelec <= 0)
       FAIL(DEREK_ERR_BAD_ARG, "system " + std::to_string(s) + ": bad sizes");
-    if (d.nelec > 2.0 * d.nbands) FAIL(DEREK_ERR_BAD_ARG, "more electrons than 2 * nbands");
+    // a scalar band holds two electrons, a spinor band one
+    if (d.nelec > (3 - d.nspinor) * (double)d.nbands) FAIL(DEREK_ERR_BAD_ARG, "more electrons than the bands hold");
     SysDev S{};
     double inv[9];
     bool have_inv = false;
@@ -274,6 +339,9 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       const size_t es = h->prec == DEREK_PREC_FP64 ? 16 : 8;
       const size_t need = (size_t)nfine[1] * nfine[2] * 8 + ((size_t)nfine[1] * (nfine[2] + 1) + 2 * kMaxDim) * es;
       if (need > 227 * 1024) FAIL(DEREK_ERR_UNSUPPORTED, "grid planes exceed shared memory");
+      // spinor passes hold both components' planes
+      if (d.nspinor == 2 && spinor_plane_smem(nfine[1], nfine[2], es) > 227 * 1024)
+        FAIL(DEREK_ERR_UNSUPPORTED, "spinor grid planes exceed shared memory");
     }
     for (int i = 0; i < 3; ++i) {
       S.n[i] = nfine[i];
@@ -306,9 +374,12 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     S.nr = nfine[0] * nfine[1] * nfine[2];
     S.nk = d.nk;
     const int nbuf = h->opts.buffer_bands >= 0 ? h->opts.buffer_bands : std::max(4, (d.nbands + 19) / 20);
-    const int nbi = d.nbands + nbuf;
+    // a spinor band is two items (up, down): counts below are items
+    const int nbi = d.nspinor * (d.nbands + nbuf);
     S.nb = nbi;
-    S.nbr = d.nbands;
+    S.nbr = d.nspinor * d.nbands;
+    S.nspinor = d.nspinor;
+    h->any_spinor |= d.nspinor == 2;
     S.ks0 = (int)h->ks.size();
     S.active = 1;
     S.volume = cell_volume(d.cell);
@@ -341,7 +412,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       K.npw = npw;
       K.npw_pad = (npw + 31) / 32 * 32;
       K.nb = nbi;
-      K.nbr = d.nbands;
+      K.nbr = S.nbr;
       K.wk = d.wk ? d.wk[k] : 1.0 / d.nk;
       for (int i = 0; i < 3; ++i) K.kfrac[i] = d.kpts[3 * k + i];
       if (sp.mx.back() - sp.mx.front() + 1 > nfine[0]) FAIL(DEREK_ERR_BAD_ARG, "sphere wider than the fine grid");
@@ -407,7 +478,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       psi_off += (long long)nbi * K.npw_pad;
       a_off += (long long)nbi * nfine[0] * K.ncol_pad;
       partial_off.push_back(part_off);
-      part_off += S.nr;
+      part_off += (d.nspinor == 2 ? 4 : 1) * (long long)S.nr;
       {
         // plane-wave start vectors: the nbi lowest kinetic energies of the
         // k-point (ties by entry index), entries in column order
@@ -483,6 +554,24 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   CK(cudaMalloc((void **)&h->d_vxc, gbytes));
   CK(cudaMalloc((void **)&h->d_cgrid, (size_t)grid_off * sizeof(double2)));
   CK(cudaMalloc((void **)&h->d_partial, (size_t)std::max<long long>(part_off, 1) * sizeof(double)));
+  if (h->any_spinor) {
+    // nc_pot starts as V_ext on the diagonal (Source/pot.f90:133-166)
+    std::vector<double2> vnc((size_t)4 * grid_off, make_double2(0.0, 0.0));
+    for (int s = 0; s < nsys; ++s) {
+      const SysDev &S = h->sys[s];
+      if (S.nspinor != 2) continue;
+      for (long long i = 0; i < S.nr; ++i) {
+        const double v = h->vext_host[S.grid_off + i];
+        vnc[4 * (S.grid_off + i)] = make_double2(v, 0.0);
+        vnc[4 * (S.grid_off + i) + 3] = make_double2(v, 0.0);
+      }
+    }
+    std::vector<float2> vnc32(vnc.size());
+    for (size_t i = 0; i < vnc.size(); ++i) vnc32[i] = make_float2((float)vnc[i].x, (float)vnc[i].y);
+    CK(upload(&h->d_vnc64, vnc));
+    CK(upload(&h->d_vnc32, vnc32));
+    CK(cudaMalloc((void **)&h->d_mag, (size_t)3 * grid_off * sizeof(double)));
+  }
   const size_t pbytes = (size_t)h->total_psi * h->elem_size();
   CK(cudaMalloc(&h->d_X, pbytes));
   CK(cudaMalloc(&h->d_Y, pbytes));
@@ -565,8 +654,8 @@ int derek_gpu_grid(derek_gpu_t *h, int s, int n_fine[3], int n_std[3]) {
 
 int derek_gpu_bands(derek_gpu_t *h, int s, int *nb, int *nbi) {
   if (!check_sys(h, s)) return DEREK_ERR_BAD_ARG;
-  if (nb) *nb = h->sys[s].nbr;
-  if (nbi) *nbi = h->sys[s].nb;
+  if (nb) *nb = h->sys[s].nbr / h->sys[s].nspinor;
+  if (nbi) *nbi = h->sys[s].nb / h->sys[s].nspinor;
   return DEREK_OK;
 }
 
@@ -605,6 +694,19 @@ int derek_gpu_fft3d(derek_gpu_t *h, int s, double *inout, int dir) {
   return DEREK_OK;
 }
 
+// write system s's 2x2 potential, given per point as V11, V21, V12, V22
+static int upload_nc(derek_gpu_t *h, int s, const std::vector<double2> &vnc) {
+  const SysDev &S = h->sys[s];
+  std::vector<float2> v32(vnc.size());
+  for (size_t i = 0; i < vnc.size(); ++i) v32[i] = make_float2((float)vnc[i].x, (float)vnc[i].y);
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_vnc64 + 4 * S.grid_off, vnc.data(), vnc.size() * sizeof(double2),
+                                cudaMemcpyHostToDevice, h->stream));
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_vnc32 + 4 * S.grid_off, v32.data(), v32.size() * sizeof(float2),
+                                cudaMemcpyHostToDevice, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
 int derek_gpu_set_vloc(derek_gpu_t *h, int s, const double *v) {
   if (!check_sys(h, s) || !v) return DEREK_ERR_BAD_ARG;
   const SysDev &S = h->sys[s];
@@ -612,7 +714,47 @@ int derek_gpu_set_vloc(derek_gpu_t *h, int s, const double *v) {
                                 cudaMemcpyHostToDevice, h->stream));
   int st = refresh_vloc32(h);
   if (st) return st;
+  if (S.nspinor == 2) {
+    // a spin-independent potential: V on the diagonal of nc_pot
+    std::vector<double2> vnc((size_t)4 * S.nr, make_double2(0.0, 0.0));
+    for (long long i = 0; i < S.nr; ++i) vnc[4 * i] = vnc[4 * i + 3] = make_double2(v[i], 0.0);
+    return upload_nc(h, s, vnc);
+  }
   DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int derek_gpu_set_nc_pot(derek_gpu_t *h, int s, const double *nc_pot) {
+  if (!check_sys(h, s) || !nc_pot) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  if (S.nspinor != 2) {
+    h->last_error = "set_nc_pot: system is not a spinor system (nspinor = 1)";
+    return DEREK_ERR_BAD_ARG;
+  }
+  // reference order nc_pot(n, i, j): component c = i + 2 j is plane c of nr values
+  std::vector<double2> vnc((size_t)4 * S.nr);
+  for (int c = 0; c < 4; ++c)
+    for (long long i = 0; i < S.nr; ++i)
+      vnc[4 * i + c] = make_double2(nc_pot[2 * (c * S.nr + i)], nc_pot[2 * (c * S.nr + i) + 1]);
+  return upload_nc(h, s, vnc);
+}
+
+int derek_gpu_get_nc_pot(derek_gpu_t *h, int s, double *nc_pot) {
+  if (!check_sys(h, s) || !nc_pot) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  if (S.nspinor != 2) {
+    h->last_error = "get_nc_pot: system is not a spinor system (nspinor = 1)";
+    return DEREK_ERR_BAD_ARG;
+  }
+  std::vector<double2> vnc((size_t)4 * S.nr);
+  DEREK_CUDA(h, cudaMemcpyAsync(vnc.data(), h->d_vnc64 + 4 * S.grid_off, vnc.size() * sizeof(double2),
+                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (int c = 0; c < 4; ++c)
+    for (long long i = 0; i < S.nr; ++i) {
+      nc_pot[2 * (c * S.nr + i)] = vnc[4 * i + c].x;
+      nc_pot[2 * (c * S.nr + i) + 1] = vnc[4 * i + c].y;
+    }
   return DEREK_OK;
 }
 
@@ -637,14 +779,17 @@ int derek_gpu_get_vloc(derek_gpu_t *h, int s, double *v) {
   return DEREK_OK;
 }
 
-// copy between a host complex128 [nbr][npw] slice in the reference's G order
-// and the padded, column-ordered device buffer (only the requested bands;
-// buffer bands stay on the device)
+// copy between a host complex128 [nspinor][nbr][npw] slice in the
+// reference's G order (coeff(gvec, band, spinor) of one k-point) and the
+// padded, column-ordered device buffer, where band b's spinor s is row
+// nspinor * b + s (only the requested bands; buffer bands stay on the device)
 static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool to_dev) {
   const KSetDev &K = h->ks[ki];
   const size_t es = h->elem_size();
   char *dev = (char *)dev_base + (size_t)K.psi_off * es;
   const int nb = K.nbr;
+  const int nsp = h->sys[K.sys].nspinor;
+  auto host_row = [nb, nsp](int p) { return nsp == 1 ? p : (p % 2) * (nb / 2) + p / 2; };
   const size_t n = (size_t)nb * K.npw_pad;
   const int32_t *perm = h->perm.data() + K.ent_off;
   const bool f64 = h->prec == DEREK_PREC_FP64;
@@ -653,7 +798,7 @@ static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool
   if (to_dev) {
     for (int b = 0; b < nb; ++b)
       for (int g = 0; g < K.npw; ++g) {
-        const size_t src = 2 * ((size_t)b * K.npw + perm[g]);
+        const size_t src = 2 * ((size_t)host_row(b) * K.npw + perm[g]);
         const size_t dst = 2 * ((size_t)b * K.npw_pad + g);
         if (f64) {
           t64[dst] = host[src];
@@ -672,7 +817,7 @@ static int copy_slice(derek_gpu_t *h, int ki, void *dev_base, double *host, bool
     DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
     for (int b = 0; b < nb; ++b)
       for (int g = 0; g < K.npw; ++g) {
-        const size_t dst = 2 * ((size_t)b * K.npw + perm[g]);
+        const size_t dst = 2 * ((size_t)host_row(b) * K.npw + perm[g]);
         const size_t src = 2 * ((size_t)b * K.npw_pad + g);
         host[dst] = f64 ? t64[src] : (double)t32[src];
         host[dst + 1] = f64 ? t64[src + 1] : (double)t32[src + 1];
@@ -697,13 +842,15 @@ int derek_gpu_apply_h(derek_gpu_t *h, int s, int k, double *hpsi) {
   int ki = ks_index(h, s, k);
   if (ki < 0 || !hpsi) return DEREK_ERR_BAD_ARG;
   const KSetDev &K = h->ks[ki];
-  int st = apply_h_items(h, K.item0, K.nb, h->cur_psi(), nullptr, h->d_HX, nullptr);
+  int st = h->sys[s].nspinor == 2 ? apply_spinor_items(h, ki, h->cur_psi(), h->d_HX)
+                                  : apply_h_items(h, K.item0, K.nb, h->cur_psi(), nullptr, h->d_HX, nullptr);
   if (st) return st;
   return copy_slice(h, ki, h->d_HX, hpsi, false);
 }
 
 int derek_gpu_density(derek_gpu_t *h, int s, const double *occ, double *rho) {
   if (!check_sys(h, s) || !occ || !rho) return DEREK_ERR_BAD_ARG;
+  if (h->sys[s].nspinor == 2) return derek_gpu_density_spinor(h, s, occ, rho, nullptr);
   const SysDev &S = h->sys[s];
   // per-item weights w_k f / Omega for this system, zero elsewhere
   std::vector<double> w(h->nitems, 0.0);
@@ -724,6 +871,42 @@ int derek_gpu_density(derek_gpu_t *h, int s, const double *occ, double *rho) {
   if (st) return st;
   DEREK_CUDA(h, cudaMemcpyAsync(rho, h->d_rho_out + S.grid_off, (size_t)S.nr * sizeof(double),
                                 cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int derek_gpu_density_spinor(derek_gpu_t *h, int s, const double *occ, double *rho, double *mag) {
+  if (!check_sys(h, s) || !occ || (!rho && !mag)) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  if (S.nspinor != 2) {
+    h->last_error = "density_spinor: system is not a spinor system (nspinor = 1)";
+    return DEREK_ERR_BAD_ARG;
+  }
+  // per-item weights w_k f / Omega, equal on both components of a band
+  const int nbr = S.nbr / 2;
+  std::vector<double> w(h->nitems, 0.0);
+  for (int k = 0; k < S.nk; ++k) {
+    const KSetDev &K = h->ks[S.ks0 + k];
+    for (int b = 0; b < nbr; ++b)
+      w[K.item0 + 2 * b] = w[K.item0 + 2 * b + 1] = K.wk * occ[(size_t)k * nbr + b] / S.volume;
+  }
+  std::vector<SysDev> masked = h->sys;
+  for (int i = 0; i < h->nsys; ++i) masked[i].active = (i == s) && h->sys[i].active;
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, masked.data(), masked.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_occw, w.data(), w.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, h->stream));
+  int st = density_spinor_items(h, h->cur_psi(), h->d_rho_out);
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
+  if (st) return st;
+  if (rho)
+    DEREK_CUDA(h, cudaMemcpyAsync(rho, h->d_rho_out + S.grid_off, (size_t)S.nr * sizeof(double),
+                                  cudaMemcpyDeviceToHost, h->stream));
+  if (mag)
+    for (int c = 0; c < 3; ++c)
+      DEREK_CUDA(h, cudaMemcpyAsync(mag + (size_t)c * S.nr, h->d_mag + c * h->total_grid + S.grid_off,
+                                    (size_t)S.nr * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
   return DEREK_OK;
 }
@@ -785,6 +968,7 @@ unsigned long long derek_gpu_launch_count(void) { return launch_total(); }
 
 int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage) {
   if (!h || nrep <= 0) return DEREK_ERR_BAD_ARG;
+  if (reject_spinor(h, "time_apply_h")) return DEREK_ERR_UNSUPPORTED;
   cudaEvent_t ev[4];
   for (auto &e : ev) DEREK_CUDA(h, cudaEventCreate(&e));
   double tot[3] = {0, 0, 0};

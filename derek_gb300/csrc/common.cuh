@@ -58,10 +58,11 @@ struct SysDev {
   int n[3];
   int nr;
   int nk;
-  int nb;                  // bands carried (requested + buffer)
-  int nbr;                 // bands requested and reported
+  int nb;                  // bands carried (requested + buffer), x nspinor
+  int nbr;                 // bands requested and reported, x nspinor
   int ks0;                 // first k-set index of this system
   int active;              // 0 once converged (work items exit early)
+  int nspinor;             // 1, or 2: band b is items 2b (up) and 2b + 1 (down)
   double volume;
   double B[9];             // inv_cell, row-major: G_i = sum_j B[i*3+j] m_j
   double ecut;
@@ -80,8 +81,8 @@ struct KSetDev {
   int kidx;
   int npw;
   int npw_pad;
-  int nb;                  // bands carried (requested + buffer)
-  int nbr;                 // bands requested and reported
+  int nb;                  // bands carried (requested + buffer), x nspinor
+  int nbr;                 // bands requested and reported, x nspinor
   int ncol;                // (y,z) columns of the sphere
   int ncol_pad;
   int nrow;                // distinct y rows holding columns

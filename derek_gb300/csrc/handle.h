@@ -52,6 +52,12 @@ struct derek_gpu {
   double *d_vext = nullptr, *d_vloc = nullptr, *d_vhxc = nullptr;
   float *d_vloc32 = nullptr;
   double *d_rho_in = nullptr, *d_rho_out = nullptr;
+  // non-collinear systems: 2x2 potential per point (V11, V21, V12, V22) and
+  // the magnetisation (mx, my, mz grids of total_grid values each)
+  bool any_spinor = false;
+  double2 *d_vnc64 = nullptr;
+  float2 *d_vnc32 = nullptr;
+  double *d_mag = nullptr;
   std::vector<std::vector<double>> start_rho;   // per system: SCF start density (empty = uniform)
   double *d_exc = nullptr, *d_vxc = nullptr;
   double2 *d_cgrid = nullptr;      // complex work grid
@@ -137,5 +143,12 @@ int apply_h_items_ex(derek_gpu *h, const Tables &base, int item_begin, int nitem
 // Density of every active system from psi buffer `psi` and per-item weights
 // h->d_occw into rho (FP64 grids).
 int density_items(derek_gpu *h, const void *psi, double *rho);
+// Spinor systems: H.psi of every band of k-set ki (in -> out, no epilogue)
+// and n, m of every active spinor system (rho, h->d_mag).
+int apply_spinor_items(derek_gpu *h, int ki, const void *in, void *out);
+// True (with last_error set) when h holds a spinor system: the SCF, NSCF,
+// gradients and timing entry points run scalar systems only.
+bool reject_spinor(derek_gpu *h, const char *what);
+int density_spinor_items(derek_gpu *h, const void *psi, double *rho);
 
 }  // namespace derek

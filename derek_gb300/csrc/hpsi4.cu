@@ -439,6 +439,14 @@ void launch_x_inv(const Tables &t, int item_begin, int nitems, int max_nchunk, i
         launch_xinv_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, max_m, psi, abuf, occ_skip, st))
       return;
   }
+  launch_x_inv_lines<R>(t, item_begin, nitems, max_nchunk, max_n1, min_n1, psi, abuf, occ_skip, st);
+}
+
+template <typename R>
+void launch_x_inv_lines(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                        int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
+                        cudaStream_t st) {
+  if (nitems <= 0) return;
   const int n = max_n1 == min_n1 ? max_n1 : 0;
   if (n == 72) x_inv_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
   else if (n == 54) x_inv_go<R, 54>(t, item_begin, nitems, max_nchunk, max_n1, psi, abuf, occ_skip, st);
@@ -468,6 +476,14 @@ void launch_x_fwd(const Tables &t, int item_begin, int nitems, int max_nchunk, i
         launch_xfwd_reg(t, item_begin, nitems, max_nchunk * kCC, max_n1, max_m, abuf, psi, prev, out, coef, st))
       return;
   }
+  launch_x_fwd_lines<R>(t, item_begin, nitems, max_nchunk, max_n1, min_n1, abuf, psi, prev, out, coef, st);
+}
+
+template <typename R>
+void launch_x_fwd_lines(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                        int min_n1, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
+                        cplx<R> *out, const Axpby *coef, cudaStream_t st) {
+  if (nitems <= 0) return;
   const int n = max_n1 == min_n1 ? max_n1 : 0;
   if (n == 72) x_fwd_go<R, 72>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
   else if (n == 54) x_fwd_go<R, 54>(t, item_begin, nitems, max_nchunk, max_n1, abuf, psi, prev, out, coef, st);
@@ -555,6 +571,11 @@ void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, in
   template void launch_x_fwd<R>(const Tables &, int, int, int, int, int, int, const cplx<R> *,   \
                                 const cplx<R> *, const cplx<R> *, cplx<R> *, const Axpby *,      \
                                 cudaStream_t);                                                    \
+  template void launch_x_inv_lines<R>(const Tables &, int, int, int, int, int, const cplx<R> *,   \
+                                      cplx<R> *, const double *, cudaStream_t);                   \
+  template void launch_x_fwd_lines<R>(const Tables &, int, int, int, int, int, const cplx<R> *,   \
+                                      const cplx<R> *, const cplx<R> *, cplx<R> *, const Axpby *, \
+                                      cudaStream_t);                                              \
   template void launch_density_plane<R>(const Tables &, int, int, int, int, int, int, int, int,   \
                                         const cplx<R> *, const double *, double *,                \
                                         const long long *, cudaStream_t);

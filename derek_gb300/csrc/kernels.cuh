@@ -60,6 +60,33 @@ template <typename R>
 void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, int max_n2, int max_n3,
                           int min_n2, int min_n3, int max_m, const cplx<R> *abuf, const double *occ,
                           double *partial, const long long *partial_off, cudaStream_t st);
+// The x passes on shared-memory lines only (the layout k_plane and the
+// spinor passes read), never the FP32 register kernels' row layouts.
+template <typename R>
+void launch_x_inv_lines(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                        int min_n1, const cplx<R> *psi, cplx<R> *abuf, const double *occ_skip,
+                        cudaStream_t st);
+template <typename R>
+void launch_x_fwd_lines(const Tables &t, int item_begin, int nitems, int max_nchunk, int max_n1,
+                        int min_n1, const cplx<R> *abuf, const cplx<R> *psi, const cplx<R> *prev,
+                        cplx<R> *out, const Axpby *coef, cudaStream_t st);
+
+// Non-collinear spinors (spinor.cu).  Band b of a spinor system is items 2b
+// (up) and 2b + 1 (down), so a launch covers an even number of items starting
+// on a pair.  vnc holds the 2x2 potential per grid point as four complex
+// numbers V11, V21, V12, V22 (the reference's nc_pot(n, i, j) order).
+template <typename R>
+void launch_plane_spinor(const Tables &t, int item_begin, int nitems, const int n[3], cplx<R> *abuf,
+                         const cplx<R> *vnc, cudaStream_t st);
+// Charge and magnetisation partials per k-set: four planes (n, mx, my, mz)
+// of nr values at partial + partial_off[k-set], from the x-line buffer the
+// x_inv pass filled for the items with nonzero weight.
+template <typename R>
+void launch_density_spinor(const Tables &t, int nks, const int max_n[3], const cplx<R> *abuf,
+                           const double *occ, double *partial, const long long *partial_off,
+                           cudaStream_t st);
+size_t spinor_plane_smem(int n2, int n3, size_t elem);
+
 constexpr int kColChunk = 64;   // columns per x-line chunk (kCC in hpsi4.cu)
 
 // FP32 (y,z)-plane passes with register-resident line transforms

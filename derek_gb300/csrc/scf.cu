@@ -320,6 +320,24 @@ int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
   if (!h || s < 0 || s >= h->nsys || k < 0 || k >= h->sys[s].nk || !out) return DEREK_ERR_BAD_ARG;
   const int ki = h->sys[s].ks0 + k;
   const KSetDev &K = h->ks[ki];
+  if (h->sys[s].nspinor == 2) {
+    // a spinor band is one contiguous run of 2 npw_pad coefficients (up, then
+    // down, zero padded), so the overlap summed over spinors (wave_dot_wfn,
+    // Source/wave.f90:955) is the scalar overlap of nb / 2 such rows
+    const int nb = K.nb / 2, nbr = K.nbr / 2;
+    const long ld = 2L * K.npw_pad;
+    const char *x = (const char *)h->cur_psi() + (size_t)K.psi_off * h->elem_size();
+    int st = derek_gpu_overlap_noalloc(x, x, nb, (int)ld, ld, h->prec, h->d_S + h->mat_off[ki], h->stream);
+    if (st) {
+      if (st == DEREK_ERR_UNSUPPORTED) h->last_error = "overlap: spinor bands need nb <= 128 and 2 npw_pad <= 65536";
+      return st;
+    }
+    DEREK_CUDA(h, cudaMemcpy2DAsync(out, (size_t)nbr * sizeof(double2), h->d_S + h->mat_off[ki],
+                                    (size_t)nb * sizeof(double2), (size_t)nbr * sizeof(double2), nbr,
+                                    cudaMemcpyDeviceToHost, h->stream));
+    DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DEREK_OK;
+  }
   if (use_tc(h))
     launch_overlap_tc(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const float2 *)h->cur_psi(),
                       (const float2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S, h->d_mat_off,
@@ -343,6 +361,7 @@ int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
 
 int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
   if (!h) return DEREK_ERR_BAD_ARG;
+  if (reject_spinor(h, "scf_iterate")) return DEREK_ERR_UNSUPPORTED;
   int s = one_iteration(h, 0.0);
   if (s) return s;
   std::vector<SysState> st;
@@ -356,6 +375,7 @@ int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
 
 int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, int *iterations) {
   if (!h || max_iter <= 0 || !(eig_tol > 0) || nconv < 0) return DEREK_ERR_BAD_ARG;
+  if (reject_spinor(h, "nscf_run")) return DEREK_ERR_UNSUPPORTED;
   // frozen potential: the filter's upper bound from max V_loc of each system
   for (auto &s : h->sys) s.active = 1;
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
@@ -433,6 +453,7 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, 
 
 int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol, derek_scf_report *rep) {
   if (!h || max_scf <= 0 || !(etol > 0)) return DEREK_ERR_BAD_ARG;
+  if (reject_spinor(h, "scf_run")) return DEREK_ERR_UNSUPPORTED;
   h->scf_started = false;
   std::vector<SysState> st;
   for (int it = 0; it < max_scf; ++it) {
@@ -483,6 +504,7 @@ int derek_gpu_get_density(derek_gpu_t *h, int s, double *rho) {
 
 int derek_gpu_grad_wells(derek_gpu_t *h, int s, double *grad) {
   if (!h || s < 0 || s >= h->nsys || !grad) return DEREK_ERR_BAD_ARG;
+  if (reject_spinor(h, "grad_wells")) return DEREK_ERR_UNSUPPORTED;
   const int nw = h->well_off[s + 1] - h->well_off[s];
   if (nw == 0 || !h->wells_define_vext[s]) {
     h->last_error = "system has no Gaussian wells defining its external potential";

@@ -73,7 +73,8 @@ typedef struct {
   const double *kpts;      /* nk*3 fractional (reciprocal basis) */
   const double *wk;        /* nk weights summing to 1; NULL = uniform */
   int    nbands;           /* n_electrons + conduction_bands (io.f90:316) */
-  int    nspinor;          /* 1 (2 = non-collinear, not supported yet) */
+  int    nspinor;          /* 1, or 2: non-collinear spinor bands (H.psi,
+                              overlaps and densities; no SCF) */
   double nelec;            /* n_electrons */
   double kT;               /* electronic_temp converted to Ha, > 0 */
   const double *vext;      /* nr FP64 values, or NULL to build from wells */
@@ -166,6 +167,31 @@ int derek_gpu_apply_h(derek_gpu_t *h, int sys, int k, double *hpsi);
  * wavefunctions.  Replaces density_calculate (Source/density.f90:101-130);
  * occ is occ(nbands, nk) as state_data%occ (Source/state.f90:43). */
 int derek_gpu_density(derek_gpu_t *h, int sys, const double *occ, double *rho);
+
+/* Non-collinear spinor systems (nspinor = 2).  The reference carries two
+ * spinor components in every wavefunction, coeff(gvec, kpt, band, 1:2)
+ * (Source/wave.f90:30,164), a 2x2 potential nc_pot(nr, 2, 2)
+ * (Source/pot.f90:33,88) and a spin density den%spin(nr, 3)
+ * (Source/density.f90:63-64); the products on them are empty stubs there
+ * (pot_apply_wfn, Source/pot.f90:344-382; density_calculate,
+ * Source/density.f90:101-130).  On a spinor system:
+ *   set_wfn / get_wfn / apply_h take coeff(gvec, band, spinor) of one k,
+ *     complex128 [2][nbands][npw];
+ *   apply_h: (H psi)_s = T psi_s + sum_s' V_ss' psi_s' with V = nc_pot;
+ *   overlap: <psi_i|psi_j> summed over both spinors (wave_dot_wfn,
+ *     Source/wave.f90:955);
+ *   density(_spinor): n = sum w |u|^2 + |d|^2 and the magnetisation
+ *     m = sum w psi^H sigma psi = (2 Re u*d, 2 Im u*d, |u|^2 - |d|^2),
+ *     mag = [3][nr] real (den%spin(:, 1:3));
+ *   set_vloc(v) sets nc_pot = diag(v, v); set_nc_pot takes the reference's
+ *     nc_pot(nr, 2, 2) complex128 (element (n, i, j) at n + nr (i + 2 j)),
+ *     nc_pot = V I + mu_B sigma.B with mu_B = 1/2 (Source/xsf.f90:44-51).
+ * The SCF, NSCF, gradient and timing entry points return
+ * DEREK_ERR_UNSUPPORTED on a handle holding a spinor system. */
+int derek_gpu_set_nc_pot(derek_gpu_t *h, int sys, const double *nc_pot);
+int derek_gpu_get_nc_pot(derek_gpu_t *h, int sys, double *nc_pot);
+int derek_gpu_density_spinor(derek_gpu_t *h, int sys, const double *occ /* nk*nbands */,
+                             double *rho /* nr, or NULL */, double *mag /* 3*nr, or NULL */);
 
 /* LDA (Slater exchange + Perdew-Wang 92 correlation, libxc ids 1 + 12),
  * spin-unpolarised: exc = energy per particle, vxc = potential. */

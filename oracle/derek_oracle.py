@@ -436,6 +436,81 @@ def band_density(sys: System, kb: KBasis, psi: np.ndarray, weights: np.ndarray) 
     return rho / sys.volume
 
 
+# --------------------------------------------------------------------------
+# Non-collinear spinors: coeff(gvec, band, 1:2) (Source/wave.f90:30,164), the
+# 2x2 nc_pot (Source/pot.f90:33) and den%spin(nr, 3) (Source/density.f90:64).
+# The reference leaves the products on them as stubs; these are their
+# definitions, reducing to apply_h / band_density per component when nc_pot
+# is diag(V, V).
+# --------------------------------------------------------------------------
+
+MU_B = 0.5   # Bohr magneton in atomic units (Source/constants.f90:102)
+
+
+def nc_from_fields(v: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """nc_pot[n, i, j] = V I + mu_B sigma.B, the form whose components
+    Source/xsf.f90:44-51 reads back; b has shape (3, nr)."""
+    bx, by, bz = b
+    nc = np.empty((len(v), 2, 2), dtype=np.complex128)
+    nc[:, 0, 0] = v + MU_B * bz
+    nc[:, 1, 1] = v - MU_B * bz
+    nc[:, 0, 1] = MU_B * (bx - 1j * by)
+    nc[:, 1, 0] = MU_B * (bx + 1j * by)
+    return nc
+
+
+def nc_components(nc: np.ndarray):
+    """(V, Bx, By, Bz) of nc_pot as Source/xsf.f90:44-51 computes them."""
+    v = (nc[:, 0, 0] + nc[:, 1, 1]) / 2.0
+    bx = (nc[:, 0, 1] + nc[:, 1, 0]) / (MU_B * 2.0)
+    by = (nc[:, 0, 1] - nc[:, 1, 0]) / (-MU_B * 2j)
+    bz = (nc[:, 0, 0] - nc[:, 1, 1]) / (2.0 * MU_B)
+    return v, bx, by, bz
+
+
+def apply_h_spinor(sys: System, kb: KBasis, nc: np.ndarray, psi: np.ndarray) -> np.ndarray:
+    """H psi for spinor psi of shape (2, nb, npw):
+    (H psi)_s = 1/2|k+G|^2 psi_s + (1/N) F[sum_s' nc[:, s, s'] F^-1 psi_s']."""
+    N = sys.nr
+    out = np.empty_like(psi)
+    box = np.zeros(N, dtype=np.complex128)
+    for b in range(psi.shape[1]):
+        r = []
+        for sp in range(2):
+            box[:] = 0
+            box[kb.fidx] = psi[sp, b]
+            r.append(fft3d(box, sys.n_fine, -1))
+        for sp in range(2):
+            w = nc[:, sp, 0] * r[0] + nc[:, sp, 1] * r[1]
+            g = fft3d(w, sys.n_fine, 1)
+            out[sp, b] = kb.kinetic * psi[sp, b] + g[kb.fidx] / N
+    return out
+
+
+def spinor_density(sys: System, kb: KBasis, psi: np.ndarray, weights: np.ndarray):
+    """(n, m) with n = sum_b w_b (|u|^2 + |d|^2) / Omega and
+    m = sum_b w_b psi^H sigma psi / Omega, shape (3, nr)."""
+    N = sys.nr
+    n = np.zeros(N)
+    m = np.zeros((3, N))
+    box = np.zeros(N, dtype=np.complex128)
+    for b in range(psi.shape[1]):
+        if weights[b] == 0.0:
+            continue
+        r = []
+        for sp in range(2):
+            box[:] = 0
+            box[kb.fidx] = psi[sp, b]
+            r.append(fft3d(box, sys.n_fine, -1))
+        u, d = r
+        ud = np.conj(u) * d
+        n += weights[b] * (np.abs(u) ** 2 + np.abs(d) ** 2)
+        m[0] += weights[b] * 2.0 * ud.real
+        m[1] += weights[b] * 2.0 * ud.imag
+        m[2] += weights[b] * (np.abs(u) ** 2 - np.abs(d) ** 2)
+    return n / sys.volume, m / sys.volume
+
+
 def hartree(sys: System, rho: np.ndarray):
     """(V_H(r), E_H): V_H(G) = 4 pi n(G)/|G|^2 with G = 0 dropped,
     n(G) = F[n]/N, E_H = Omega/2 sum_G 4 pi |n(G)|^2/|G|^2."""

@@ -1,0 +1,235 @@
+"""Non-collinear spinor systems (nspinor = 2): H.psi with a 2x2 potential,
+charge and magnetisation densities, overlaps summed over spinors.
+
+The reference carries the data (coeff(gvec, kpt, band, 1:2), nc_pot(nr,2,2),
+den%spin(nr,3)) but leaves the products as stubs, so parity is against the
+oracle's restatement, which is pinned here by reduction to the scalar
+operations (nc_pot = diag(V, V)), Hermiticity, the V/B decomposition of
+Source/xsf.f90:44-51, and the exact Zeeman splitting of plane waves in a
+uniform field.  Tolerances as the scalar primitives: FP64 1e-11, mixed 2e-5
+relative (max-norm).
+"""
+import numpy as np
+import pytest
+
+FP64_TOL = 1e-11
+FP32_TOL = 2e-5
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def random_fields(rng, nr, scale=0.3):
+    return scale * rng.standard_normal(nr), scale * rng.standard_normal((3, nr))
+
+
+def random_spinors(rng, nb, npw):
+    return rng.standard_normal((2, nb, npw)) + 1j * rng.standard_normal((2, nb, npw))
+
+
+# ---- oracle pins (CPU)
+@pytest.fixture(scope="module")
+def small(oracle):
+    rng = np.random.default_rng(3)
+    s = oracle.make_system(5.0, 3.0, 2.0, 3, oracle.random_wells(rng, 2), kpts=[(0.1, -0.2, 0.3)])
+    return s, oracle.KBasis(s, 0)
+
+
+def test_nc_components_round_trip(oracle):
+    rng = np.random.default_rng(0)
+    v, b = random_fields(rng, 50)
+    got = oracle.nc_components(oracle.nc_from_fields(v, b))
+    for g, r in zip(got, (v, *b)):
+        assert np.max(np.abs(g - r)) < 1e-15
+    nc = oracle.nc_from_fields(v, b)
+    assert np.max(np.abs(nc - np.conj(nc.transpose(0, 2, 1)))) == 0.0   # Hermitian per point
+
+
+def test_spinor_oracle_reduces_to_scalar(oracle, small):
+    s, kb = small
+    rng = np.random.default_rng(1)
+    psi = random_spinors(rng, 2, kb.npw)
+    v = s.vext + 0.2 * rng.standard_normal(s.nr)
+    nc = oracle.nc_from_fields(v, np.zeros((3, s.nr)))
+    got = oracle.apply_h_spinor(s, kb, nc, psi)
+    for sp in range(2):
+        assert rel_err(got[sp], oracle.apply_h(s, kb, v, psi[sp])) < 1e-13
+    w = np.array([0.7, 1.0])
+    n, m = oracle.spinor_density(s, kb, psi, w)
+    n_ref = oracle.band_density(s, kb, psi[0], w) + oracle.band_density(s, kb, psi[1], w)
+    assert rel_err(n, n_ref) < 1e-13
+    mz_ref = oracle.band_density(s, kb, psi[0], w) - oracle.band_density(s, kb, psi[1], w)
+    assert rel_err(m[2], mz_ref) < 1e-12
+    # n >= |m| pointwise (equality for one band)
+    assert np.all(n * (1 + 1e-12) >= np.linalg.norm(m, axis=0))
+    n1, m1 = oracle.spinor_density(s, kb, psi[:, :1], np.ones(1))
+    assert rel_err(np.linalg.norm(m1, axis=0), n1) < 1e-12
+
+
+def test_spinor_oracle_hermitian(oracle, small):
+    s, kb = small
+    rng = np.random.default_rng(2)
+    v, b = random_fields(rng, s.nr)
+    nc = oracle.nc_from_fields(v, b)
+    phi, psi = random_spinors(rng, 1, kb.npw), random_spinors(rng, 1, kb.npw)
+    a = np.vdot(phi, oracle.apply_h_spinor(s, kb, nc, psi))
+    c = np.vdot(oracle.apply_h_spinor(s, kb, nc, phi), psi)
+    assert abs(a - c) < 1e-12 * abs(a)
+
+
+def zeeman_case(oracle, s, kb, v0=0.37, field=(0.3, -0.8, 0.5)):
+    """Plane waves times the eigen-spinors of sigma.B in a uniform V0 and B:
+    H psi = (1/2|k+G|^2 + V0 +/- mu_B |B|) psi exactly."""
+    bvec = np.asarray(field, dtype=float)
+    nc = oracle.nc_from_fields(np.full(s.nr, v0), np.repeat(bvec[:, None], s.nr, axis=1))
+    sb = np.array([[bvec[2], bvec[0] - 1j * bvec[1]], [bvec[0] + 1j * bvec[1], -bvec[2]]])
+    lam, chi = np.linalg.eigh(sb)                 # eigenvalues -|B|, +|B|
+    nb = 4
+    psi = np.zeros((2, nb, kb.npw), dtype=np.complex128)
+    expect = np.zeros(nb)
+    for b in range(nb):
+        g, j = b // 2, b % 2
+        psi[:, b, g] = chi[:, j]
+        expect[b] = kb.kinetic[g] + v0 + oracle.MU_B * lam[j]
+    return nc, psi, expect
+
+
+def test_spinor_oracle_zeeman(oracle, small):
+    s, kb = small
+    nc, psi, expect = zeeman_case(oracle, s, kb)
+    got = oracle.apply_h_spinor(s, kb, nc, psi)
+    assert np.max(np.abs(got - expect[None, :, None] * psi)) < 1e-13
+
+
+def test_spinor_symbols_exported():
+    import derek_gb300 as dg
+    for name in ("derek_gpu_set_nc_pot", "derek_gpu_get_nc_pot", "derek_gpu_density_spinor"):
+        assert hasattr(dg.lib, name)
+
+
+# ---- GPU parity
+def make_spinor_pair(oracle, L=7.0, ecut=6.0, nb=4, kpts=((0.1, 0.2, -0.3),), nelec=3.0, seed=0,
+                     cell=None):
+    import derek_gb300 as dg
+    rng = np.random.default_rng(seed)
+    wells = oracle.random_wells(rng, 3)
+    cell = np.eye(3) * L if cell is None else np.asarray(cell, dtype=float)
+    n_std, nf = oracle.grid_sizes(cell, ecut, 2.0, "smooth23")
+    vext = oracle.vext_jellium_wells(cell, nf, nelec, wells)
+    s = oracle.System(cell, ecut, nf, n_std, np.array(kpts, dtype=float),
+                      np.full(len(kpts), 1.0 / len(kpts)), nb, nelec, 0.01, vext, wells)
+    spec = dg.SystemSpec(cell, ecut, kpts, nb, nelec, kT=0.01, vext=vext, n_fine=nf,
+                         inv_cell=oracle.inv_cell(cell), nspinor=2)
+    return s, spec
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, FP64_TOL), (1, FP32_TOL)])
+@pytest.mark.parametrize("geom", ["cubic", "triclinic"])
+def test_apply_h_spinor_matches_oracle(oracle, precision, tol, geom):
+    import derek_gb300 as dg
+    kw = {}
+    if geom == "triclinic":
+        kw = dict(cell=np.array([[7.0, 0.4, 0.0], [0.0, 6.5, 0.3], [0.2, 0.0, 7.5]]), ecut=5.0)
+    s, spec = make_spinor_pair(oracle, **kw)
+    kb = oracle.KBasis(s, 0)
+    rng = np.random.default_rng(5)
+    psi = random_spinors(rng, s.nbands, kb.npw)
+    v, b = random_fields(rng, s.nr)
+    nc = oracle.nc_from_fields(s.vext + v, b)
+    with dg.Handle(spec, precision=precision) as h:
+        assert h.bands() == (s.nbands, h.bands()[1]) and h.bands()[1] >= s.nbands
+        h.set_nc_pot(nc)
+        h.set_wfn(psi)
+        assert rel_err(h.get_wfn(), psi) < (1e-16 if precision == 0 else 1e-7)
+        got = h.pot_apply_wfn()
+    ref = oracle.apply_h_spinor(s, kb, nc, psi)
+    assert got.shape == ref.shape
+    assert rel_err(got, ref) < tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, FP64_TOL), (1, FP32_TOL)])
+def test_density_spinor_matches_oracle(oracle, precision, tol):
+    import derek_gb300 as dg
+    kpts = [(0.0, 0.0, 0.0), (0.25, -0.25, 0.25), (-0.25, 0.25, 0.25)]
+    s, spec = make_spinor_pair(oracle, kpts=kpts, nb=5)
+    rng = np.random.default_rng(7)
+    occ = rng.uniform(0, 1, (len(kpts), s.nbands))
+    occ[1, 3] = 0.0
+    n_ref = np.zeros(s.nr)
+    m_ref = np.zeros((3, s.nr))
+    with dg.Handle(spec, precision=precision) as h:
+        for ik in range(len(kpts)):
+            kb = oracle.KBasis(s, ik)
+            psi = random_spinors(rng, s.nbands, kb.npw)
+            psi /= np.linalg.norm(psi, axis=(0, 2))[None, :, None]
+            h.set_wfn(psi, 0, ik)
+            n, m = oracle.spinor_density(s, kb, psi, occ[ik])
+            n_ref += s.wk[ik] * n
+            m_ref += s.wk[ik] * m
+        n_got, m_got = h.density_spinor(occ)
+        n_only = h.density_calculate(occ)
+    assert rel_err(n_got, n_ref) < tol
+    assert rel_err(m_got, m_ref) < tol
+    assert np.array_equal(n_only, n_got)
+    # charge: integral of n is sum_k w_k sum_b f for normalised spinor bands
+    assert abs(n_got.sum() * s.volume / s.nr - (s.wk[:, None] * occ).sum()) < 1e-9 + tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 2e-6)])
+def test_spinor_overlap_sums_spinors(oracle, precision, tol):
+    import derek_gb300 as dg
+    s, spec = make_spinor_pair(oracle, nb=6)
+    kb = oracle.KBasis(s, 0)
+    psi = random_spinors(np.random.default_rng(11), s.nbands, kb.npw)
+    with dg.Handle(spec, precision=precision) as h:
+        h.set_wfn(psi)
+        got = h.wave_dot()
+    ref = np.einsum("sig,sjg->ij", np.conj(psi), psi)
+    assert rel_err(got, ref) < tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 5e-6)])
+def test_spinor_zeeman_exact(oracle, precision, tol):
+    import derek_gb300 as dg
+    s, spec = make_spinor_pair(oracle)
+    kb = oracle.KBasis(s, 0)
+    nc, psi, expect = zeeman_case(oracle, s, kb)
+    with dg.Handle(spec, precision=precision) as h:
+        h.set_nc_pot(nc)
+        h.set_wfn(psi)
+        got = h.pot_apply_wfn()
+    assert np.max(np.abs(got - expect[None, :, None] * psi)) < tol * np.max(np.abs(expect))
+
+
+@pytest.mark.gpu
+def test_spinor_potential_setters_and_limits(oracle):
+    import derek_gb300 as dg
+    s, spec = make_spinor_pair(oracle)
+    rng = np.random.default_rng(4)
+    v, b = random_fields(rng, s.nr)
+    with dg.Handle(spec) as h:
+        nc0 = h.get_nc_pot()
+        assert np.array_equal(nc0[:, 0, 0].real, s.vext) and np.array_equal(nc0[:, 1, 1].real, s.vext)
+        assert not np.any(nc0[:, 0, 1]) and not np.any(nc0[:, 1, 0])
+        nc = oracle.nc_from_fields(v, b)
+        h.set_nc_pot(nc)
+        assert np.array_equal(h.get_nc_pot(), nc)
+        h.set_vloc(v)
+        nc1 = h.get_nc_pot()
+        assert np.array_equal(nc1[:, 0, 0], v.astype(complex)) and np.array_equal(nc1[:, 1, 1], v.astype(complex))
+        with pytest.raises(dg.DerekError) as e:
+            h.electronic_scf(max_scf=2)
+        assert e.value.status == 8
+    scalar = dg.SystemSpec(spec.cell, spec.ecut, spec.kpts, 4, 3.0, vext=spec.vext, n_fine=spec.n_fine)
+    with dg.Handle(scalar) as h:
+        with pytest.raises(dg.DerekError):
+            h.set_nc_pot(nc)
+    too_many = dg.SystemSpec(spec.cell, spec.ecut, spec.kpts, 4, 5.0, vext=spec.vext, n_fine=spec.n_fine,
+                             nspinor=2)
+    with pytest.raises(dg.DerekError):
+        dg.Handle(too_many)   # a spinor band holds one electron
