@@ -352,8 +352,8 @@ class Handle:
     # ---- bandstructure and dos (non-self-consistent)
     def nscf(self, max_iter=200, eig_tol=1e-9, nconv=0):
         """Eigenvalues (nk, nbands) per system in the potential set with
-        set_vloc, the lowest nconv bands (0: all) converged to eig_tol Ha;
-        returns (eigenvalues list, iterations)."""
+        set_vloc (set_nc_pot on spinor systems), the lowest nconv bands (0:
+        all) converged to eig_tol Ha; returns (eigenvalues list, iterations)."""
         it = ctypes.c_int()
         _check(lib.derek_gpu_nscf_run(self._h, int(max_iter), float(eig_tol), int(nconv), ctypes.byref(it)),
                self._h, "nscf_run")

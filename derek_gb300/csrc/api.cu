@@ -77,6 +77,17 @@ static void apply_h_t(derek_gpu *h, const Tables &base, int item_begin, int nite
 
 int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
                   void *out, const Axpby *coef) {
+  if (h->any_spinor) {
+    // spinor items pair up within a k-set: all items of an all-spinor batch,
+    // or one spinor k-set (mixed batches run per k-set)
+    if (item_begin == 0 && nitems == h->nitems) {
+      if (h->all_spinor) return apply_spinor_items(h, item_begin, nitems, in, prev, out, coef);
+      h->last_error = "H.psi over a batch mixing spinor and scalar systems";
+      return DEREK_ERR_UNSUPPORTED;
+    }
+    if (h->sys[h->ks[h->item_ks[item_begin]].sys].nspinor == 2)
+      return apply_spinor_items(h, item_begin, nitems, in, prev, out, coef);
+  }
   if (h->prec == DEREK_PREC_FP64)
     apply_h_t<double>(h, h->tab, item_begin, nitems, in, prev, out, coef, h->d_vloc);
   else
@@ -119,29 +130,46 @@ int density_items(derek_gpu *h, const void *psi, double *rho) {
   return DEREK_OK;
 }
 
-// H.psi of every band of k-set ki of a spinor system: x-line passes per
-// component, the 2x2 plane pass per band
-template <typename R> static void apply_spinor_t(derek_gpu *h, int ki, const void *in, void *out) {
-  const KSetDev &K = h->ks[ki];
-  const SysDev &S = h->sys[K.sys];
-  const int nchunk = (K.ncol + kColChunk - 1) / kColChunk;
+// Spinor H.psi over one grid-size class: x-line passes per component, the
+// 2x2 plane pass per band, the filter epilogue per component
+template <typename R>
+static void apply_spinor_class(derek_gpu *h, const Tables &t, int item_begin, int nitems, int nchunk,
+                               const int n[3], const void *in, const void *prev, void *out,
+                               const Axpby *coef) {
   const cplx<R> *vnc;
   if constexpr (std::is_same<R, double>::value)
     vnc = h->d_vnc64;
   else
     vnc = h->d_vnc32;
-  launch_x_inv_lines<R>(h->tab, K.item0, K.nb, nchunk, S.n[0], S.n[0], (const cplx<R> *)in,
+  launch_x_inv_lines<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)in,
                         (cplx<R> *)h->d_abuf, nullptr, h->stream);
-  launch_plane_spinor<R>(h->tab, K.item0, K.nb, S.n, (cplx<R> *)h->d_abuf, vnc, h->stream);
-  launch_x_fwd_lines<R>(h->tab, K.item0, K.nb, nchunk, S.n[0], S.n[0], (const cplx<R> *)h->d_abuf,
-                        (const cplx<R> *)in, nullptr, (cplx<R> *)out, nullptr, h->stream);
+  launch_plane_spinor<R>(t, item_begin, nitems, n, (cplx<R> *)h->d_abuf, vnc, h->stream);
+  launch_x_fwd_lines<R>(t, item_begin, nitems, nchunk, n[0], n[0], (const cplx<R> *)h->d_abuf,
+                        (const cplx<R> *)in, (const cplx<R> *)prev, (cplx<R> *)out, coef, h->stream);
 }
 
-int apply_spinor_items(derek_gpu *h, int ki, const void *in, void *out) {
+template <typename R>
+static void apply_spinor_t(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
+                           void *out, const Axpby *coef) {
+  if (item_begin == 0 && nitems == h->nitems) {
+    for (const auto &c : h->classes) {
+      Tables t = h->tab;
+      t.item_list = c.d_list;
+      apply_spinor_class<R>(h, t, 0, c.count, c.nchunk, c.n, in, prev, out, coef);
+    }
+    return;
+  }
+  const KSetDev &K = h->ks[h->item_ks[item_begin]];
+  apply_spinor_class<R>(h, h->tab, item_begin, nitems, (K.ncol + kColChunk - 1) / kColChunk,
+                        h->sys[K.sys].n, in, prev, out, coef);
+}
+
+int apply_spinor_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
+                       void *out, const Axpby *coef) {
   if (h->prec == DEREK_PREC_FP64)
-    apply_spinor_t<double>(h, ki, in, out);
+    apply_spinor_t<double>(h, item_begin, nitems, in, prev, out, coef);
   else
-    apply_spinor_t<float>(h, ki, in, out);
+    apply_spinor_t<float>(h, item_begin, nitems, in, prev, out, coef);
   DEREK_CUDA(h, cudaGetLastError());
   return DEREK_OK;
 }
@@ -256,7 +284,7 @@ int derek_gpu_destroy(derek_gpu_t *h) {
                   h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
                   h->d_Yp,    h->d_HX,      h->d_abuf,    h->d_occw,      h->d_eig,
                   h->d_occ,   h->d_coef,    h->d_cells,   h->d_wells,     h->d_well_off,
-                  h->d_hfpart, h->d_hfgrad, h->d_vnc64, h->d_vnc32, h->d_mag};
+                  h->d_hfpart, h->d_hfgrad, h->d_vnc64, h->d_vnc32, h->d_mag, h->d_ks_band};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (auto &c : h->classes)
@@ -380,6 +408,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     S.nbr = d.nspinor * d.nbands;
     S.nspinor = d.nspinor;
     h->any_spinor |= d.nspinor == 2;
+    h->all_spinor &= d.nspinor == 2;
     S.ks0 = (int)h->ks.size();
     S.active = 1;
     S.volume = cell_volume(d.cell);
@@ -509,6 +538,15 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   CK(upload(&h->d_sys, h->sys));
   CK(upload(&h->d_ks, h->ks));
+  h->ks_band = h->ks;
+  for (auto &K : h->ks_band)
+    if (h->sys[K.sys].nspinor == 2) {
+      K.nb /= 2;
+      K.nbr /= 2;
+      K.npw_pad *= 2;
+      K.npw = K.npw_pad;
+    }
+  CK(upload(&h->d_ks_band, h->ks_band));
   CK(upload(&h->d_item_ks, h->item_ks));
   CK(upload(&h->d_item_band, h->item_band));
   CK(upload(&h->d_ent_col, ent_col));
@@ -606,6 +644,8 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
   h->tab.tw32 = h->d_tw32;
   h->tab.item_list = nullptr;
   h->tab.item_shift = nullptr;
+  h->tab_band = h->tab;
+  h->tab_band.ks = h->d_ks_band;
   {
     // group items by grid size; a single class over all items needs no list
     std::map<std::array<int, 3>, std::vector<int>> groups;
@@ -842,8 +882,7 @@ int derek_gpu_apply_h(derek_gpu_t *h, int s, int k, double *hpsi) {
   int ki = ks_index(h, s, k);
   if (ki < 0 || !hpsi) return DEREK_ERR_BAD_ARG;
   const KSetDev &K = h->ks[ki];
-  int st = h->sys[s].nspinor == 2 ? apply_spinor_items(h, ki, h->cur_psi(), h->d_HX)
-                                  : apply_h_items(h, K.item0, K.nb, h->cur_psi(), nullptr, h->d_HX, nullptr);
+  int st = apply_h_items(h, K.item0, K.nb, h->cur_psi(), nullptr, h->d_HX, nullptr);
   if (st) return st;
   return copy_slice(h, ki, h->d_HX, hpsi, false);
 }

@@ -37,6 +37,14 @@ struct derek_gpu {
 
   // ---- device tables
   derek::Tables tab{};
+  // band view for the subspace kernels (overlaps, Cholesky, Jacobi,
+  // rotations, filter bounds): equal to tab except that a spinor k-set's
+  // band is one row of 2 npw_pad coefficients (nb, nbr halved; npw = npw_pad
+  // = 2 npw_pad), its eigenvalue j at eig[item0 + j]
+  derek::Tables tab_band{};
+  std::vector<derek::KSetDev> ks_band;
+  derek::KSetDev *d_ks_band = nullptr;
+  int max_nb_band = 0, max_npw_band = 0;
   derek::SysDev *d_sys = nullptr;
   derek::KSetDev *d_ks = nullptr;
   int *d_item_ks = nullptr, *d_item_band = nullptr;
@@ -55,6 +63,7 @@ struct derek_gpu {
   // non-collinear systems: 2x2 potential per point (V11, V21, V12, V22) and
   // the magnetisation (mx, my, mz grids of total_grid values each)
   bool any_spinor = false;
+  bool all_spinor = true;         // every system has nspinor = 2
   double2 *d_vnc64 = nullptr;
   float2 *d_vnc32 = nullptr;
   double *d_mag = nullptr;
@@ -143,9 +152,12 @@ int apply_h_items_ex(derek_gpu *h, const Tables &base, int item_begin, int nitem
 // Density of every active system from psi buffer `psi` and per-item weights
 // h->d_occw into rho (FP64 grids).
 int density_items(derek_gpu *h, const void *psi, double *rho);
-// Spinor systems: H.psi of every band of k-set ki (in -> out, no epilogue)
-// and n, m of every active spinor system (rho, h->d_mag).
-int apply_spinor_items(derek_gpu *h, int ki, const void *in, void *out);
+// Spinor systems: H.psi over items [item_begin, item_begin + nitems) (all
+// items of an all-spinor batch, or the items of one spinor k-set) with the
+// same epilogue as apply_h_items, and n, m of every active spinor system
+// (rho, h->d_mag).
+int apply_spinor_items(derek_gpu *h, int item_begin, int nitems, const void *in, const void *prev,
+                       void *out, const Axpby *coef);
 // True (with last_error set) when h holds a spinor system: the SCF, NSCF,
 // gradients and timing entry points run scalar systems only.
 bool reject_spinor(derek_gpu *h, const char *what);

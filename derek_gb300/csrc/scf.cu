@@ -28,20 +28,20 @@ template <typename T> cudaError_t dalloc(T **p, size_t n) {
 
 // -- pieces of an iteration -------------------------------------------------
 bool use_tc(const derek_gpu *h) {
-  return h->prec == DEREK_PREC_MIXED && h->opts.use_tensor_cores && h->max_nb <= kMaxBands;
+  return h->prec == DEREK_PREC_MIXED && h->opts.use_tensor_cores && h->max_nb <= kMaxBands && !h->any_spinor;
 }
 
 int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int hermitize) {
   if (use_tc(h))
-    launch_overlap_tc(h->tab, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit, (const float2 *)A,
+    launch_overlap_tc(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, kOverlapSplit, (const float2 *)A,
                       (const float2 *)B, h->d_opart, h->d_opart_off, out, h->d_mat_off, hermitize,
                       h->d_status, h->stream);
   else if (h->prec == DEREK_PREC_FP64)
-    launch_overlap<double>(h->tab, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit,
+    launch_overlap<double>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, kOverlapSplit,
                            (const double2 *)A, (const double2 *)B, h->d_opart, h->d_opart_off, out,
                            h->d_mat_off, hermitize, h->stream);
   else
-    launch_overlap<float>(h->tab, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit,
+    launch_overlap<float>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, kOverlapSplit,
                           (const float2 *)A, (const float2 *)B, h->d_opart, h->d_opart_off, out,
                           h->d_mat_off, hermitize, h->stream);
   return DEREK_OK;
@@ -49,13 +49,13 @@ int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int he
 
 int rotate_all(derek_gpu *h, void *X, const double2 *C) {
   if (use_tc(h) && h->opts.use_tensor_cores >= 2)
-    launch_rotate_tc(h->tab, 0, h->nks, h->max_nb, h->max_npw, (float2 *)X, C, h->d_mat_off,
+    launch_rotate_tc(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, (float2 *)X, C, h->d_mat_off,
                      h->d_rot_img, h->d_status, h->stream);
   else if (h->prec == DEREK_PREC_FP64)
-    launch_rotate<double>(h->tab, 0, h->nks, h->max_nb, h->max_npw, (double2 *)X, C, h->d_mat_off,
+    launch_rotate<double>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, (double2 *)X, C, h->d_mat_off,
                           h->stream);
   else
-    launch_rotate<float>(h->tab, 0, h->nks, h->max_nb, h->max_npw, (float2 *)X, C, h->d_mat_off,
+    launch_rotate<float>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, (float2 *)X, C, h->d_mat_off,
                          h->stream);
   return DEREK_OK;
 }
@@ -64,7 +64,7 @@ int rotate_all(derek_gpu *h, void *X, const double2 *C) {
 int cholqr_rr(derek_gpu *h) {
   void *X = h->cur_psi();
   overlap_all(h, X, X, h->d_S, 1);
-  launch_cholesky_inv(h->tab, 0, h->nks, h->max_nb, h->d_S, h->d_C, h->d_mat_off, h->d_scratch,
+  launch_cholesky_inv(h->tab_band, 0, h->nks, h->max_nb_band, h->d_S, h->d_C, h->d_mat_off, h->d_scratch,
                       h->d_status, h->stream);
   rotate_all(h, X, h->d_C);
   int st = apply_h_items(h, 0, h->nitems, X, nullptr, h->d_HX, nullptr);
@@ -75,14 +75,14 @@ int cholqr_rr(derek_gpu *h) {
   // relative), so 1e-10 leaves eigenvalue errors of order 1e-20 / gap while
   // saving about one of the four sweeps near convergence.
   const double jtol = h->prec == DEREK_PREC_FP64 ? 1e-14 : 1e-10;
-  launch_jacobi(h->tab, 0, h->nks, h->max_nb, h->d_Hs, h->d_C, h->d_mat_off, h->d_eig,
+  launch_jacobi(h->tab_band, 0, h->nks, h->max_nb_band, h->d_Hs, h->d_C, h->d_mat_off, h->d_eig,
                 h->d_scratch, 30, jtol, 0, h->d_sweeps, h->stream);
   rotate_all(h, X, h->d_C);
   return DEREK_OK;
 }
 
 int filter(derek_gpu *h, int m) {
-  launch_filter_coef(h->tab, h->nks, h->d_eig, h->d_state, h->d_coef_all, m, h->stream);
+  launch_filter_coef(h->tab_band, h->nks, h->d_eig, h->d_state, h->d_coef_all, m, h->stream);
   int in = h->cur, prev = -1;
   for (int i = 0; i < m; ++i) {
     const int out = prev < 0 ? (in + 1) % 3 : 3 - in - prev;
@@ -264,6 +264,10 @@ extern "C" int derek_scf_alloc(derek_gpu_t *h) {
     poff += (long long)((K.npw + kOverlapSplit - 1) / kOverlapSplit) * K.nb * K.nb;
     h->max_npw = std::max(h->max_npw, K.npw);
   }
+  for (const auto &K : h->ks_band) {
+    h->max_nb_band = std::max(h->max_nb_band, K.nb);
+    h->max_npw_band = std::max(h->max_npw_band, K.npw);
+  }
   std::vector<long long> hist_off;
   long long hoff = 0;
   for (const auto &S : h->sys) {
@@ -375,7 +379,10 @@ int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
 
 int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, int *iterations) {
   if (!h || max_iter <= 0 || !(eig_tol > 0) || nconv < 0) return DEREK_ERR_BAD_ARG;
-  if (reject_spinor(h, "nscf_run")) return DEREK_ERR_UNSUPPORTED;
+  if (h->any_spinor && !h->all_spinor) {
+    h->last_error = "nscf_run: a batch mixing spinor and scalar systems";
+    return DEREK_ERR_UNSUPPORTED;
+  }
   // frozen potential: the filter's upper bound from max V_loc of each system
   for (auto &s : h->sys) s.active = 1;
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
@@ -384,8 +391,23 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, 
   for (int s = 0; s < h->nsys; ++s) {
     std::memset(&st[s], 0, sizeof(SysState));
     st[s].slot = -1;
-    std::vector<double> v(h->sys[s].nr);
-    DEREK_CUDA(h, cudaMemcpy(v.data(), h->d_vloc + h->sys[s].grid_off, v.size() * sizeof(double),
+    const SysDev &S = h->sys[s];
+    if (S.nspinor == 2) {
+      // largest eigenvalue of the Hermitian part of nc_pot over the grid
+      std::vector<double2> v((size_t)4 * S.nr);
+      DEREK_CUDA(h, cudaMemcpy(v.data(), h->d_vnc64 + 4 * S.grid_off, v.size() * sizeof(double2),
+                               cudaMemcpyDeviceToHost));
+      double vmax = -1e300;
+      for (long long i = 0; i < S.nr; ++i) {
+        const double a = v[4 * i].x, d = v[4 * i + 3].x;
+        const double br = 0.5 * (v[4 * i + 2].x + v[4 * i + 1].x), bi = 0.5 * (v[4 * i + 2].y - v[4 * i + 1].y);
+        vmax = std::max(vmax, 0.5 * (a + d) + std::sqrt(0.25 * (a - d) * (a - d) + br * br + bi * bi));
+      }
+      st[s].vmax = vmax;
+      continue;
+    }
+    std::vector<double> v(S.nr);
+    DEREK_CUDA(h, cudaMemcpy(v.data(), h->d_vloc + S.grid_off, v.size() * sizeof(double),
                              cudaMemcpyDeviceToHost));
     st[s].vmax = *std::max_element(v.begin(), v.end());
   }
@@ -425,7 +447,7 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, 
     if (!prev.empty()) {
       double d = 0;
       for (int q = 0; q < h->nks; ++q) {
-        const auto &K = h->ks[q];
+        const auto &K = h->ks_band[q];
         for (int b = 0; b < (nconv > 0 ? std::min(nconv, K.nbr) : K.nbr); ++b) {
           const double x = std::fabs(eig[K.item0 + b] - prev[K.item0 + b]);
           if (x > d) {
@@ -481,10 +503,12 @@ int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol, derek_scf_report
 static int get_items(derek_gpu_t *h, int s, const double *src, double *out) {
   if (!h || s < 0 || s >= h->nsys || !out) return DEREK_ERR_BAD_ARG;
   const SysDev &S = h->sys[s];
-  // first nbr items of each k-point (the buffer bands are not reported)
+  // first nbr entries of each k-point (the buffer bands are not reported); a
+  // spinor k-set keeps band j's entry at item0 + j
   const KSetDev &K0 = h->ks[S.ks0];
-  DEREK_CUDA(h, cudaMemcpy2DAsync(out, (size_t)S.nbr * sizeof(double), src + K0.item0,
-                                  (size_t)S.nb * sizeof(double), (size_t)S.nbr * sizeof(double),
+  const int nbr = S.nbr / S.nspinor;
+  DEREK_CUDA(h, cudaMemcpy2DAsync(out, (size_t)nbr * sizeof(double), src + K0.item0,
+                                  (size_t)S.nb * sizeof(double), (size_t)nbr * sizeof(double),
                                   S.nk, cudaMemcpyDeviceToHost, h->stream));
   DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
   return DEREK_OK;

@@ -487,6 +487,23 @@ def apply_h_spinor(sys: System, kb: KBasis, nc: np.ndarray, psi: np.ndarray) -> 
     return out
 
 
+def dense_h_spinor(sys: System, kb: KBasis, nc: np.ndarray) -> np.ndarray:
+    """Dense 2 Npw x 2 Npw spinor Hamiltonian, blocks (s, s') of Npw rows:
+    T delta_ss' + V_ss'(G - G') with V_ss'(G) = F[nc[:, s, s']] / N.  Row
+    s * Npw + g holds spinor s of plane wave g (apply_h_spinor's layout)."""
+    n1, n2, n3 = sys.n_fine
+    d = kb.miller[:, None, :] - kb.miller[None, :, :]
+    ix = (np.mod(d[..., 0], n1), np.mod(d[..., 1], n2), np.mod(d[..., 2], n3))
+    npw = kb.npw
+    H = np.zeros((2 * npw, 2 * npw), dtype=np.complex128)
+    for a in range(2):
+        for b in range(2):
+            vG = fft3d(np.ascontiguousarray(nc[:, a, b]), sys.n_fine, 1).reshape(sys.n_fine) / sys.nr
+            H[a * npw:(a + 1) * npw, b * npw:(b + 1) * npw] = vG[ix]
+    H[np.diag_indices_from(H)] += np.concatenate([kb.kinetic, kb.kinetic])
+    return H
+
+
 def spinor_density(sys: System, kb: KBasis, psi: np.ndarray, weights: np.ndarray):
     """(n, m) with n = sum_b w_b (|u|^2 + |d|^2) / Omega and
     m = sum_b w_b psi^H sigma psi / Omega, shape (3, nr)."""

@@ -102,6 +102,23 @@ def test_spinor_oracle_zeeman(oracle, small):
     assert np.max(np.abs(got - expect[None, :, None] * psi)) < 1e-13
 
 
+def test_dense_spinor_hamiltonian(oracle, small):
+    s, kb = small
+    rng = np.random.default_rng(8)
+    v, b = random_fields(rng, s.nr)
+    nc = oracle.nc_from_fields(s.vext + v, b)
+    H = oracle.dense_h_spinor(s, kb, nc)
+    assert np.max(np.abs(H - H.conj().T)) < 1e-14
+    psi = random_spinors(rng, 2, kb.npw)
+    hv = oracle.apply_h_spinor(s, kb, nc, psi)
+    for j in range(2):
+        assert rel_err((H @ psi[:, j].reshape(-1)).reshape(2, -1), hv[:, j]) < 1e-12
+    # B = 0: two copies of the scalar spectrum
+    H0 = oracle.dense_h_spinor(s, kb, oracle.nc_from_fields(s.vext, np.zeros((3, s.nr))))
+    e0 = np.linalg.eigvalsh(oracle.dense_h(s, kb, s.vext))
+    assert np.max(np.abs(np.linalg.eigvalsh(H0) - np.sort(np.repeat(e0, 2)))) < 1e-12
+
+
 def test_spinor_symbols_exported():
     import derek_gb300 as dg
     for name in ("derek_gpu_set_nc_pot", "derek_gpu_get_nc_pot", "derek_gpu_density_spinor"):
@@ -204,6 +221,40 @@ def test_spinor_zeeman_exact(oracle, precision, tol):
         h.set_wfn(psi)
         got = h.pot_apply_wfn()
     assert np.max(np.abs(got - expect[None, :, None] * psi)) < tol * np.max(np.abs(expect))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-8), (1, 2e-5)])
+def test_spinor_nscf_matches_dense(oracle, precision, tol):
+    """Band energies of spinor bands in a non-uniform 2x2 potential against
+    the oracle's dense spinor Hamiltonian, at two k-points."""
+    import derek_gb300 as dg
+    kpts = [(0.1, 0.2, -0.3), (0.0, 0.0, 0.0)]
+    s, spec = make_spinor_pair(oracle, L=6.0, ecut=4.0, nb=6, kpts=kpts)
+    rng = np.random.default_rng(9)
+    v, b = random_fields(rng, s.nr, scale=0.5)
+    nc = oracle.nc_from_fields(s.vext + v, b)
+    with dg.Handle(spec, precision=precision, use_tensor_cores=0, init_vectors=1) as h:
+        h.set_nc_pot(nc)
+        eig = h.nscf(max_iter=300, eig_tol=1e-10 if precision == 0 else 2e-6, nconv=4)[0][0]
+    for ik in range(len(kpts)):
+        ref = np.linalg.eigvalsh(oracle.dense_h_spinor(s, oracle.KBasis(s, ik), nc))[:4]
+        assert np.max(np.abs(eig[ik, :4] - ref)) < tol, (ik, eig[ik, :4], ref)
+
+
+@pytest.mark.gpu
+def test_spinor_nscf_zeeman_levels(oracle):
+    """Uniform V0 and B: the spinor levels are 1/2|k+G|^2 + V0 -/+ mu_B |B|."""
+    import derek_gb300 as dg
+    s, spec = make_spinor_pair(oracle, L=6.0, ecut=4.0, nb=6)
+    kb = oracle.KBasis(s, 0)
+    nc, _, _ = zeeman_case(oracle, s, kb, field=(0.2, 0.1, -0.4))
+    with dg.Handle(spec, use_tensor_cores=0, init_vectors=1) as h:
+        h.set_nc_pot(nc)
+        eig = h.nscf(max_iter=300, eig_tol=1e-11, nconv=4)[0][0]
+    bmag = np.linalg.norm([0.2, 0.1, -0.4])
+    levels = np.sort(np.concatenate([kb.kinetic + 0.37 - oracle.MU_B * bmag, kb.kinetic + 0.37 + oracle.MU_B * bmag]))
+    assert np.max(np.abs(eig[0, :4] - levels[:4])) < 1e-9
 
 
 @pytest.mark.gpu
