@@ -296,6 +296,92 @@ def lda_x_c(rho: np.ndarray):
     return tuple(out)
 
 
+# PW92 parameter columns of src/lda_c_pw.c:41-50: eps_c(rs, 0), eps_c(rs, 1)
+# and -alpha_c(rs); fz20 = f''(0)
+PW92_POL = dict(a=(0.031091, 0.015545, 0.016887), alpha1=(0.21370, 0.20548, 0.11125),
+                beta1=(7.5957, 14.1189, 10.357), beta2=(3.5876, 6.1977, 3.6231),
+                beta3=(1.6382, 3.3662, 0.88026), beta4=(0.49294, 0.62517, 0.49671), fz20=1.709921)
+ZETA_THRESHOLD = np.finfo(np.float64).eps   # libxc's default zeta threshold
+
+
+def _pw_g(k: int, rs: np.ndarray):
+    """G_k(rs) of maple/lda_exc/lda_c_pw.mpl:34-37 (equation 10 of Perdew and
+    Wang 1992) and dG_k/drs for parameter column k."""
+    P = PW92_POL
+    a, al = P["a"][k], P["alpha1"][k]
+    srs = np.sqrt(rs)
+    q0 = -2.0 * a * (1.0 + al * rs)
+    q1 = 2.0 * a * (P["beta1"][k] * srs + P["beta2"][k] * rs + P["beta3"][k] * rs * srs + P["beta4"][k] * rs * rs)
+    dq1 = a * (P["beta1"][k] / srs + 2.0 * P["beta2"][k] + 3.0 * P["beta3"][k] * srs + 4.0 * P["beta4"][k] * rs)
+    lg = np.log(1.0 + 1.0 / q1)
+    return q0 * lg, -2.0 * a * al * lg - q0 * dq1 / (q1 * q1 + q1)
+
+
+def lda_pol(rhoa: np.ndarray, rhob: np.ndarray):
+    """Spin-polarised LDA_X + LDA_C_PW: (eps_x, v_x (n, 2), eps_c, v_c (n, 2)).
+
+    Follows libxc 6.2.2: each spin density is raised to the density
+    threshold and points with rhoa + rhob below it give zeros
+    (src/work_lda_inc.c:48-55); zeta is kept 1e-16 inside [-1, 1] (z_thr,
+    maple/util.mpl:77-82); an exchange channel with n_s <= threshold is
+    screened (maple/util.mpl:101-110).  Exchange per channel is
+    -(3/8)(3/pi)^{1/3} (2 n_s)^{4/3} / n, v_x,s = -(6 n_s / pi)^{1/3}.
+    Correlation: eps_c = G1 + z^4 f(z) (G2 - G1 + G3/fz20) - f(z) G3/fz20
+    (maple/lda_exc/lda_c_pw.mpl:42-44), f(z) = ((1+z)^{4/3} + (1-z)^{4/3} - 2)
+    / (2^{4/3} - 2); v_c,s = eps_c - rs/3 d eps_c/drs -/+ (z -/+ 1) d eps_c/dz.
+    """
+    ra = np.asarray(rhoa, dtype=np.float64)
+    rb = np.asarray(rhob, dtype=np.float64)
+    n_pts = ra.shape[0]
+    ex = np.zeros(n_pts)
+    ec = np.zeros(n_pts)
+    vx = np.zeros((n_pts, 2))
+    vc = np.zeros((n_pts, 2))
+    mask = (ra + rb) >= DENS_THRESHOLD
+    na = np.maximum(ra[mask], DENS_THRESHOLD)
+    nb = np.maximum(rb[mask], DENS_THRESHOLD)
+    n = na + nb
+    zt = ZETA_THRESHOLD
+    # 1 +/- zeta as 2 n_s / n: no cancellation next to full polarisation
+    opz = 2.0 * na / n
+    omz = 2.0 * nb / n
+    opz, omz = np.where(opz <= zt, zt, np.where(omz <= zt, 2.0 - zt, opz)), \
+        np.where(omz <= zt, zt, np.where(opz <= zt, 2.0 - zt, omz))
+    z = opz - 1.0
+    cx = -0.75 * (3.0 / math.pi) ** (1.0 / 3.0)
+    e_x = np.zeros_like(n)
+    for ns, sign, col in ((na, 1.0, 0), (nb, -1.0, 1)):
+        live = ns > DENS_THRESHOLD
+        opz_s = opz if sign > 0 else omz
+        e_x += np.where(live, 0.5 * cx * np.cbrt(n) * opz_s ** (4.0 / 3.0), 0.0)
+        vx_s = np.where(live, -np.cbrt(6.0 * ns / math.pi), 0.0)
+        tmp = np.zeros(n_pts)
+        tmp[mask] = vx_s
+        vx[:, col] = tmp
+    ex[mask] = e_x
+    rs = (3.0 / (FOUR_PI * n)) ** (1.0 / 3.0)
+    g1, d1 = _pw_g(0, rs)
+    g2, d2 = _pw_g(1, rs)
+    g3, d3 = _pw_g(2, rs)
+    fz20 = PW92_POL["fz20"]
+    den = 2.0 ** (4.0 / 3.0) - 2.0
+    fz = (opz ** (4.0 / 3.0) + omz ** (4.0 / 3.0) - 2.0) / den
+    dfz = (4.0 / 3.0) * (np.cbrt(opz) - np.cbrt(omz)) / den
+    z4 = z ** 4
+    e_c = g1 + z4 * fz * (g2 - g1 + g3 / fz20) - fz * g3 / fz20
+    de_rs = d1 + z4 * fz * (d2 - d1 + d3 / fz20) - fz * d3 / fz20
+    de_z = (4.0 * z ** 3 * fz + z4 * dfz) * (g2 - g1 + g3 / fz20) - dfz * g3 / fz20
+    base = e_c - rs / 3.0 * de_rs
+    ec[mask] = e_c
+    tmp = np.zeros(n_pts)
+    tmp[mask] = base + omz * de_z
+    vc[:, 0] = tmp
+    tmp = np.zeros(n_pts)
+    tmp[mask] = base - opz * de_z
+    vc[:, 1] = tmp
+    return ex, vx, ec, vc
+
+
 def lda_exc_vxc(rho: np.ndarray):
     ex, vx, ec, vc = lda_x_c(rho)
     return ex + ec, vx + vc
