@@ -260,6 +260,30 @@ class Handle:
                self._h, "get_nc_pot")
         return np.ascontiguousarray(f.transpose(2, 1, 0))
 
+    def magnetisation(self, sys=0):
+        """m(r) of a spinor system's last density pass, shape (3, nr)."""
+        nf, _ = self.grid(sys)
+        mag = np.zeros((3, int(np.prod(nf))))
+        _check(lib.derek_gpu_get_magnetisation(self._h, sys, _dptr(mag)), self._h, "get_magnetisation")
+        return mag
+
+    def set_start_magnetisation(self, mag, sys=0):
+        """Start magnetisation (3, nr) of a spinor system's SCF (None: zero)."""
+        if mag is None:
+            _check(lib.derek_gpu_set_start_magnetisation(self._h, sys, None), self._h, "set_start_magnetisation")
+            return
+        m = np.ascontiguousarray(np.asarray(mag, dtype=np.float64))
+        _check(lib.derek_gpu_set_start_magnetisation(self._h, sys, _dptr(m)), self._h, "set_start_magnetisation")
+
+    def xc_lsda(self, rho_up, rho_down):
+        """(eps_xc, v_up, v_down) of the spin-polarised LDA on the GPU."""
+        a = np.ascontiguousarray(np.asarray(rho_up, dtype=np.float64))
+        b = np.ascontiguousarray(np.asarray(rho_down, dtype=np.float64))
+        e, va, vb = np.zeros_like(a), np.zeros_like(a), np.zeros_like(a)
+        _check(lib.derek_gpu_xc_lsda(self._h, ctypes.c_long(a.size), _dptr(a), _dptr(b), _dptr(e), _dptr(va),
+                                     _dptr(vb)), self._h, "xc_lsda")
+        return e, va, vb
+
     def xc_lda(self, rho):
         rho = np.ascontiguousarray(np.asarray(rho, dtype=np.float64))
         exc = np.zeros_like(rho)

@@ -10,6 +10,7 @@
 
 #include "basis.h"
 #include "handle.h"
+#include "scf_kernels.cuh"
 
 using derek::KSetDev;
 using derek::SysDev;
@@ -284,7 +285,8 @@ int derek_gpu_destroy(derek_gpu_t *h) {
                   h->d_cgrid, h->d_partial, h->d_partial_off, h->d_X,     h->d_Y,
                   h->d_Yp,    h->d_HX,      h->d_abuf,    h->d_occw,      h->d_eig,
                   h->d_occ,   h->d_coef,    h->d_cells,   h->d_wells,     h->d_well_off,
-                  h->d_hfpart, h->d_hfgrad, h->d_vnc64, h->d_vnc32, h->d_mag, h->d_ks_band};
+                  h->d_hfpart, h->d_hfgrad, h->d_vnc64, h->d_vnc32, h->d_mag, h->d_ks_band,
+                  h->d_vnc_ext};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (auto &c : h->classes)
@@ -608,6 +610,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     for (size_t i = 0; i < vnc.size(); ++i) vnc32[i] = make_float2((float)vnc[i].x, (float)vnc[i].y);
     CK(upload(&h->d_vnc64, vnc));
     CK(upload(&h->d_vnc32, vnc32));
+    CK(upload(&h->d_vnc_ext, vnc));
     CK(cudaMalloc((void **)&h->d_mag, (size_t)3 * grid_off * sizeof(double)));
   }
   const size_t pbytes = (size_t)h->total_psi * h->elem_size();
@@ -734,9 +737,13 @@ int derek_gpu_fft3d(derek_gpu_t *h, int s, double *inout, int dir) {
   return DEREK_OK;
 }
 
-// write system s's 2x2 potential, given per point as V11, V21, V12, V22
-static int upload_nc(derek_gpu_t *h, int s, const std::vector<double2> &vnc) {
+// write system s's 2x2 potential, given per point as V11, V21, V12, V22: the
+// H.psi potential and, with ext, the SCF's external potential too
+static int upload_nc(derek_gpu_t *h, int s, const std::vector<double2> &vnc, bool ext = false) {
   const SysDev &S = h->sys[s];
+  if (ext)
+    DEREK_CUDA(h, cudaMemcpyAsync(h->d_vnc_ext + 4 * S.grid_off, vnc.data(), vnc.size() * sizeof(double2),
+                                  cudaMemcpyHostToDevice, h->stream));
   std::vector<float2> v32(vnc.size());
   for (size_t i = 0; i < vnc.size(); ++i) v32[i] = make_float2((float)vnc[i].x, (float)vnc[i].y);
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_vnc64 + 4 * S.grid_off, vnc.data(), vnc.size() * sizeof(double2),
@@ -776,7 +783,8 @@ int derek_gpu_set_nc_pot(derek_gpu_t *h, int s, const double *nc_pot) {
   for (int c = 0; c < 4; ++c)
     for (long long i = 0; i < S.nr; ++i)
       vnc[4 * i + c] = make_double2(nc_pot[2 * (c * S.nr + i)], nc_pot[2 * (c * S.nr + i) + 1]);
-  return upload_nc(h, s, vnc);
+  h->scf_started = false;
+  return upload_nc(h, s, vnc, true);
 }
 
 int derek_gpu_get_nc_pot(derek_gpu_t *h, int s, double *nc_pot) {
@@ -950,6 +958,23 @@ int derek_gpu_density_spinor(derek_gpu_t *h, int s, const double *occ, double *r
   return DEREK_OK;
 }
 
+int derek_gpu_xc_lsda(derek_gpu_t *h, long n, const double *rho_a, const double *rho_b, double *exc,
+                      double *va, double *vb) {
+  if (!h || n <= 0 || !rho_a || !rho_b || !exc || !va || !vb) return DEREK_ERR_BAD_ARG;
+  double *d = nullptr;
+  DEREK_CUDA(h, cudaMalloc((void **)&d, 5 * (size_t)n * sizeof(double)));
+  cudaMemcpyAsync(d, rho_a, n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(d + n, rho_b, n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  launch_lsda(n, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, h->stream);
+  cudaMemcpyAsync(exc, d + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(va, d + 3 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(vb, d + 4 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_status(e, h, "xc_lsda");
+  return DEREK_OK;
+}
+
 int derek_gpu_xc_lda(derek_gpu_t *h, long n, const double *rho, double *exc, double *vxc) {
   if (!h || n <= 0 || !rho || (!exc && !vxc)) return DEREK_ERR_BAD_ARG;
   double *d = nullptr;
@@ -991,6 +1016,12 @@ int derek_gpu_set_vext(derek_gpu_t *h, int s, const double *v) {
                                 cudaMemcpyHostToDevice, h->stream));
   std::copy(v, v + S.nr, h->vext_host.begin() + S.grid_off);
   h->scf_started = false;
+  if (S.nspinor == 2) {
+    // the spinor SCF's external potential: V_ext on the diagonal, no field
+    std::vector<double2> vnc((size_t)4 * S.nr, make_double2(0.0, 0.0));
+    for (long long i = 0; i < S.nr; ++i) vnc[4 * i] = vnc[4 * i + 3] = make_double2(v[i], 0.0);
+    return upload_nc(h, s, vnc, true);
+  }
   return DEREK_OK;
 }
 

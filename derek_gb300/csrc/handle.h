@@ -67,6 +67,11 @@ struct derek_gpu {
   double2 *d_vnc64 = nullptr;
   float2 *d_vnc32 = nullptr;
   double *d_mag = nullptr;
+  // non-collinear SCF: external nc_pot, mixed input magnetisation, xc field,
+  // mixing history of m, per-system start magnetisation (empty = zero)
+  double2 *d_vnc_ext = nullptr;
+  double *d_mag_in = nullptr, *d_bxc = nullptr, *d_min_hist = nullptr, *d_mres_hist = nullptr;
+  std::vector<std::vector<double>> start_mag;
   std::vector<std::vector<double>> start_rho;   // per system: SCF start density (empty = uniform)
   double *d_exc = nullptr, *d_vxc = nullptr;
   double2 *d_cgrid = nullptr;      // complex work grid

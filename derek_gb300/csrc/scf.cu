@@ -102,20 +102,46 @@ int subspace_step(derek_gpu *h, int m) {
   return cholqr_rr(h);
 }
 
+// the non-collinear SCF's grids (on = 0 for scalar batches)
+SpinGrids spin_grids(const derek_gpu *h) {
+  SpinGrids g{};
+  g.on = h->all_spinor && h->d_mag_in != nullptr;
+  if (!g.on) return g;
+  g.tg = h->total_grid;
+  g.vnc_ext = h->d_vnc_ext;
+  g.mag_in = h->d_mag_in;
+  g.mag_out = h->d_mag;
+  g.bxc = h->d_bxc;
+  g.vnc64 = h->d_vnc64;
+  g.vnc32 = h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vnc32;
+  g.min_hist = h->d_min_hist;
+  g.mres_hist = h->d_mres_hist;
+  return g;
+}
+
+// a batch mixing spinor and scalar systems runs no SCF
+bool reject_mixed(derek_gpu *h, const char *what) {
+  if (!h->any_spinor || h->all_spinor) return false;
+  h->last_error = std::string(what) + ": a batch mixing spinor and scalar systems";
+  return true;
+}
+
 int finish_iteration(derek_gpu *h) {
-  launch_occupations(h->tab, h->nsys, h->d_eig, h->d_occ, h->d_occw, h->d_state, h->stream);
-  int st = density_items(h, h->cur_psi(), h->d_rho_out);
+  const SpinGrids sg = spin_grids(h);
+  launch_occupations(h->tab_band, h->nsys, h->d_eig, h->d_occ, h->d_occw, h->d_state, h->stream);
+  int st = sg.on ? density_spinor_items(h, h->cur_psi(), h->d_rho_out)
+                 : density_items(h, h->cur_psi(), h->d_rho_out);
   if (st) return st;
   launch_density_fft(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_out, h->d_cgrid,
                      h->stream);
   launch_energies(h->tab, h->nsys, h->d_vhxc, h->d_rho_in, h->d_rho_out, h->d_cgrid, h->d_epart, h->d_state,
-                  h->d_sys, h->d_status, h->stream);
+                  h->d_sys, h->d_status, sg, h->stream);
   launch_mix(h->tab, h->nsys, (int)h->max_nr, h->d_rho_in, h->d_rho_out, h->d_nin_hist,
              h->d_res_hist, h->d_hist_off, h->d_state, h->hist, h->d_gpart, h->d_cgrid,
-             h->opts.mix_alpha, h->opts.kerker_q0, h->max_nmax, h->stream);
+             h->opts.mix_alpha, h->opts.kerker_q0, h->max_nmax, sg, h->stream);
   launch_potential(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_in, h->d_cgrid,
                    h->d_vext, h->d_vhxc, h->d_vloc, h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vloc32,
-                   h->d_epart, h->d_state, 0, h->stream);
+                   h->d_epart, h->d_state, 0, sg, h->stream);
   DEREK_CUDA(h, cudaGetLastError());
   return DEREK_OK;
 }
@@ -143,9 +169,20 @@ int scf_start(derek_gpu *h, double etol) {
       DEREK_CUDA(h, cudaMemcpyAsync(h->d_rho_in + h->sys[s].grid_off, h->start_rho[s].data(),
                                     h->start_rho[s].size() * sizeof(double), cudaMemcpyHostToDevice,
                                     h->stream));
+  const SpinGrids sg = spin_grids(h);
+  if (sg.on) {
+    DEREK_CUDA(h, cudaMemsetAsync(h->d_mag_in, 0, 3 * (size_t)h->total_grid * sizeof(double), h->stream));
+    for (int s = 0; s < h->nsys && s < (int)h->start_mag.size(); ++s)
+      if (!h->start_mag[s].empty())
+        for (int c = 0; c < 3; ++c)
+          DEREK_CUDA(h, cudaMemcpyAsync(h->d_mag_in + c * h->total_grid + h->sys[s].grid_off,
+                                        h->start_mag[s].data() + (size_t)c * h->sys[s].nr,
+                                        (size_t)h->sys[s].nr * sizeof(double), cudaMemcpyHostToDevice,
+                                        h->stream));
+  }
   launch_potential(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_in, h->d_cgrid,
                    h->d_vext, h->d_vhxc, h->d_vloc, h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vloc32,
-                   h->d_epart, h->d_state, 1, h->stream);
+                   h->d_epart, h->d_state, 1, sg, h->stream);
   h->cur = 0;
   const int *pw = h->opts.init_vectors == 1 ? h->d_pw_entry : nullptr;
   if (h->prec == DEREK_PREC_FP64)
@@ -295,6 +332,14 @@ extern "C" int derek_scf_alloc(derek_gpu_t *h) {
   A(dalloc(&h->d_res_hist, hoff));
   A(dalloc(&h->d_epart, (size_t)h->nsys * 64 * 8));
   A(dalloc(&h->d_gpart, (size_t)h->nsys * 64 * kMaxHist));
+  if (h->all_spinor) {
+    A(dalloc(&h->d_mag_in, 3 * (size_t)h->total_grid));
+    A(dalloc(&h->d_bxc, 3 * (size_t)h->total_grid));
+    A(dalloc(&h->d_min_hist, 3 * (size_t)hoff));
+    A(dalloc(&h->d_mres_hist, 3 * (size_t)hoff));
+    A(cudaMemset(h->d_mag_in, 0, 3 * (size_t)h->total_grid * sizeof(double)));
+    A(cudaMemset(h->d_bxc, 0, 3 * (size_t)h->total_grid * sizeof(double)));
+  }
   A(cudaMemcpy(h->d_mat_off, h->mat_off.data(), h->mat_off.size() * sizeof(long long),
                cudaMemcpyHostToDevice));
   A(cudaMemcpy(h->d_opart_off, opart_off.data(), opart_off.size() * sizeof(long long),
@@ -313,7 +358,7 @@ extern "C" void derek_scf_free(derek_gpu_t *h) {
   void *ptrs[] = {h->d_state,  h->d_S,      h->d_Hs,       h->d_C,        h->d_scratch,
                   h->d_opart,  h->d_mat_off, h->d_opart_off, h->d_hist_off, h->d_status,
                   h->d_sweeps, h->d_coef_all, h->d_nin_hist, h->d_res_hist, h->d_epart,
-                  h->d_gpart,  h->d_rot_img};
+                  h->d_gpart,  h->d_rot_img, h->d_mag_in, h->d_bxc, h->d_min_hist, h->d_mres_hist};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -365,7 +410,7 @@ int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
 
 int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
   if (!h) return DEREK_ERR_BAD_ARG;
-  if (reject_spinor(h, "scf_iterate")) return DEREK_ERR_UNSUPPORTED;
+  if (reject_mixed(h, "scf_iterate")) return DEREK_ERR_UNSUPPORTED;
   int s = one_iteration(h, 0.0);
   if (s) return s;
   std::vector<SysState> st;
@@ -379,10 +424,7 @@ int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
 
 int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, int *iterations) {
   if (!h || max_iter <= 0 || !(eig_tol > 0) || nconv < 0) return DEREK_ERR_BAD_ARG;
-  if (h->any_spinor && !h->all_spinor) {
-    h->last_error = "nscf_run: a batch mixing spinor and scalar systems";
-    return DEREK_ERR_UNSUPPORTED;
-  }
+  if (reject_mixed(h, "nscf_run")) return DEREK_ERR_UNSUPPORTED;
   // frozen potential: the filter's upper bound from max V_loc of each system
   for (auto &s : h->sys) s.active = 1;
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
@@ -475,7 +517,7 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, 
 
 int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol, derek_scf_report *rep) {
   if (!h || max_scf <= 0 || !(etol > 0)) return DEREK_ERR_BAD_ARG;
-  if (reject_spinor(h, "scf_run")) return DEREK_ERR_UNSUPPORTED;
+  if (reject_mixed(h, "scf_run")) return DEREK_ERR_UNSUPPORTED;
   h->scf_started = false;
   std::vector<SysState> st;
   for (int it = 0; it < max_scf; ++it) {
@@ -516,6 +558,36 @@ static int get_items(derek_gpu_t *h, int s, const double *src, double *out) {
 
 int derek_gpu_get_eigenvalues(derek_gpu_t *h, int s, double *e) { return get_items(h, s, h ? h->d_eig : nullptr, e); }
 int derek_gpu_get_occupations(derek_gpu_t *h, int s, double *o) { return get_items(h, s, h ? h->d_occ : nullptr, o); }
+
+int derek_gpu_get_magnetisation(derek_gpu_t *h, int s, double *mag) {
+  if (!h || s < 0 || s >= h->nsys || !mag) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  if (S.nspinor != 2 || !h->d_mag) {
+    h->last_error = "get_magnetisation: system is not a spinor system";
+    return DEREK_ERR_BAD_ARG;
+  }
+  for (int c = 0; c < 3; ++c)
+    DEREK_CUDA(h, cudaMemcpyAsync(mag + (size_t)c * S.nr, h->d_mag + c * h->total_grid + S.grid_off,
+                                  (size_t)S.nr * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DEREK_OK;
+}
+
+int derek_gpu_set_start_magnetisation(derek_gpu_t *h, int s, const double *mag) {
+  if (!h || s < 0 || s >= h->nsys) return DEREK_ERR_BAD_ARG;
+  const SysDev &S = h->sys[s];
+  if (S.nspinor != 2) {
+    h->last_error = "set_start_magnetisation: system is not a spinor system";
+    return DEREK_ERR_BAD_ARG;
+  }
+  if ((int)h->start_mag.size() < h->nsys) h->start_mag.resize(h->nsys);
+  if (!mag)
+    h->start_mag[s].clear();
+  else
+    h->start_mag[s].assign(mag, mag + 3 * (size_t)S.nr);
+  h->scf_started = false;
+  return DEREK_OK;
+}
 
 int derek_gpu_get_density(derek_gpu_t *h, int s, double *rho) {
   if (!h || s < 0 || s >= h->nsys || !rho) return DEREK_ERR_BAD_ARG;

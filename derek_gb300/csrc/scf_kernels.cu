@@ -115,8 +115,12 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
   const int s = blockIdx.x;
   const SysDev &S = t.sys[s];
   if (!S.active) return;
-  // only the requested bands are occupied; the buffer bands get f = 0
-  const int nb = S.nbr, nk = S.nk;
+  // only the requested bands are occupied; the buffer bands get f = 0.  A
+  // scalar band holds up to two electrons, a spinor band one; t is the band
+  // view, so band j's eigenvalue is eig[item0 + j] either way
+  const int nsp = S.nspinor;
+  const double g = nsp == 2 ? 1.0 : 2.0;
+  const int nb = S.nbr / nsp, nk = S.nk;
   const int ntot = nb * nk;
   const double kT = S.kT, ne = S.nelec;
   // bracket
@@ -155,8 +159,8 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
       const KSetDev &K = t.ks[S.ks0 + i / nb];
       const double x = fmin(fmax((eig[K.item0 + i % nb] - mu) / kT, -200.0), 200.0);
       const double f = 1.0 / (1.0 + exp(x));
-      cnt += K.wk * 2.0 * f;
-      der += K.wk * 2.0 * f * (1.0 - f) / kT;
+      cnt += K.wk * g * f;
+      der += K.wk * g * f * (1.0 - f) / kT;
     }
     cnt = block_sum(cnt, red);
     der = block_sum(der, red);
@@ -175,30 +179,35 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
     if (s_done) break;
   }
   const double mu = s_mu;
+  // S.nb items per k-set (both components of a spinor band are items)
   for (int i = threadIdx.x; i < nk * S.nb; i += blockDim.x) {
     const KSetDev &K = t.ks[S.ks0 + i / S.nb];
-    if (i % S.nb >= nb) {
-      occ[K.item0 + i % S.nb] = 0.0;
-      occw[K.item0 + i % S.nb] = 0.0;
-    }
+    occ[K.item0 + i % S.nb] = 0.0;
+    occw[K.item0 + i % S.nb] = 0.0;
   }
+  __syncthreads();
   double ent = 0, eb = 0;
   for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
     const KSetDev &K = t.ks[S.ks0 + i / nb];
-    const int item = K.item0 + i % nb;
-    const double e = eig[item];
+    const int j = i % nb;
+    const double e = eig[K.item0 + j];
     const double x = fmin(fmax((e - mu) / kT, -200.0), 200.0);
     const double f = 1.0 / (1.0 + exp(x));
-    occ[item] = 2.0 * f;
-    occw[item] = K.wk * 2.0 * f / S.volume;
+    occ[K.item0 + j] = g * f;
+    if (nsp == 2) {
+      occw[K.item0 + 2 * j] = K.wk * f / S.volume;
+      occw[K.item0 + 2 * j + 1] = K.wk * f / S.volume;
+    } else {
+      occw[K.item0 + j] = K.wk * g * f / S.volume;
+    }
     if (f > 0.0 && f < 1.0) ent += K.wk * (f * log(f) + (1.0 - f) * log1p(-f));
-    eb += K.wk * 2.0 * f * e;
+    eb += K.wk * g * f * e;
   }
   ent = block_sum(ent, red);
   eb = block_sum(eb, red);
   if (threadIdx.x == 0) {
     st[s].mu = mu;
-    st[s].entropy = -2.0 * ent;
+    st[s].entropy = -g * ent;
     st[s].e_band = eb;
   }
 }
@@ -208,7 +217,7 @@ __global__ void __launch_bounds__(256) k_energy_partials(const Tables t, const d
                                                          const double *__restrict__ rho_in,
                                                          const double *__restrict__ rho_out,
                                                          const double2 *__restrict__ cgrid,
-                                                         double *__restrict__ part) {
+                                                         double *__restrict__ part, const SpinGrids sg) {
   __shared__ double red[256];
   const int s = blockIdx.y;
   const SysDev &S = t.sys[s];
@@ -222,7 +231,23 @@ __global__ void __launch_bounds__(256) k_energy_partials(const Tables t, const d
     q3 = fmax(q3, fabs(nr - rho_in[S.grid_off + r]));
     q0 += vhxc[S.grid_off + r] * nr;
     double e, v;
-    lda_point(nr, e, v);
+    if (sg.on) {
+      // non-collinear: double counting tr(V_Hxc rho_out) = v n + b.m, and
+      // E_xc of (n, |m|) as spin densities (n +/- |m|)/2
+      const long long i = S.grid_off + r;
+      double m2 = 0.0;
+      for (int c = 0; c < 3; ++c) {
+        const double mo = sg.mag_out[c * sg.tg + i];
+        q0 += sg.bxc[c * sg.tg + i] * mo;
+        q3 = fmax(q3, fabs(mo - sg.mag_in[c * sg.tg + i]));
+        m2 += mo * mo;
+      }
+      const double am = sqrt(m2);
+      double va, vb;
+      lsda_point(0.5 * (nr + am), 0.5 * (nr - am), e, va, vb);
+    } else {
+      lda_point(nr, e, v);
+    }
     q1 += nr * e;
     const double g2 = gsq(S, r);
     if (g2 > 0) {
@@ -435,6 +460,76 @@ __global__ void __launch_bounds__(256) k_mix_combine(const Tables t, double *__r
   }
 }
 
+// ---- non-collinear: the magnetisation joins the Pulay vector (n, m).  Its
+// history holds 3 x nr values per slot at 3 hist_off[s]; its residual dots
+// add to the charge's Gram partials; it combines with the same coefficients
+// (no Kerker: that preconditions the charge alone).
+__global__ void __launch_bounds__(256) k_mix_store_m(const Tables t, const SpinGrids sg,
+                                                     const long long *__restrict__ hist_off,
+                                                     const SysState *__restrict__ st, int H) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const int slot = (st[s].slot + 1) % H;
+  const long long n = S.nr;
+  double *ni = sg.min_hist + 3 * hist_off[s] + (long long)slot * 3 * n;
+  double *re = sg.mres_hist + 3 * hist_off[s] + (long long)slot * 3 * n;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < 3 * n;
+       r += (long long)gridDim.x * blockDim.x) {
+    const long long c = r / n, i = S.grid_off + (r - c * n);
+    const double a = sg.mag_in[c * sg.tg + i];
+    ni[r] = a;
+    re[r] = sg.mag_out[c * sg.tg + i] - a;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mix_gram_m(const Tables t, const SpinGrids sg,
+                                                    const long long *__restrict__ hist_off,
+                                                    const SysState *__restrict__ st, int H,
+                                                    double *__restrict__ part) {
+  __shared__ double red[256];
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const int slot = (st[s].slot + 1) % H;
+  const int m = min(st[s].nhist + 1, H);
+  const long long n = 3 * (long long)S.nr;
+  const long long chunk = (n + RB - 1) / RB;
+  const long long r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+  const double *rs = sg.mres_hist + 3 * hist_off[s] + (long long)slot * n;
+  for (int j = 0; j < m; ++j) {
+    const double *rj = sg.mres_hist + 3 * hist_off[s] + (long long)j * n;
+    double q = 0;
+    for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) q += rs[r] * rj[r];
+    q = block_sum(q, red);
+    if (threadIdx.x == 0) part[((long long)s * RB + blockIdx.x) * kMaxHist + j] += q;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mix_combine_m(const Tables t, const SpinGrids sg,
+                                                       const long long *__restrict__ hist_off,
+                                                       const SysState *__restrict__ st, double alpha) {
+  const int s = blockIdx.y;
+  const SysDev &S = t.sys[s];
+  if (!S.active) return;
+  const int m = st[s].nhist;
+  double c[kMaxHist];
+  for (int j = 0; j < kMaxHist; ++j) c[j] = j < m ? st[s].coef[j] : 0.0;
+  const long long n = 3 * (long long)S.nr;
+  const double *ni = sg.min_hist + 3 * hist_off[s];
+  const double *re = sg.mres_hist + 3 * hist_off[s];
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
+       r += (long long)gridDim.x * blockDim.x) {
+    double a = 0, b = 0;
+    for (int j = 0; j < m; ++j) {
+      a += c[j] * ni[(long long)j * n + r];
+      b += c[j] * re[(long long)j * n + r];
+    }
+    const long long cc = r / S.nr, i = S.grid_off + (r - cc * S.nr);
+    sg.mag_in[cc * sg.tg + i] = a + alpha * b;
+  }
+}
+
 // cgrid <- alpha G^2/(G^2 + q0^2) cgrid / N (the /N undoes the unnormalised pair)
 __global__ void __launch_bounds__(256) k_kerker_scale(const Tables t, double2 *__restrict__ cgrid,
                                                       double alpha, double q0) {
@@ -495,7 +590,7 @@ __global__ void __launch_bounds__(256) k_build_vloc(const Tables t, const double
                                                     double *__restrict__ vhxc,
                                                     double *__restrict__ vloc,
                                                     float *__restrict__ vloc32,
-                                                    double *__restrict__ part, int all) {
+                                                    double *__restrict__ part, int all, const SpinGrids sg) {
   __shared__ double red[256];
   const int s = blockIdx.y;
   const SysDev &S = t.sys[s];
@@ -507,6 +602,38 @@ __global__ void __launch_bounds__(256) k_build_vloc(const Tables t, const double
   for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const long long i = S.grid_off + r;
     double e, v;
+    if (sg.on) {
+      // non-collinear: V = V_ext + (V_H + (v_up + v_down)/2) I + b.sigma with
+      // b = (v_up - v_down)/2 m/|m|, spin densities (n +/- |m|)/2 of n_in, m_in
+      const long long tg = sg.tg;
+      const double mx = sg.mag_in[i], my = sg.mag_in[tg + i], mz = sg.mag_in[2 * tg + i];
+      const double am = sqrt(mx * mx + my * my + mz * mz);
+      const double n = rho_in[i];
+      double va, vb;
+      lsda_point(0.5 * (n + am), 0.5 * (n - am), e, va, vb);
+      const double hx = vh[i].x + 0.5 * (va + vb);
+      const double sc = am > 0.0 ? 0.5 * (va - vb) / am : 0.0;
+      const double bx = sc * mx, by = sc * my, bz = sc * mz;
+      sg.bxc[i] = bx;
+      sg.bxc[tg + i] = by;
+      sg.bxc[2 * tg + i] = bz;
+      vhxc[i] = hx;
+      const double2 *x = sg.vnc_ext + 4 * i;
+      const double2 w[4] = {make_double2(x[0].x + hx + bz, x[0].y), make_double2(x[1].x + bx, x[1].y + by),
+                            make_double2(x[2].x + bx, x[2].y - by), make_double2(x[3].x + hx - bz, x[3].y)};
+      for (int c = 0; c < 4; ++c) {
+        sg.vnc64[4 * i + c] = w[c];
+        if (sg.vnc32) sg.vnc32[4 * i + c] = make_float2((float)w[c].x, (float)w[c].y);
+      }
+      const double vl = 0.5 * (w[0].x + w[3].x);
+      vloc[i] = vl;
+      if (vloc32) vloc32[i] = (float)vl;
+      // filter bound: largest eigenvalue of the Hermitian part of V
+      const double ore = 0.5 * (w[2].x + w[1].x), oim = 0.5 * (w[2].y - w[1].y);
+      const double hd = 0.5 * (w[0].x - w[3].x);
+      vm = fmax(vm, vl + sqrt(hd * hd + ore * ore + oim * oim));
+      continue;
+    }
     lda_point(rho_in[i], e, v);
     const double hx = vh[i].x + v;
     vhxc[i] = hx;
@@ -564,21 +691,25 @@ void launch_occupations(const Tables &t, int nsys, const double *eig, double *oc
 
 void launch_energies(const Tables &t, int nsys, const double *vhxc, const double *rho_in,
                      const double *rho_out, const double2 *cgrid, double *part, SysState *st,
-                     SysDev *sys_rw, const int *ks_status, cudaStream_t s) {
-  derek::note_launch(), k_energy_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, vhxc, rho_in, rho_out, cgrid, part);
+                     SysDev *sys_rw, const int *ks_status, const SpinGrids &sg, cudaStream_t s) {
+  derek::note_launch(), k_energy_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, vhxc, rho_in, rho_out, cgrid, part, sg);
   derek::note_launch(), k_energy_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, sys_rw, ks_status);
 }
 
 void launch_mix(const Tables &t, int nsys, int max_nr, double *rho_in, const double *rho_out,
                 double *nin_hist, double *res_hist, const long long *hist_off, SysState *st, int H,
-                double *part, double2 *cgrid, double alpha, double q0, int max_n, cudaStream_t s) {
+                double *part, double2 *cgrid, double alpha, double q0, int max_n, const SpinGrids &sg,
+                cudaStream_t s) {
   const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
   derek::note_launch(), k_mix_store<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, rho_out, nin_hist, res_hist, hist_off, st, H);
+  if (sg.on) derek::note_launch(), k_mix_store_m<<<dim3(gx, nsys), 256, 0, s>>>(t, sg, hist_off, st, H);
   derek::note_launch(), k_mix_gram_partials<<<dim3(RB, nsys), 256, 0, s>>>(t, res_hist, hist_off, st, H, part);
+  if (sg.on) derek::note_launch(), k_mix_gram_m<<<dim3(RB, nsys), 256, 0, s>>>(t, sg, hist_off, st, H, part);
   derek::note_launch(), k_mix_solve<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, H);
   const int kerker = q0 > 0;
   derek::note_launch(), k_mix_combine<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, nin_hist, res_hist, hist_off, st, cgrid,
                                                alpha, kerker);
+  if (sg.on) derek::note_launch(), k_mix_combine_m<<<dim3(gx, nsys), 256, 0, s>>>(t, sg, hist_off, st, alpha);
   if (kerker) {
     launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
     derek::note_launch(), k_kerker_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, alpha, q0);
@@ -589,14 +720,31 @@ void launch_mix(const Tables &t, int nsys, int max_nr, double *rho_in, const dou
 
 void launch_potential(const Tables &t, int nsys, int max_nr, int max_n, const double *rho_in,
                       double2 *cgrid, const double *vext, double *vhxc, double *vloc, float *vloc32,
-                      double *part, SysState *st, int all, cudaStream_t s) {
+                      double *part, SysState *st, int all, const SpinGrids &sg, cudaStream_t s) {
   const int gx = (int)std::min<long long>(((long long)max_nr + 255) / 256, 256);
   derek::note_launch(), k_real_to_complex<<<dim3(gx, nsys), 256, 0, s>>>(t, rho_in, cgrid, all);
   launch_fft3d_grid(t, 0, nsys, max_n, cgrid, -1, s);
   derek::note_launch(), k_hartree_scale<<<dim3(gx, nsys), 256, 0, s>>>(t, cgrid, all);
   launch_fft3d_grid(t, 0, nsys, max_n, cgrid, +1, s);
-  derek::note_launch(), k_build_vloc<<<dim3(RB, nsys), 256, 0, s>>>(t, rho_in, cgrid, vext, vhxc, vloc, vloc32, part, all);
+  derek::note_launch(), k_build_vloc<<<dim3(RB, nsys), 256, 0, s>>>(t, rho_in, cgrid, vext, vhxc, vloc, vloc32, part, all, sg);
   derek::note_launch(), k_vmax_final<<<(nsys + 63) / 64, 64, 0, s>>>(t, nsys, part, st, all);
+}
+
+__global__ void k_lsda(long n, const double *__restrict__ ra, const double *__restrict__ rb,
+                       double *__restrict__ exc, double *__restrict__ va, double *__restrict__ vb) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double e, a, b;
+    lsda_point(ra[i], rb[i], e, a, b);
+    exc[i] = e;
+    va[i] = a;
+    vb[i] = b;
+  }
+}
+
+void launch_lsda(long n, const double *rho_a, const double *rho_b, double *exc, double *va, double *vb,
+                 cudaStream_t s) {
+  const int blocks = (int)std::min<long>((n + 255) / 256, 152 * 8);
+  derek::note_launch(), k_lsda<<<blocks, 256, 0, s>>>(n, rho_a, rho_b, exc, va, vb);
 }
 
 void launch_density_fft(const Tables &t, int nsys, int max_nr, int max_n, const double *rho,

@@ -73,8 +73,7 @@ typedef struct {
   const double *kpts;      /* nk*3 fractional (reciprocal basis) */
   const double *wk;        /* nk weights summing to 1; NULL = uniform */
   int    nbands;           /* n_electrons + conduction_bands (io.f90:316) */
-  int    nspinor;          /* 1, or 2: non-collinear spinor bands (H.psi,
-                              overlaps and densities; no SCF) */
+  int    nspinor;          /* 1, or 2: non-collinear spinor bands */
   double nelec;            /* n_electrons */
   double kT;               /* electronic_temp converted to Ha, > 0 */
   const double *vext;      /* nr FP64 values, or NULL to build from wells */
@@ -185,13 +184,29 @@ int derek_gpu_density(derek_gpu_t *h, int sys, const double *occ, double *rho);
  *     mag = [3][nr] real (den%spin(:, 1:3));
  *   set_vloc(v) sets nc_pot = diag(v, v); set_nc_pot takes the reference's
  *     nc_pot(nr, 2, 2) complex128 (element (n, i, j) at n + nr (i + 2 j)),
- *     nc_pot = V I + mu_B sigma.B with mu_B = 1/2 (Source/xsf.f90:44-51).
- * The SCF, NSCF, gradient and timing entry points return
- * DEREK_ERR_UNSUPPORTED on a handle holding a spinor system. */
+ *     nc_pot = V I + mu_B sigma.B with mu_B = 1/2 (Source/xsf.f90:44-51);
+ *     it is also the SCF's external potential (set_vext: diag(V_ext));
+ *   scf_run / scf_iterate: the non-collinear SCF.  A band holds one
+ *     electron; V = nc_ext + (V_H + (v_up + v_down)/2) I + b.sigma with
+ *     b = (v_up - v_down)/2 m/|m| from the spin-polarised LDA (Slater + PW92)
+ *     of the spin densities (n +/- |m|)/2; Pulay mixing of (n, m); the
+ *     energy's double counting is int (V_Hxc n + b.m).  The start
+ *     magnetisation is zero unless set_start_magnetisation gives one;
+ *     get_magnetisation returns m of the last density pass;
+ *   nscf_run: band energies in the frozen nc_pot.
+ * A batch mixing spinor and scalar systems runs no SCF or NSCF; the
+ * gradient and timing entry points run scalar batches only
+ * (DEREK_ERR_UNSUPPORTED). */
 int derek_gpu_set_nc_pot(derek_gpu_t *h, int sys, const double *nc_pot);
 int derek_gpu_get_nc_pot(derek_gpu_t *h, int sys, double *nc_pot);
 int derek_gpu_density_spinor(derek_gpu_t *h, int sys, const double *occ /* nk*nbands */,
                              double *rho /* nr, or NULL */, double *mag /* 3*nr, or NULL */);
+int derek_gpu_get_magnetisation(derek_gpu_t *h, int sys, double *mag /* 3*nr */);
+int derek_gpu_set_start_magnetisation(derek_gpu_t *h, int sys, const double *mag /* 3*nr, NULL = zero */);
+/* Spin-polarised LDA_X + LDA_C_PW (libxc 6.2.2 conventions) on n points:
+ * energy per particle and d(n exc)/dn_up, d(n exc)/dn_down. */
+int derek_gpu_xc_lsda(derek_gpu_t *h, long n, const double *rho_up, const double *rho_down,
+                      double *exc, double *v_up, double *v_down);
 
 /* LDA (Slater exchange + Perdew-Wang 92 correlation, libxc ids 1 + 12),
  * spin-unpolarised: exc = energy per particle, vxc = potential. */

@@ -627,17 +627,19 @@ def hartree(sys: System, rho: np.ndarray):
     return vh, eh
 
 
-def fermi_occupations(eigs: np.ndarray, wk: np.ndarray, nelec: float, kT: float, tol: float = 1e-14):
-    """Fermi-Dirac occupations f in [0,2] (spin-unpolarised) with the Fermi
-    level found by bisection so that sum_k w_k sum_n f_nk = Ne.
-    Returns (f, mu, entropy) where entropy S = -2 sum w f~ ln f~ + (1-f~) ln(1-f~),
-    f~ = f/2, so that the free energy is E - kT S."""
+def fermi_occupations(eigs: np.ndarray, wk: np.ndarray, nelec: float, kT: float, tol: float = 1e-14,
+                      g: float = 2.0):
+    """Fermi-Dirac occupations f in [0, g] (g = 2 for spin-degenerate bands,
+    1 for spinor bands) with the Fermi level found by bisection so that
+    sum_k w_k sum_n f_nk = Ne.  Returns (f, mu, entropy) where entropy
+    S = -g sum w f~ ln f~ + (1-f~) ln(1-f~), f~ = f/g, so that the free
+    energy is E - kT S."""
     lo = float(eigs.min()) - 50.0 * kT - 1.0
     hi = float(eigs.max()) + 50.0 * kT + 1.0
 
     def count(mu):
         x = np.clip((eigs - mu) / kT, -200.0, 200.0)
-        f = 2.0 / (1.0 + np.exp(x))
+        f = g / (1.0 + np.exp(x))
         return float((wk[:, None] * f).sum())
 
     for _ in range(200):
@@ -653,8 +655,8 @@ def fermi_occupations(eigs: np.ndarray, wk: np.ndarray, nelec: float, kT: float,
     ft = 1.0 / (1.0 + np.exp(x))
     with np.errstate(divide="ignore", invalid="ignore"):
         s = np.where((ft > 0) & (ft < 1), ft * np.log(ft) + (1 - ft) * np.log1p(-ft), 0.0)
-    entropy = -2.0 * float((wk[:, None] * s).sum())
-    return 2.0 * ft, mu, entropy
+    entropy = -g * float((wk[:, None] * s).sum())
+    return g * ft, mu, entropy
 
 
 class PulayMixer:
@@ -776,4 +778,98 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
             break
         e_prev = free
         nin = mixer.mix(nin, nout)
+    return result
+
+
+# --------------------------------------------------------------------------
+# Non-collinear SCF (spinor bands, nspinor = 2)
+# --------------------------------------------------------------------------
+
+def xc_noncollinear(n: np.ndarray, m: np.ndarray):
+    """(eps_xc, vbar, b) of the spin-polarised LDA on the local spin
+    densities (n +/- |m|)/2: V_xc = vbar I + b.sigma with vbar = (v_up +
+    v_down)/2 and b = (v_up - v_down)/2 m/|m| (b = 0 where m = 0)."""
+    am = np.linalg.norm(m, axis=0)
+    ex, vx, ec, vc = lda_pol(0.5 * (n + am), 0.5 * (n - am))
+    va, vb = vx[:, 0] + vc[:, 0], vx[:, 1] + vc[:, 1]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        sc = np.where(am > 0.0, 0.5 * (va - vb) / am, 0.0)
+    return ex + ec, 0.5 * (va + vb), sc[None, :] * m
+
+
+@dataclass
+class SpinorScfResult:
+    converged: bool
+    iterations: int
+    energy: float
+    free_energy: float
+    efermi: float
+    eigenvalues: np.ndarray   # (nk, nb)
+    occupations: np.ndarray   # (nk, nb), f in [0, 1]
+    density: np.ndarray       # n_out
+    magnetisation: np.ndarray  # m_out, (3, nr)
+    history: list
+
+
+def scf_spinor(sys: System, nc_ext: np.ndarray, max_scf: int = 100, etol: float = 1e-10,
+               alpha: float = 0.3, history: int = 8, start_m: np.ndarray = None,
+               verbose: bool = False) -> SpinorScfResult:
+    """Non-collinear SCF in an external 2x2 potential nc_ext (nr, 2, 2).
+
+    Each iteration diagonalises the dense spinor Hamiltonian of
+    nc = nc_ext + (V_H[n_in] + vbar) I + b.sigma exactly, fills spinor bands
+    (one electron each) with Fermi-Dirac occupations, forms n_out and m_out,
+    evaluates E = sum w f eps - int (V_Hxc n_out + b.m_out) + E_H[n_out] +
+    E_xc[n_out, m_out] and mixes (n, m) with Pulay on the stacked vector
+    (plain dot, alpha, no Kerker).  Start: uniform n, m = start_m or 0.
+    """
+    import scipy.linalg as sla
+
+    kbs = [KBasis(sys, ik) for ik in range(len(sys.kpts))]
+    N = sys.nr
+    dv = sys.volume / N
+    nin = np.full(N, sys.nelec / sys.volume)
+    min_ = np.zeros((3, N)) if start_m is None else np.array(start_m, dtype=np.float64).reshape(3, N)
+    mixer = PulayMixer(sys, alpha=alpha, history=history, q0=0.0)
+    e_prev, hist, result = None, [], None
+    for it in range(1, max_scf + 1):
+        vh, _ = hartree(sys, nin)
+        _, vbar, b = xc_noncollinear(nin, min_)
+        vhxc = vh + vbar
+        nc = np.array(nc_ext, dtype=np.complex128, copy=True)
+        nc[:, 0, 0] += vhxc + b[2]
+        nc[:, 1, 1] += vhxc - b[2]
+        nc[:, 0, 1] += b[0] - 1j * b[1]
+        nc[:, 1, 0] += b[0] + 1j * b[1]
+        eigs = np.zeros((len(kbs), sys.nbands))
+        vecs = []
+        for ik, kb in enumerate(kbs):
+            w, v = sla.eigh(dense_h_spinor(sys, kb, nc), subset_by_index=[0, sys.nbands - 1], driver="evr")
+            eigs[ik] = w
+            vecs.append(v.T.reshape(sys.nbands, 2, kb.npw).transpose(1, 0, 2).copy())
+        f, mu, ent = fermi_occupations(eigs, sys.wk, sys.nelec, sys.kT, g=1.0)
+        nout = np.zeros(N)
+        mout = np.zeros((3, N))
+        for ik, kb in enumerate(kbs):
+            n_k, m_k = spinor_density(sys, kb, vecs[ik], f[ik])
+            nout += sys.wk[ik] * n_k
+            mout += sys.wk[ik] * m_k
+        eband = float((sys.wk[:, None] * f * eigs).sum())
+        _, eh = hartree(sys, nout)
+        e_out, _, _ = xc_noncollinear(nout, mout)
+        exc = dv * float(np.dot(nout, e_out))
+        e_dc = dv * (float(np.dot(vhxc, nout)) + float(np.sum(b * mout)))
+        energy = eband - e_dc + eh + exc
+        free = energy - sys.kT * ent
+        resid = max(float(np.max(np.abs(nout - nin))), float(np.max(np.abs(mout - min_))))
+        hist.append((it, energy, free, mu, resid))
+        if verbose:
+            print(f"scf {it:3d} E={energy:.12f} F={free:.12f} mu={mu:.8f} |R|={resid:.2e}")
+        result = SpinorScfResult(False, it, energy, free, mu, eigs, f, nout, mout, hist)
+        if e_prev is not None and abs(free - e_prev) < etol:
+            result.converged = True
+            break
+        e_prev = free
+        x = mixer.mix(np.concatenate([nin, min_.ravel()]), np.concatenate([nout, mout.ravel()]))
+        nin, min_ = x[:N], x[N:].reshape(3, N)
     return result

@@ -284,3 +284,88 @@ def test_spinor_potential_setters_and_limits(oracle):
                              nspinor=2)
     with pytest.raises(dg.DerekError):
         dg.Handle(too_many)   # a spinor band holds one electron
+
+
+# ---- non-collinear SCF
+def scf_pair(oracle, nb_spinor=8):
+    import derek_gb300 as dg
+    rng = np.random.default_rng(0)
+    wells = oracle.random_wells(rng, 2)
+    s = oracle.make_system(6.0, 4.0, 4.0, nb_spinor, wells, kT=0.02)
+    spec = dg.SystemSpec(s.cell, s.ecut, s.kpts, nb_spinor, s.nelec, kT=s.kT, vext=s.vext, n_fine=s.n_fine,
+                         inv_cell=oracle.inv_cell(s.cell), nspinor=2)
+    return s, spec
+
+
+def spiral_field(oracle, s, b0=0.6, bz=0.3):
+    ph = 2.0 * np.pi * oracle.real_frac_points(s.n_fine)[:, 0]
+    return np.stack([b0 * np.cos(ph), b0 * np.sin(ph), np.full_like(ph, bz)])
+
+
+@pytest.mark.gpu
+def test_lsda_matches_oracle(oracle):
+    import derek_gb300 as dg
+    rng = np.random.default_rng(12)
+    tot = 10 ** rng.uniform(-12, 3, 5000)
+    z = rng.uniform(-1, 1, tot.size)
+    z[:20], z[20:40], z[40:60] = 1.0, -1.0, 0.0
+    ra, rb = tot * (1 + z) / 2, tot * (1 - z) / 2
+    ex, vx, ec, vc = oracle.lda_pol(ra, rb)
+    s, spec = make_spinor_pair(oracle)
+    with dg.Handle(spec) as h:
+        e, va, vb = h.xc_lsda(ra, rb)
+    assert np.max(np.abs(e - (ex + ec)) / np.abs(ex + ec)) < 1e-13
+    v = np.stack([va, vb], 1)
+    ref = vx + vc
+    assert np.max(np.abs(v - ref) / np.abs(ref).max(axis=1, keepdims=True)) < 1e-13
+
+
+@pytest.mark.gpu
+def test_spinor_scf_zero_field_matches_scalar(oracle):
+    """With no field and no start magnetisation the spinor SCF is the scalar
+    SCF: every level twice, m = 0, the same F and Fermi level."""
+    import derek_gb300 as dg
+    s, spec = scf_pair(oracle, nb_spinor=8)
+    scalar = dg.SystemSpec(s.cell, s.ecut, s.kpts, 4, s.nelec, kT=s.kT, vext=s.vext, n_fine=s.n_fine,
+                           inv_cell=oracle.inv_cell(s.cell))
+    with dg.Handle(scalar) as h:
+        r0 = h.electronic_scf(max_scf=60, etol=1e-11)[0]
+        e0 = h.eigenvalues()[0]
+    with dg.Handle(spec) as h:
+        r1 = h.electronic_scf(max_scf=60, etol=1e-11)[0]
+        e1 = h.eigenvalues()[0]
+        m = h.magnetisation()
+        occ = h.occupations()[0]
+    assert r1.converged and abs(r1.free_energy - r0.free_energy) < 1e-9
+    assert abs(r1.efermi - r0.efermi) < 1e-8
+    assert np.max(np.abs(e1 - np.repeat(e0, 2))) < 1e-8
+    assert np.max(np.abs(m)) < 1e-10 and np.max(occ) <= 1.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-8), (1, 2e-6)])
+def test_spinor_scf_spiral_field_matches_oracle(oracle, precision, tol):
+    """A spiral external field (nc_pot = V_ext I + mu_B sigma.B(r)) induces a
+    non-collinear magnetisation; F, E, mu, the band energies and m against
+    the oracle's dense non-collinear SCF."""
+    import derek_gb300 as dg
+    s, spec = scf_pair(oracle)
+    nc = oracle.nc_from_fields(s.vext, spiral_field(oracle, s))
+    ref = oracle.scf_spinor(s, nc, etol=1e-12)
+    assert ref.converged
+    with dg.Handle(spec, precision=precision) as h:
+        h.set_nc_pot(nc)
+        r = h.electronic_scf(max_scf=80, etol=1e-11 if precision == 0 else 1e-8)[0]
+        eig = h.eigenvalues()[0]
+        m = h.magnetisation()
+        n = h.density()
+    assert r.converged
+    assert abs(r.free_energy - ref.free_energy) < tol
+    assert abs(r.energy - ref.energy) < tol
+    assert abs(r.efermi - ref.efermi) < 10 * tol
+    assert np.max(np.abs(eig - ref.eigenvalues[0])) < 10 * tol
+    assert np.max(np.abs(m - ref.magnetisation)) < 100 * tol * np.max(np.abs(ref.magnetisation)) + 1e-9
+    assert np.max(np.abs(n - ref.density)) < 100 * tol * np.max(ref.density)
+    # the moment is not along one axis: m and B(r) turn together
+    ang = (m * spiral_field(oracle, s)).sum(0) / np.linalg.norm(m, axis=0) / np.linalg.norm(spiral_field(oracle, s), axis=0)
+    assert np.all(ang < -0.5)
