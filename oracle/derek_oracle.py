@@ -813,7 +813,7 @@ class SpinorScfResult:
 
 def scf_spinor(sys: System, nc_ext: np.ndarray, max_scf: int = 100, etol: float = 1e-10,
                alpha: float = 0.3, history: int = 8, start_m: np.ndarray = None,
-               verbose: bool = False) -> SpinorScfResult:
+               verbose: bool = False, rtol: float = None) -> SpinorScfResult:
     """Non-collinear SCF in an external 2x2 potential nc_ext (nr, 2, 2).
 
     Each iteration diagonalises the dense spinor Hamiltonian of
@@ -822,6 +822,7 @@ def scf_spinor(sys: System, nc_ext: np.ndarray, max_scf: int = 100, etol: float 
     evaluates E = sum w f eps - int (V_Hxc n_out + b.m_out) + E_H[n_out] +
     E_xc[n_out, m_out] and mixes (n, m) with Pulay on the stacked vector
     (plain dot, alpha, no Kerker).  Start: uniform n, m = start_m or 0.
+    With rtol set, convergence also needs max|(n, m)_out - (n, m)_in| < rtol.
     """
     import scipy.linalg as sla
 
@@ -866,7 +867,7 @@ def scf_spinor(sys: System, nc_ext: np.ndarray, max_scf: int = 100, etol: float 
         if verbose:
             print(f"scf {it:3d} E={energy:.12f} F={free:.12f} mu={mu:.8f} |R|={resid:.2e}")
         result = SpinorScfResult(False, it, energy, free, mu, eigs, f, nout, mout, hist)
-        if e_prev is not None and abs(free - e_prev) < etol:
+        if e_prev is not None and abs(free - e_prev) < etol and (rtol is None or resid < rtol):
             result.converged = True
             break
         e_prev = free

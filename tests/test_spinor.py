@@ -274,12 +274,16 @@ def test_spinor_potential_setters_and_limits(oracle):
         nc1 = h.get_nc_pot()
         assert np.array_equal(nc1[:, 0, 0], v.astype(complex)) and np.array_equal(nc1[:, 1, 1], v.astype(complex))
         with pytest.raises(dg.DerekError) as e:
-            h.electronic_scf(max_scf=2)
+            h.time_apply_h()
         assert e.value.status == 8
     scalar = dg.SystemSpec(spec.cell, spec.ecut, spec.kpts, 4, 3.0, vext=spec.vext, n_fine=spec.n_fine)
     with dg.Handle(scalar) as h:
         with pytest.raises(dg.DerekError):
             h.set_nc_pot(nc)
+    with dg.Handle([spec, scalar]) as h:   # spinor and scalar systems in one batch: primitives only
+        with pytest.raises(dg.DerekError) as e:
+            h.electronic_scf(max_scf=2)
+        assert e.value.status == 8
     too_many = dg.SystemSpec(spec.cell, spec.ecut, spec.kpts, 4, 5.0, vext=spec.vext, n_fine=spec.n_fine,
                              nspinor=2)
     with pytest.raises(dg.DerekError):
@@ -314,10 +318,10 @@ def test_lsda_matches_oracle(oracle):
     s, spec = make_spinor_pair(oracle)
     with dg.Handle(spec) as h:
         e, va, vb = h.xc_lsda(ra, rb)
-    assert np.max(np.abs(e - (ex + ec)) / np.abs(ex + ec)) < 1e-13
+    assert np.max(np.abs(e - (ex + ec)) / np.abs(ex + ec)) < 5e-12
     v = np.stack([va, vb], 1)
     ref = vx + vc
-    assert np.max(np.abs(v - ref) / np.abs(ref).max(axis=1, keepdims=True)) < 1e-13
+    assert np.max(np.abs(v - ref) / np.abs(ref).max(axis=1, keepdims=True)) < 5e-12
 
 
 @pytest.mark.gpu
@@ -328,17 +332,17 @@ def test_spinor_scf_zero_field_matches_scalar(oracle):
     s, spec = scf_pair(oracle, nb_spinor=8)
     scalar = dg.SystemSpec(s.cell, s.ecut, s.kpts, 4, s.nelec, kT=s.kT, vext=s.vext, n_fine=s.n_fine,
                            inv_cell=oracle.inv_cell(s.cell))
-    with dg.Handle(scalar) as h:
-        r0 = h.electronic_scf(max_scf=60, etol=1e-11)[0]
+    with dg.Handle(scalar, density_tol=1e-10) as h:
+        r0 = h.electronic_scf(max_scf=80, etol=1e-11)[0]
         e0 = h.eigenvalues()[0]
-    with dg.Handle(spec) as h:
-        r1 = h.electronic_scf(max_scf=60, etol=1e-11)[0]
+    with dg.Handle(spec, density_tol=1e-10) as h:
+        r1 = h.electronic_scf(max_scf=80, etol=1e-11)[0]
         e1 = h.eigenvalues()[0]
         m = h.magnetisation()
         occ = h.occupations()[0]
-    assert r1.converged and abs(r1.free_energy - r0.free_energy) < 1e-9
-    assert abs(r1.efermi - r0.efermi) < 1e-8
-    assert np.max(np.abs(e1 - np.repeat(e0, 2))) < 1e-8
+    assert r1["converged"] and abs(r1["free_energy"] - r0["free_energy"]) < 1e-9
+    assert abs(r1["efermi"] - r0["efermi"]) < 1e-8
+    assert np.max(np.abs(e1 - np.repeat(e0, 2))) < 5e-9
     assert np.max(np.abs(m)) < 1e-10 and np.max(occ) <= 1.0
 
 
@@ -351,21 +355,25 @@ def test_spinor_scf_spiral_field_matches_oracle(oracle, precision, tol):
     import derek_gb300 as dg
     s, spec = scf_pair(oracle)
     nc = oracle.nc_from_fields(s.vext, spiral_field(oracle, s))
-    ref = oracle.scf_spinor(s, nc, etol=1e-12)
+    # F is variational: 1e-8 (FP64).  E, mu, the band energies, n and m are
+    # first order in the density residual, converged here to 1e-8 on both
+    # sides; the magnetisation's slowest mixing mode contracts by about 0.95
+    # per iteration, so they get looser bounds.
+    ref = oracle.scf_spinor(s, nc, etol=1e-12, rtol=1e-8)
     assert ref.converged
-    with dg.Handle(spec, precision=precision) as h:
+    with dg.Handle(spec, precision=precision, density_tol=1e-8 if precision == 0 else 1e-6) as h:
         h.set_nc_pot(nc)
-        r = h.electronic_scf(max_scf=80, etol=1e-11 if precision == 0 else 1e-8)[0]
+        r = h.electronic_scf(max_scf=100, etol=1e-11 if precision == 0 else 1e-8)[0]
         eig = h.eigenvalues()[0]
         m = h.magnetisation()
         n = h.density()
-    assert r.converged
-    assert abs(r.free_energy - ref.free_energy) < tol
-    assert abs(r.energy - ref.energy) < tol
-    assert abs(r.efermi - ref.efermi) < 10 * tol
-    assert np.max(np.abs(eig - ref.eigenvalues[0])) < 10 * tol
-    assert np.max(np.abs(m - ref.magnetisation)) < 100 * tol * np.max(np.abs(ref.magnetisation)) + 1e-9
-    assert np.max(np.abs(n - ref.density)) < 100 * tol * np.max(ref.density)
+    assert r["converged"]
+    assert abs(r["free_energy"] - ref.free_energy) < tol
+    assert abs(r["energy"] - ref.energy) < 20 * tol
+    assert abs(r["efermi"] - ref.efermi) < 50 * tol
+    assert np.max(np.abs(eig - ref.eigenvalues[0])) < 50 * tol
+    assert np.max(np.abs(m - ref.magnetisation)) < 1e3 * tol * np.max(np.abs(ref.magnetisation))
+    assert np.max(np.abs(n - ref.density)) < 1e3 * tol * np.max(ref.density)
     # the moment is not along one axis: m and B(r) turn together
     ang = (m * spiral_field(oracle, s)).sum(0) / np.linalg.norm(m, axis=0) / np.linalg.norm(spiral_field(oracle, s), axis=0)
     assert np.all(ang < -0.5)
