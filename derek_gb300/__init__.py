@@ -252,12 +252,15 @@ class Handle:
         _check(lib.derek_gpu_set_nc_pot(self._h, sys, f.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
                self._h, "set_nc_pot")
 
-    def get_nc_pot(self, sys=0):
+    def get_nc_pot(self, sys=0, external=False):
+        """nc_pot[n, i, j] of a spinor system: the H.psi potential (after an
+        SCF, its last input potential), or with external=True the SCF's
+        external potential."""
         nf, _ = self.grid(sys)
         nr = int(np.prod(nf))
         f = np.zeros((2, 2, nr), dtype=np.complex128)
-        _check(lib.derek_gpu_get_nc_pot(self._h, sys, f.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
-               self._h, "get_nc_pot")
+        fn = lib.derek_gpu_get_nc_ext if external else lib.derek_gpu_get_nc_pot
+        _check(fn(self._h, sys, f.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), self._h, "get_nc_pot")
         return np.ascontiguousarray(f.transpose(2, 1, 0))
 
     def magnetisation(self, sys=0):
@@ -385,11 +388,12 @@ class Handle:
 
     def dos(self, energies, sigma=0.01, sys=0):
         """Density of states per Ha (both spins) of the last eigenvalues:
-        sum_k w_k sum_b 2 g_sigma(E - e_kb), Gaussian of width sigma Ha."""
+        sum_k w_k sum_b g g_sigma(E - e_kb), Gaussian of width sigma Ha, with
+        g = 2 for scalar bands and 1 for spinor bands."""
         s = self.systems[sys]
         eig = self.eigenvalues(sys)
         wk = np.full(len(s.kpts), 1.0 / len(s.kpts)) if s.wk is None else np.asarray(s.wk)
-        return dos_gaussian(eig, wk, energies, sigma)
+        return dos_gaussian(eig, wk, energies, sigma, degeneracy=2.0 / s.nspinor)
 
     # ---- files and restart
     def set_start_density(self, rho, sys=0):
@@ -405,43 +409,61 @@ class Handle:
         """All wavefunctions in the reference's wavefunction%coeff layout:
         (n_std product, nk, nbands, 2) complex128, the sphere's coefficients
         at their box rows (Source/basis.f90:125-149 order), zeros elsewhere
-        and in the second spinor component (Source/wave.f90:164)."""
+        and, for a scalar system, in the second spinor component
+        (Source/wave.f90:164)."""
         s = self.systems[sys]
         _, ns = self.grid(sys)
         nbox = int(np.prod(ns))
         c = np.zeros((nbox, len(s.kpts), s.nbands, 2), dtype=np.complex128, order="F")
         for k in range(len(s.kpts)):
             rows, _, _ = self.gsphere(sys, k)
-            c[rows, k, :, 0] = self.get_wfn(sys, k).T
+            psi = self.get_wfn(sys, k)
+            if s.nspinor == 1:
+                c[rows, k, :, 0] = psi.T
+            else:
+                for sp in range(2):
+                    c[rows, k, :, sp] = psi[sp].T
         return c
 
     def write_state(self, seed, sys=0):
         """seed.den, seed.pot, seed.potex and seed.wvfn of system sys as the
         reference writes them (Source/state.f90:203-232 and the type-bound
         writers): the last density, the local potential and the external
-        potential on the spin diagonal, and the wavefunctions."""
+        potential (on the spin diagonal for a scalar system; a spinor system
+        writes its magnetisation as den%spin and its 2x2 potentials), and the
+        wavefunctions."""
         nf, ns = self.grid(sys)
         nr = int(np.prod(nf))
-        write_den(seed + ".den", ns, self.density(sys).astype(np.complex128))
-        for ext, v in ((".pot", self.get_vloc(sys)), (".potex", self.get_vext(sys))):
-            nc = np.zeros((nr, 2, 2), dtype=np.complex128, order="F")
-            nc[:, 0, 0] = v
-            nc[:, 1, 1] = v
-            write_pot(seed + ext, ns, nc)
+        spinor = self.systems[sys].nspinor == 2
+        spin = self.magnetisation(sys).T.astype(np.complex128) if spinor else None
+        write_den(seed + ".den", ns, self.density(sys).astype(np.complex128), spin)
+        if spinor:
+            write_pot(seed + ".pot", ns, self.get_nc_pot(sys))
+            write_pot(seed + ".potex", ns, self.get_nc_pot(sys, external=True))
+        else:
+            for ext, v in ((".pot", self.get_vloc(sys)), (".potex", self.get_vext(sys))):
+                nc = np.zeros((nr, 2, 2), dtype=np.complex128, order="F")
+                nc[:, 0, 0] = v
+                nc[:, 1, 1] = v
+                write_pot(seed + ext, ns, nc)
         write_wvfn(seed + ".wvfn", ns, self.wavefunction_box(sys))
 
     def restart_density(self, path, sys=0):
-        """Start the next SCF of system sys from the charge in a .den file."""
+        """Start the next SCF of system sys from the charge (and, for a
+        spinor system, the magnetisation) in a .den file."""
         nf, ns = self.grid(sys)
-        charge, _ = read_den(path, ns, int(np.prod(nf)))
+        charge, spin = read_den(path, ns, int(np.prod(nf)))
         self.set_start_density(charge.real, sys)
+        if self.systems[sys].nspinor == 2:
+            self.set_start_magnetisation(np.ascontiguousarray(spin.real.T), sys)
 
 
-def dos_gaussian(eig, wk, energies, sigma):
-    """sum_k w_k sum_b 2 exp(-(E - e_kb)^2 / (2 sigma^2)) / (sigma sqrt(2 pi))."""
+def dos_gaussian(eig, wk, energies, sigma, degeneracy=2.0):
+    """sum_k w_k sum_b d exp(-(E - e_kb)^2 / (2 sigma^2)) / (sigma sqrt(2 pi)),
+    d = degeneracy (2 for scalar bands, 1 for spinor bands)."""
     e = np.asarray(energies, dtype=np.float64)[:, None, None]
     g = np.exp(-0.5 * ((e - np.asarray(eig)[None]) / sigma) ** 2) / (sigma * np.sqrt(2 * np.pi))
-    return 2.0 * np.einsum("ekb,k->e", g, np.asarray(wk, dtype=np.float64))
+    return degeneracy * np.einsum("ekb,k->e", g, np.asarray(wk, dtype=np.float64))
 
 
 def read_info(path):

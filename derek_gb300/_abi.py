@@ -112,6 +112,7 @@ SIGNATURES = {
     "derek_gpu_density_spinor": (_i, [_vp, _i, _pd, _pd, _pd]),
     "derek_gpu_set_nc_pot": (_i, [_vp, _i, _pd]),
     "derek_gpu_get_nc_pot": (_i, [_vp, _i, _pd]),
+    "derek_gpu_get_nc_ext": (_i, [_vp, _i, _pd]),
     "derek_gpu_get_magnetisation": (_i, [_vp, _i, _pd]),
     "derek_gpu_set_start_magnetisation": (_i, [_vp, _i, _pd]),
     "derek_gpu_xc_lsda": (_i, [_vp, ctypes.c_long, _pd, _pd, _pd, _pd, _pd]),

@@ -787,16 +787,18 @@ int derek_gpu_set_nc_pot(derek_gpu_t *h, int s, const double *nc_pot) {
   return upload_nc(h, s, vnc, true);
 }
 
-int derek_gpu_get_nc_pot(derek_gpu_t *h, int s, double *nc_pot) {
+// copy system s's 2x2 potential (H.psi's, or the SCF's external one) out in
+// the reference's nc_pot(nr, 2, 2) order
+static int read_nc(derek_gpu_t *h, int s, double *nc_pot, bool ext) {
   if (!check_sys(h, s) || !nc_pot) return DEREK_ERR_BAD_ARG;
   const SysDev &S = h->sys[s];
   if (S.nspinor != 2) {
-    h->last_error = "get_nc_pot: system is not a spinor system (nspinor = 1)";
+    h->last_error = "nc_pot: system is not a spinor system (nspinor = 1)";
     return DEREK_ERR_BAD_ARG;
   }
   std::vector<double2> vnc((size_t)4 * S.nr);
-  DEREK_CUDA(h, cudaMemcpyAsync(vnc.data(), h->d_vnc64 + 4 * S.grid_off, vnc.size() * sizeof(double2),
-                                cudaMemcpyDeviceToHost, h->stream));
+  DEREK_CUDA(h, cudaMemcpyAsync(vnc.data(), (ext ? h->d_vnc_ext : h->d_vnc64) + 4 * S.grid_off,
+                                vnc.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
   DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
   for (int c = 0; c < 4; ++c)
     for (long long i = 0; i < S.nr; ++i) {
@@ -805,6 +807,9 @@ int derek_gpu_get_nc_pot(derek_gpu_t *h, int s, double *nc_pot) {
     }
   return DEREK_OK;
 }
+
+int derek_gpu_get_nc_pot(derek_gpu_t *h, int s, double *nc_pot) { return read_nc(h, s, nc_pot, false); }
+int derek_gpu_get_nc_ext(derek_gpu_t *h, int s, double *nc_pot) { return read_nc(h, s, nc_pot, true); }
 
 int derek_gpu_set_start_density(derek_gpu_t *h, int s, const double *rho) {
   if (!check_sys(h, s)) return DEREK_ERR_BAD_ARG;

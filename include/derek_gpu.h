@@ -182,7 +182,7 @@ int derek_gpu_density(derek_gpu_t *h, int sys, const double *occ, double *rho);
  *   density(_spinor): n = sum w |u|^2 + |d|^2 and the magnetisation
  *     m = sum w psi^H sigma psi = (2 Re u*d, 2 Im u*d, |u|^2 - |d|^2),
  *     mag = [3][nr] real (den%spin(:, 1:3));
- *   set_vloc(v) sets nc_pot = diag(v, v); set_nc_pot takes the reference's
+ *   set_vloc(v) sets nc_pot = diag(v, v) (H.psi only); set_nc_pot takes the reference's
  *     nc_pot(nr, 2, 2) complex128 (element (n, i, j) at n + nr (i + 2 j)),
  *     nc_pot = V I + mu_B sigma.B with mu_B = 1/2 (Source/xsf.f90:44-51);
  *     it is also the SCF's external potential (set_vext: diag(V_ext));
@@ -199,6 +199,8 @@ int derek_gpu_density(derek_gpu_t *h, int sys, const double *occ, double *rho);
  * (DEREK_ERR_UNSUPPORTED). */
 int derek_gpu_set_nc_pot(derek_gpu_t *h, int sys, const double *nc_pot);
 int derek_gpu_get_nc_pot(derek_gpu_t *h, int sys, double *nc_pot);
+/* the SCF's external nc_pot (set_nc_pot, or V_ext on the diagonal) */
+int derek_gpu_get_nc_ext(derek_gpu_t *h, int sys, double *nc_pot);
 int derek_gpu_density_spinor(derek_gpu_t *h, int sys, const double *occ /* nk*nbands */,
                              double *rho /* nr, or NULL */, double *mag /* 3*nr, or NULL */);
 int derek_gpu_get_magnetisation(derek_gpu_t *h, int sys, double *mag /* 3*nr */);

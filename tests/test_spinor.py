@@ -377,3 +377,37 @@ def test_spinor_scf_spiral_field_matches_oracle(oracle, precision, tol):
     # the moment is not along one axis: m and B(r) turn together
     ang = (m * spiral_field(oracle, s)).sum(0) / np.linalg.norm(m, axis=0) / np.linalg.norm(spiral_field(oracle, s), axis=0)
     assert np.all(ang < -0.5)
+
+
+@pytest.mark.gpu
+def test_spinor_state_files_and_restart(oracle, tmp_path):
+    """write_state of a spinor system: den%spin is the magnetisation, .pot and
+    .potex the SCF's and the external 2x2 potentials, .wvfn both spinor
+    components; a restart from the .den (charge and magnetisation) reaches
+    the same F in fewer iterations."""
+    import derek_gb300 as dg
+    s, spec = scf_pair(oracle)
+    nc = oracle.nc_from_fields(s.vext, spiral_field(oracle, s))
+    seed = str(tmp_path / "spin")
+    with dg.Handle(spec, density_tol=1e-8) as h:
+        h.set_nc_pot(nc)
+        r = h.electronic_scf(max_scf=100, etol=1e-11)[0]
+        h.write_state(seed)
+        nf, ns = h.grid()
+        nr = int(np.prod(nf))
+        charge, spin = dg.read_den(seed + ".den", ns, nr)
+        assert np.array_equal(charge.real, h.density()) and np.array_equal(spin.real, h.magnetisation().T)
+        assert np.array_equal(dg.read_pot(seed + ".potex", ns, nr), nc)
+        assert np.array_equal(dg.read_pot(seed + ".pot", ns, nr), h.get_nc_pot())
+        box = dg.read_wvfn(seed + ".wvfn", ns, int(np.prod(ns)), 1, s.nbands, 2)
+        rows, _, _ = h.gsphere()
+        psi = h.get_wfn()
+        for sp in range(2):
+            assert np.array_equal(box[rows, 0, :, sp], psi[sp].T)
+    with dg.Handle(spec, density_tol=1e-8) as h2:
+        h2.set_nc_pot(nc)
+        h2.restart_density(seed + ".den")
+        r2 = h2.electronic_scf(max_scf=100, etol=1e-11)[0]
+    assert r["converged"] and r2["converged"]
+    assert abs(r2["free_energy"] - r["free_energy"]) < 1e-9
+    assert r2["iterations"] < r["iterations"]
