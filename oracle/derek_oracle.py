@@ -874,3 +874,39 @@ def scf_spinor(sys: System, nc_ext: np.ndarray, max_scf: int = 100, etol: float 
         x = mixer.mix(np.concatenate([nin, min_.ravel()]), np.concatenate([nout, mout.ravel()]))
         nin, min_ = x[:N], x[N:].reshape(3, N)
     return result
+
+
+def external_nc_pot(p: dict, n_fine) -> np.ndarray:
+    """nc_pot (nr, 2, 2) of pot_external_pot (Source/pot.f90:128-166) for
+    the preset kinds, from a parameter dict as read_info returns it, with
+    mu_B sigma.B of a uniform ext_bfield added.  A point-by-point loop over
+    the reference's real grid (small grids only)."""
+    n1, n2, n3 = n_fine
+    nr = n1 * n2 * n3
+    nc = np.zeros((nr, 2, 2), dtype=np.complex128)
+    kind = p["external_pot"]
+    half_w = [w / 2.0 for w in p["finite_barrier_width"]]
+    g = p["periodic_pot_grid"]
+    for ix in range(n1):
+        for iy in range(n2):
+            for iz in range(n3):
+                r = (ix * n2 + iy) * n3 + iz
+                fr = ((ix + 1) / n1, (iy + 1) / n2, (iz + 1) / n3)
+                if kind == "jelly":
+                    v = 0.5 * p["n_electrons"] / nr
+                elif kind == "finite_barrier":
+                    inside = all(abs(fr[a] - 0.5) < half_w[a] for a in range(3))
+                    v = 0.5 * p["finite_barrier_height"] if inside else 0.0
+                elif kind == "periodic_pot":
+                    x = fr[0]
+                    v = 0.5 * p["periodic_pot_amp"] * math.sin(2 * math.pi * g[0] * x) * \
+                        math.sin(2 * math.pi * g[1] * x) * math.sin(2 * math.pi * g[2] * x)
+                else:
+                    v = 0.0
+                nc[r, 0, 0] = nc[r, 1, 1] = v
+    bx, by, bz = p["ext_bfield"]
+    nc[:, 0, 0] += MU_B * bz
+    nc[:, 1, 1] -= MU_B * bz
+    nc[:, 0, 1] += MU_B * (bx - 1j * by)
+    nc[:, 1, 0] += MU_B * (bx + 1j * by)
+    return nc
