@@ -367,7 +367,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
     {
       // density planes hold an FP64 accumulator plus one (y,z) plane
       const size_t es = h->prec == DEREK_PREC_FP64 ? 16 : 8;
-      const size_t need = (size_t)nfine[1] * nfine[2] * 8 + ((size_t)nfine[1] * (nfine[2] + 1) + 2 * kMaxDim) * es;
+      const size_t need = (size_t)((nfine[1] * nfine[2] + 1) & ~1) * 8 + ((size_t)nfine[1] * (nfine[2] + 1) + 2 * kMaxDim) * es;
       if (need > 227 * 1024) FAIL(DEREK_ERR_UNSUPPORTED, "grid planes exceed shared memory");
       // spinor passes hold both components' planes
       if (d.nspinor == 2 && spinor_plane_smem(nfine[1], nfine[2], es) > 227 * 1024)

@@ -320,6 +320,10 @@ __global__ void __launch_bounds__(256) k_x_fwd(Tables t, int item_begin, const c
 }
 
 // ---- density: per (k-set, x-plane), loop over bands ------------------------
+// FP64 accumulators of one plane, rounded up to an even count so that the
+// complex planes after them start on a 16-byte boundary (a double2 needs it)
+__host__ __device__ constexpr int density_acc_count(int points) { return (points + 1) & ~1; }
+
 template <typename R>
 __global__ void __launch_bounds__(512) k_density_plane(Tables t, int ks_begin, const cplx<R> *__restrict__ abuf,
                                                        const double *__restrict__ occ,
@@ -335,7 +339,8 @@ __global__ void __launch_bounds__(512) k_density_plane(Tables t, int ks_begin, c
   if (x >= n1) return;
   const int pz = n3 + 1;
   double *acc = reinterpret_cast<double *>(smem_raw);
-  cplx<R> *P = reinterpret_cast<cplx<R> *>(acc + n2 * n3);
+  // the planes start on a 16-byte boundary: an even count of accumulators
+  cplx<R> *P = reinterpret_cast<cplx<R> *>(acc + density_acc_count(n2 * n3));
   cplx<R> *twy = P + n2 * pz;
   cplx<R> *twz = twy + n2;
   for (int i = threadIdx.x; i < n2 * n3; i += blockDim.x) acc[i] = 0.0;
@@ -382,7 +387,7 @@ __global__ void __launch_bounds__(NT) k_density_fixed(Tables t, int ks_begin, co
   const int n1 = S.n[0];
   if (x >= n1) return;
   double *acc = reinterpret_cast<double *>(smem_raw);
-  cplx<R> *P = reinterpret_cast<cplx<R> *>(acc + N * N);
+  cplx<R> *P = reinterpret_cast<cplx<R> *>(acc + density_acc_count(N * N));
   cplx<R> *tw = P + N * PZ;
   for (int i = threadIdx.x; i < N * N; i += NT) acc[i] = 0.0;
   for (int i = threadIdx.x; i < N; i += NT) tw[i] = twtab<R>(t)[S.lp[1].tw_off + i];
@@ -535,7 +540,7 @@ static bool try_density_fixed(const Tables &t, int ks_begin, int nks, int max_n1
                               cudaStream_t st) {
   if (max_n2 != N || max_n3 != N || min_n2 != N || min_n3 != N) return false;
   constexpr int NT = 384;
-  const size_t sm = (size_t)N * N * sizeof(double) + ((size_t)N * (N + 1) + N) * sizeof(cplx<R>);
+  const size_t sm = (size_t)density_acc_count(N * N) * sizeof(double) + ((size_t)N * (N + 1) + N) * sizeof(cplx<R>);
   cudaFuncSetAttribute(k_density_fixed<R, N, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   derek::note_launch(), k_density_fixed<R, N, NT><<<dim3(nks, max_n1), NT, sm, st>>>(t, ks_begin, abuf, occ, partial, partial_off);
   return true;
@@ -558,7 +563,7 @@ void launch_density_plane(const Tables &t, int ks_begin, int nks, int max_n1, in
       try_density_fixed<R, 48>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st) ||
       try_density_fixed<R, 32>(t, ks_begin, nks, max_n1, max_n2, max_n3, min_n2, min_n3, abuf, occ, partial, partial_off, st))
     return;
-  const size_t sm = (size_t)max_n2 * max_n3 * sizeof(double) + smem_plane<R>(max_n2, max_n3);
+  const size_t sm = (size_t)density_acc_count(max_n2 * max_n3) * sizeof(double) + smem_plane<R>(max_n2, max_n3);
   cudaFuncSetAttribute(k_density_plane<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   derek::note_launch(), k_density_plane<R><<<dim3(nks, max_n1), 512, sm, st>>>(t, ks_begin, abuf, occ, partial, partial_off);
 }
