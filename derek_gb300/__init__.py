@@ -550,6 +550,22 @@ def write_xsf(path, cell, n_fine, data):
     _check(lib.derek_io_write_xsf(str(path).encode(), cm, _ns(n_fine), _dptr(d)), None, "write_xsf")
 
 
+def write_fden(path, n_fine, charge, spin=None):
+    """Formatted density table (.fden, Source/density.f90:165-211): charge
+    (nr,) real and spin (3, nr) real or None."""
+    c = np.ascontiguousarray(np.asarray(charge, dtype=np.float64).real)
+    sp = None if spin is None else _dptr(np.ascontiguousarray(np.asarray(spin, dtype=np.float64).real))
+    _check(lib.derek_io_write_fden(str(path).encode(), _ns(n_fine), _dptr(c), sp), None, "write_fden")
+
+
+def write_fpot(path, n_fine, nc_pot):
+    """Formatted potential table (.fpot / .fpotex, Source/pot.f90:228-287):
+    nc_pot (nr, 2, 2) complex."""
+    nr = np.asarray(nc_pot).shape[0]
+    v = _cplx(nc_pot, (nr, 2, 2))
+    _check(lib.derek_io_write_fpot(str(path).encode(), _ns(n_fine), _dptr(v)), None, "write_fpot")
+
+
 def set_subrecord_limit(nbytes=0):
     """Largest Fortran subrecord written (0: gfortran's 2^31 - 9 bytes)."""
     _check(lib.derek_io_set_subrecord_limit(int(nbytes)), None, "subrecord_limit")

@@ -141,6 +141,8 @@ SIGNATURES = {
     "derek_io_write_wvfn": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _i, _i, _i, _pd]),
     "derek_io_read_wvfn": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.c_longlong, _i, _i, _i, _pd]),
     "derek_io_write_xsf": (_i, [ctypes.c_char_p, ctypes.POINTER(_d), ctypes.POINTER(_i), _pd]),
+    "derek_io_write_fden": (_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _pd, _pd]),
+    "derek_io_write_fpot": (_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _pd]),
     "derek_io_set_subrecord_limit": (_i, [ctypes.c_longlong]),
     "derek_host_prime_fact": (_i, [_i]),
     "derek_host_grid_sizes": (_i, [ctypes.POINTER(_d), _d, _d, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),

@@ -216,6 +216,38 @@ std::string fortran_f20_10(double x) {
   return s.size() > 20 ? std::string(20, '*') : s;
 }
 
+// Fw.d as gfortran writes it: right-justified, w asterisks when the number
+// does not fit, NaN and Infinity spelled out.
+std::string fortran_f(double x, int w, int d) {
+  std::string s;
+  if (std::isnan(x)) {
+    s = "NaN";
+  } else if (std::isinf(x)) {
+    s = x > 0 ? "Infinity" : "-Infinity";
+    if ((int)s.size() > w) s = x > 0 ? "Inf" : "-Inf";
+  } else {
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%*.*f", w, d, x);
+    s = buf;
+  }
+  if ((int)s.size() > w) return std::string(w, '*');
+  return std::string(w - s.size(), ' ') + s;
+}
+
+// The formatted grid tables of density_writef (Source/density.f90:165-211)
+// and pot_writef (Source/pot.f90:228-287): the fine-grid size block, column
+// titles, a rule, then one row per point, x outermost.  Records as gfortran
+// writes them: list-directed lines start with one blank, trailing X editing
+// writes nothing.  The reference's io_out_file_header banner (a logo and
+// the write time) is replaced by this library's own comment lines.
+void table_head(FILE *f, const char *kind, const int n_fine[3]) {
+  std::fprintf(f, " # DEReK-GB300 %s FILE\n # values in atomic units\n", kind);
+  std::fprintf(f, "  FFT FINE BASIS GRID  \n");
+  const char *ax[3] = {"nx:", "ny:", "nz:"};
+  for (int i = 0; i < 3; ++i) std::fprintf(f, "  %s %6d\n", ax[i], n_fine[i]);
+  std::fprintf(f, "\n");
+}
+
 }  // namespace
 
 extern "C" {
@@ -315,6 +347,54 @@ int derek_io_read_wvfn(const char *path, const int n_std[3], long long nbox, int
       !read_true(rr))
     return DEREK_ERR_BAD_ARG;
   return DEREK_OK;
+}
+
+int derek_io_write_fden(const char *path, const int n_fine[3], const double *charge, const double *spin) {
+  if (!path || !n_fine || !charge || n_fine[0] <= 0 || n_fine[1] <= 0 || n_fine[2] <= 0) return DEREK_ERR_BAD_ARG;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return DEREK_ERR_BAD_ARG;
+  table_head(f, "DENSITY", n_fine);
+  // format(1x,3(a4,2x),5x,4(3x,A6,1x)) and format(1x,3(i4,2x),5x,4(f9.4,2x))
+  std::fprintf(f, " %4s  %4s  %4s       %9s    %6s    %6s    %6s\n", "ix", "iy", "iz", "Charge", "Sx", "Sy", "Sz");
+  std::fprintf(f, " %s\n", std::string(65, '-').c_str());
+  const long long nr = (long long)n_fine[0] * n_fine[1] * n_fine[2];
+  long long n = 0;
+  for (int ix = 1; ix <= n_fine[0]; ++ix)
+    for (int iy = 1; iy <= n_fine[1]; ++iy)
+      for (int iz = 1; iz <= n_fine[2]; ++iz, ++n) {
+        std::fprintf(f, " %4d  %4d  %4d       %s", ix, iy, iz, fortran_f(charge[n], 9, 4).c_str());
+        for (int c = 0; c < 3; ++c)
+          std::fprintf(f, "  %s", fortran_f(spin ? spin[c * nr + n] : 0.0, 9, 4).c_str());
+        std::fprintf(f, "\n");
+      }
+  return std::fclose(f) == 0 ? DEREK_OK : DEREK_ERR_BAD_ARG;
+}
+
+int derek_io_write_fpot(const char *path, const int n_fine[3], const double *nc_pot) {
+  if (!path || !n_fine || !nc_pot || n_fine[0] <= 0 || n_fine[1] <= 0 || n_fine[2] <= 0) return DEREK_ERR_BAD_ARG;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return DEREK_ERR_BAD_ARG;
+  table_head(f, "POTENTIAL", n_fine);
+  // format(1x,3(a4,2x),5x,4(9x,A5,6x,4x)) and format(1x,3(i4,2x),5x,4(f9.4,2x,f9.4,4x));
+  // columns (1,1), (1,2), (2,1), (2,2) of nc_pot(n, i, j) at n + nr (i + 2 j)
+  std::fprintf(f, " %4s  %4s  %4s       ", "ix", "iy", "iz");
+  const char *heads[4] = {"(1,1)", "(1,2)", "(2,1)", "(2,2)"};
+  for (int c = 0; c < 4; ++c) std::fprintf(f, "%s%14s", c ? "          " : "", heads[c]);
+  std::fprintf(f, "\n %s\n", std::string(115, '-').c_str());
+  const long long nr = (long long)n_fine[0] * n_fine[1] * n_fine[2];
+  const int comp[4] = {0, 2, 1, 3};   // (1,1), (1,2), (2,1), (2,2) as i + 2 j
+  long long n = 0;
+  for (int ix = 1; ix <= n_fine[0]; ++ix)
+    for (int iy = 1; iy <= n_fine[1]; ++iy)
+      for (int iz = 1; iz <= n_fine[2]; ++iz, ++n) {
+        std::fprintf(f, " %4d  %4d  %4d       ", ix, iy, iz);
+        for (int c = 0; c < 4; ++c) {
+          const double *z = nc_pot + 2 * (comp[c] * nr + n);
+          std::fprintf(f, "%s%s  %s", c ? "    " : "", fortran_f(z[0], 9, 4).c_str(), fortran_f(z[1], 9, 4).c_str());
+        }
+        std::fprintf(f, "\n");
+      }
+  return std::fclose(f) == 0 ? DEREK_OK : DEREK_ERR_BAD_ARG;
 }
 
 int derek_io_write_xsf(const char *path, const double cell[9], const int n_fine[3], const double *data) {

@@ -15,8 +15,8 @@ import os
 import numpy as np
 
 from . import (DEREK_GRID_REFERENCE, DEREK_PREC_MIXED, Handle, SystemSpec, dos_gaussian,
-               host_grid_sizes, read_den, read_info, read_pot, write_den, write_pot,  # noqa: F401
-               write_wvfn, write_xsf)
+               host_grid_sizes, read_den, read_info, read_pot, write_den, write_fden,  # noqa: F401
+               write_fpot, write_pot, write_wvfn, write_xsf)
 from .workloads import mp_grid
 
 MU_B = 0.5   # Bohr magneton, atomic units (Source/constants.f90:102)
@@ -167,9 +167,10 @@ def _xsf_components(path_stem, nc, cell, n_fine, written):
 
 
 def _write_files(h, p, seed, nc_ext, n_std, n_fine, cell, nspinor):
-    """The files of state_finalise (Source/state.f90:203-480) that have a
-    binary or XSF form here (the formatted .fpotex/.fpot/.fden tables are
-    not written)."""
+    """The files of state_finalise (Source/state.f90:203-480).  A formatted
+    potential is written as XSF components when write_xsf is set, else as a
+    .fpot / .fpotex table; .fpotex goes to its own file (the reference's
+    formatted branch writes to the binary .potex unit instead)."""
     written = []
     preset = p["external_pot"] in POT_TAG
     ext_stem = f"{seed}-{POT_TAG[p['external_pot']]}" if preset else seed
@@ -177,18 +178,32 @@ def _write_files(h, p, seed, nc_ext, n_std, n_fine, cell, nspinor):
         f = ext_stem + ".potex"
         write_pot(f, n_std, _nc_of(h, nspinor, "ext") if nspinor == 2 else nc_ext)
         written.append(f)
-    if p["write_formatted_potex"] and p["write_xsf"]:
-        _xsf_components(ext_stem, nc_ext, cell, n_fine, written)
+    if p["write_formatted_potex"]:
+        if p["write_xsf"]:
+            _xsf_components(ext_stem, nc_ext, cell, n_fine, written)
+        else:
+            f = ext_stem + ".fpotex"
+            write_fpot(f, n_fine, nc_ext)
+            written.append(f)
     if p["write_potential"]:
         f = seed + ".pot"
         write_pot(f, n_std, _nc_of(h, nspinor, "tot"))
         written.append(f)
-    if p["write_formatted_potential"] and p["write_xsf"]:
-        _xsf_components(seed, _nc_of(h, nspinor, "tot"), cell, n_fine, written)
+    if p["write_formatted_potential"]:
+        if p["write_xsf"]:
+            _xsf_components(seed, _nc_of(h, nspinor, "tot"), cell, n_fine, written)
+        else:
+            f = seed + ".fpot"
+            write_fpot(f, n_fine, _nc_of(h, nspinor, "tot"))
+            written.append(f)
     if p["write_density"]:
         f = seed + ".den"
         spin = h.magnetisation().T.astype(np.complex128) if nspinor == 2 else None
         write_den(f, n_std, h.density().astype(np.complex128), spin)
+        written.append(f)
+    if p["write_formatted_density"]:
+        f = seed + ".fden"
+        write_fden(f, n_fine, h.density(), h.magnetisation() if nspinor == 2 else None)
         written.append(f)
     if p["write_wvfn"]:
         f = seed + ".wvfn"

@@ -391,6 +391,19 @@ module derek_gpu
        integer(c_int), intent(in)         :: n_fine(3)
        real(c_double), intent(in)         :: data(*)
      end function
+     integer(c_int) function derek_io_write_fden(path, n_fine, charge, spin) bind(C, name="derek_io_write_fden")
+       import :: c_char, c_int, c_double, c_ptr
+       character(kind=c_char), intent(in) :: path(*)
+       integer(c_int), intent(in)         :: n_fine(3)
+       real(c_double), intent(in)         :: charge(*)
+       type(c_ptr), value                 :: spin
+     end function
+     integer(c_int) function derek_io_write_fpot(path, n_fine, nc_pot) bind(C, name="derek_io_write_fpot")
+       import :: c_char, c_int, c_double_complex
+       character(kind=c_char), intent(in)    :: path(*)
+       integer(c_int), intent(in)            :: n_fine(3)
+       complex(c_double_complex), intent(in) :: nc_pot(*)
+     end function
      integer(c_int) function derek_io_set_subrecord_limit(bytes) bind(C, name="derek_io_set_subrecord_limit")
        import :: c_int, c_long_long
        integer(c_long_long), value :: bytes

@@ -331,6 +331,14 @@ int derek_io_read_wvfn(const char *path, const int n_std[3], long long nbox, int
 /* XSF grid file (Source/xsf.f90:67-128): cell rows in F20.10, one value per
  * line in E20.10, in the array's flat order as the reference writes it. */
 int derek_io_write_xsf(const char *path, const double cell[9], const int n_fine[3], const double *data);
+/* Formatted grid tables (.fden, .fpot, .fpotex): density_writef
+ * (Source/density.f90:165-211) and pot_writef (Source/pot.f90:228-287) row
+ * for row, F9.4 values, x outermost; the banner of io_out_file_header is
+ * replaced by two comment lines of this library.  charge: nr reals; spin:
+ * 3 nr reals (component-major) or NULL for zeros; nc_pot: the reference's
+ * nc_pot(nr, 2, 2) complex128. */
+int derek_io_write_fden(const char *path, const int n_fine[3], const double *charge, const double *spin);
+int derek_io_write_fpot(const char *path, const int n_fine[3], const double *nc_pot);
 /* Test hook: largest subrecord in bytes (0 = gfortran's 2147483639). */
 int derek_io_set_subrecord_limit(long long bytes);
 

@@ -116,3 +116,135 @@ def xsf_text(cell, n_fine, data):
     out += [fortran_e(v) + "\n" for v in np.asarray(data, dtype=np.float64).ravel()]
     out += ["END_DATAGRID_3D\n", "END_BLOCK_DATAGRID_3D\n"]
     return "".join(out)
+
+
+def _expand_format(fmt):
+    """Edit descriptors of a Fortran format string, repeat groups expanded:
+    [('X', n) | ('A', w) | ('I', w) | ('F', w, d)]."""
+    import re
+    s = fmt.strip()
+    assert s[0] == "(" and s[-1] == ")"
+    s = s[1:-1].replace(" ", "")
+
+    def parse(t, i):
+        out = []
+        while i < len(t):
+            if t[i] == ",":
+                i += 1
+                continue
+            if t[i] == ")":
+                return out, i + 1
+            m = re.match(r"(\d*)\(", t[i:])
+            if m:
+                inner, j = parse(t, i + len(m.group(0)))
+                out += inner * int(m.group(1) or 1)
+                i = j
+                continue
+            m = re.match(r"(\d+)[xX]", t[i:])
+            if m:
+                out.append(("X", int(m.group(1))))
+                i += len(m.group(0))
+                continue
+            m = re.match(r"(\d*)([aAiI])(\d*)", t[i:])
+            if m:
+                w = int(m.group(3)) if m.group(3) else None   # A without a width: the string's length
+                out += [(m.group(2).upper(), w)] * int(m.group(1) or 1)
+                i += len(m.group(0))
+                continue
+            m = re.match(r"(\d*)[fF](\d+)\.(\d+)", t[i:])
+            if m:
+                out += [("F", int(m.group(2)), int(m.group(3)))] * int(m.group(1) or 1)
+                i += len(m.group(0))
+                continue
+            raise ValueError(t[i:])
+        return out, i
+
+    return parse(s, 0)[0]
+
+
+def fortran_write(fmt, *values):
+    """One record of write(unit, fmt) values: X positions only when data
+    follows (trailing X writes nothing), Aw right-justifies, Iw and Fw.d as
+    gfortran writes them."""
+    out, pending, k = "", 0, 0
+    for d in _expand_format(fmt):
+        if d[0] == "X":
+            pending += d[1]
+            continue
+        if k >= len(values):
+            break
+        out += " " * pending
+        pending = 0
+        v = values[k]
+        k += 1
+        if d[0] == "A":
+            w = len(v) if d[1] is None else d[1]
+            out += v[:w] if len(v) >= w else " " * (w - len(v)) + v
+        elif d[0] == "I":
+            t = str(int(v))
+            out += "*" * d[1] if len(t) > d[1] else t.rjust(d[1])
+        else:
+            out += fortran_f_edit(v, d[1], d[2])
+    return out
+
+
+def fortran_f_edit(x, w, d):
+    """Fw.d: right-justified, w asterisks on overflow, NaN / Infinity."""
+    import math
+    if math.isnan(x):
+        s = "NaN"
+    elif math.isinf(x):
+        s = "Infinity" if x > 0 else "-Infinity"
+        if len(s) > w:
+            s = "Inf" if x > 0 else "-Inf"
+    else:
+        s = f"{x:.{d}f}"
+    return "*" * w if len(s) > w else s.rjust(w)
+
+
+def _table_lines(kind, n_fine):
+    # the library's own two comment lines stand in for io_out_file_header's
+    # banner; then density_writef / pot_writef's list-directed and format-10
+    # records (Source/density.f90:187-193, Source/pot.f90:252-266)
+    lines = [f" # DEReK-GB300 {kind} FILE", " # values in atomic units", " " + " FFT FINE BASIS GRID  "]
+    for ax, n in zip(("nx:", "ny:", "nz:"), n_fine):
+        lines.append(fortran_write("(2x,a,1x,i6)", ax, n))
+    lines.append("")
+    return lines
+
+
+def fden_text(n_fine, charge, spin=None):
+    """density_writef (Source/density.f90:185-208): formats 20 and 21."""
+    nr = int(np.prod(n_fine))
+    spin = np.zeros((3, nr)) if spin is None else np.asarray(spin).reshape(3, nr)
+    lines = _table_lines("DENSITY", n_fine)
+    lines.append(fortran_write("(1x,3(a4,2x), 5x, 4(3x, A6, 1x))", "ix", "iy", "iz", "Charge", "Sx", "Sy", "Sz"))
+    lines.append(" " + "-" * 65)
+    n = 0
+    for ix in range(1, n_fine[0] + 1):
+        for iy in range(1, n_fine[1] + 1):
+            for iz in range(1, n_fine[2] + 1):
+                lines.append(fortran_write("(1x,3(i4,2x), 5x, 4(f9.4,2x))", ix, iy, iz, float(charge[n]),
+                                           float(spin[0, n]), float(spin[1, n]), float(spin[2, n])))
+                n += 1
+    return "\n".join(lines) + "\n"
+
+
+def fpot_text(n_fine, nc_pot):
+    """pot_writef (Source/pot.f90:250-284): formats 20 and 21, columns
+    (1,1), (1,2), (2,1), (2,2) as real and imaginary parts."""
+    nc = np.asarray(nc_pot, dtype=np.complex128).reshape(-1, 2, 2)
+    lines = _table_lines("POTENTIAL", n_fine)
+    lines.append(fortran_write("(1x,3(a4,2x), 5x, 4(9x, A5, 6x, 4x))", "ix", "iy", "iz",
+                               "(1,1)", "(1,2)", "(2,1)", "(2,2)"))
+    lines.append(" " + "-" * 115)
+    n = 0
+    for ix in range(1, n_fine[0] + 1):
+        for iy in range(1, n_fine[1] + 1):
+            for iz in range(1, n_fine[2] + 1):
+                v = []
+                for i, j in ((0, 0), (0, 1), (1, 0), (1, 1)):
+                    v += [float(nc[n, i, j].real), float(nc[n, i, j].imag)]
+                lines.append(fortran_write("(1x,3(i4,2x), 5x, 4(f9.4,2x,f9.4,4x))", ix, iy, iz, *v))
+                n += 1
+    return "\n".join(lines) + "\n"

@@ -118,3 +118,28 @@ def test_xsf_matches_oracle(tmp_path):
     p = tmp_path / "v.xsf"
     dg.write_xsf(p, cell, n, data)
     assert p.read_text() == F.xsf_text(cell, n, data)
+
+
+def test_formatted_tables_match_oracle(tmp_path):
+    """.fden / .fpot tables byte for byte against the oracle, which applies
+    the reference's own format strings through an edit-descriptor
+    interpreter (overflow, negative zero, NaN included)."""
+    import derek_gb300 as dg
+    rng = np.random.default_rng(5)
+    n = (3, 4, 2)
+    nr = int(np.prod(n))
+    charge = rng.uniform(0, 2, nr)
+    charge[0], charge[1], charge[2] = 12345.6789, -0.00004, float("nan")
+    spin = rng.standard_normal((3, nr))
+    p = tmp_path / "a.fden"
+    dg.write_fden(p, n, charge, spin)
+    assert p.read_text() == F.fden_text(n, charge, spin)
+    dg.write_fden(p, n, charge)
+    assert p.read_text() == F.fden_text(n, charge)
+    nc = rng.standard_normal((nr, 2, 2)) + 1j * rng.standard_normal((nr, 2, 2))
+    nc[3, 0, 1] = -1e9
+    q = tmp_path / "a.fpot"
+    dg.write_fpot(q, n, nc)
+    assert q.read_text() == F.fpot_text(n, nc)
+    rows = q.read_text().splitlines()
+    assert rows[7].startswith("   ix    iy    iz                (1,1)") and set(rows[8]) == {" ", "-"}
