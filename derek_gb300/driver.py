@@ -15,8 +15,8 @@ import os
 import numpy as np
 
 from . import (DEREK_GRID_REFERENCE, DEREK_PREC_MIXED, Handle, SystemSpec, dos_gaussian,
-               host_grid_sizes, read_den, read_info, read_pot, write_den, write_fden,  # noqa: F401
-               write_fpot, write_pot, write_wvfn, write_xsf)
+               host_grid_sizes, read_info, read_pot, write_den, write_fden, write_fpot, write_pot,
+               write_wvfn, write_xsf)
 from .workloads import mp_grid
 
 MU_B = 0.5   # Bohr magneton, atomic units (Source/constants.f90:102)
