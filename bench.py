@@ -62,6 +62,41 @@ KPTS64_ITERATIONS = 11
 FP64_TOL = 1e-6      # Ha per electron: |F_mixed - F_FP64| / N_e must stay below
 
 
+def dist_setup():
+    """Replicas under torchrun: one process per GPU (LOCAL_RANK), a process
+    group for the barrier and the two reductions below (NCCL on GPUs, gloo
+    on CPU).  None for a single process."""
+    if int(os.environ.get("WORLD_SIZE", "1")) <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    use_cuda = torch.cuda.is_available()
+    if use_cuda:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if not dist.is_initialized():
+        dist.init_process_group("nccl" if use_cuda else "gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def replica_totals(dist, units, ms):
+    """Whole-job aggregate of independent replicas: the units every rank
+    processed (sum) and the slowest rank's time (max)."""
+    if dist is None:
+        return float(units), float(ms)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()), float(t.item())
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -183,6 +218,8 @@ def run_ours(args):
     import derek_gb300 as dg
     from derek_gb300 import workloads
 
+    dist = dist_setup()   # N > 1: every rank runs an independent replica of the workload
+    rank0 = int(os.environ.get("RANK", "0")) == 0
     specs, mix = workloads.WORKLOADS[args.workload]()
     ETOL = ETOL_PER_E  # per electron: each system stops at |dF| < ETOL * its N_e
     scf_opts = dict(SOLVER, etol_per_electron=1, **mix)
@@ -193,7 +230,7 @@ def run_ours(args):
 
     # ---- accuracy gate: FP64 path once, untimed
     f64 = None
-    if not args.skip_fp64:
+    if not args.skip_fp64 and rank0:
         with dg.Handle(specs, precision=dg.DEREK_PREC_FP64, **scf_opts) as h64:
             t = time.time()
             rep64 = h64.electronic_scf(max_scf=100, etol=ETOL * 1e-2)
@@ -210,15 +247,17 @@ def run_ours(args):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = []
     with clocks:
+        barrier(dist)
         torch.cuda.synchronize()
         ev0.record(ext)
         for _ in range(args.steps):
             reps.append(h.electronic_scf(max_scf=100, etol=ETOL))
         ev1.record(ext)
         torch.cuda.synchronize()
+        barrier(dist)
     launches = dg.launch_count() - l0
-    ms = ev0.elapsed_time(ev1)
-    converged = sum(int(r["converged"]) for rep in reps for r in rep)
+    converged, ms = replica_totals(dist, sum(int(r["converged"]) for rep in reps for r in rep),
+                                   ev0.elapsed_time(ev1))
     value = converged / (ms / 1e3)
     iters = [r["iterations"] for r in reps[-1]]
 
@@ -237,6 +276,7 @@ def run_ours(args):
     ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     h2d = sum(v.numel() * 8 for v in vext_host)
     d2h = 0
+    barrier(dist)
     torch.cuda.synchronize()
     ev2.record(ext)
     for _ in range(args.steps):
@@ -248,8 +288,9 @@ def run_ours(args):
             d2h += h.eigenvalues(si).nbytes + h.occupations(si).nbytes + h.density(si).nbytes
     ev3.record(ext)
     torch.cuda.synchronize()
-    e2e_ms = ev2.elapsed_time(ev3)
-    e2e = {"value": round(len(specs) * args.steps / (e2e_ms / 1e3), 4), "unit": UNIT,
+    barrier(dist)
+    e2e_units, e2e_ms = replica_totals(dist, len(specs) * args.steps, ev2.elapsed_time(ev3))
+    e2e = {"value": round(e2e_units / (e2e_ms / 1e3), 4), "unit": UNIT,
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     # ---- roofline of the fused H.psi
@@ -297,8 +338,9 @@ def run_ours(args):
         "hpsi_band_applications_per_ground_state": bands_per_gs,
     })
     h.close()
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and rank0 and dist is None:   # rank 0 at N = 1 only
         out["cpu_baseline"] = cpu_baseline(specs, scf_opts, bands_per_gs, workers=1)
+    barrier(dist)
     return out
 
 
