@@ -9,7 +9,8 @@ header it binds, checked statically (no Fortran compiler is needed):
   `type(c_ptr), value`;
 * the bind(C) derived types list the C structs' members in order, with the
   same kinds and array lengths;
-* the status, precision and grid-policy constants carry the header's values.
+* the status, precision and grid-policy constants carry the header's values;
+* the Python package's ctypes signatures agree with the same prototypes.
 """
 import os
 import re
@@ -170,3 +171,46 @@ def test_bound_names_exported():
     _, _, ifaces = f90_module()
     for name in ifaces:
         assert hasattr(dg.lib, name), name
+
+
+def _ctypes_kind(t):
+    """(kind, is_pointer) of a ctypes argument type."""
+    import ctypes
+    if t in (ctypes.c_void_p, ctypes.c_char_p):
+        return ("c_ptr" if t is ctypes.c_void_p else "c_char"), True
+    scalars = {ctypes.c_int: "c_int", ctypes.c_long: "c_long", ctypes.c_longlong: "c_long_long",
+               ctypes.c_double: "c_double", ctypes.c_uint64: "c_int64_t"}
+    if t in scalars:
+        return scalars[t], False
+    target = getattr(t, "_type_", None)
+    if target is not None and not isinstance(target, str):
+        if target in scalars:
+            return scalars[target], True
+        return "struct", True
+    raise AssertionError(f"unmapped ctypes type {t}")
+
+
+def test_ctypes_signatures_match_header():
+    """derek_gb300's ctypes argument lists against the C prototypes: every
+    declared function has a signature with the same count of arguments, and
+    each scalar / pointer agrees with its C declaration."""
+    from derek_gb300 import _abi
+    _, _, funcs = c_header()
+    missing = sorted(set(funcs) - set(_abi.SIGNATURES))
+    assert not missing, missing
+    for name, (_, args) in _abi.SIGNATURES.items():
+        params = funcs[name]
+        assert len(args) == len(params), (name, len(args), len(params))
+        for t, p in zip(args, params):
+            kind, is_ptr = _c_param(p)
+            ckind, cptr = _ctypes_kind(t)
+            if kind == "c_ptr" and not is_ptr:          # handle or void * by value
+                assert ckind == "c_ptr", (name, p)
+                continue
+            assert cptr == is_ptr, (name, p, t)
+            if not is_ptr:
+                # LP64 (x86_64 and aarch64 Linux): ctypes.c_long is c_longlong, both 8 bytes
+                same = {kind, ckind} <= {"c_long", "c_long_long"}
+                assert ckind == kind or same, (name, p, t)
+            elif ckind not in ("c_ptr", "struct", "c_char"):
+                assert ckind == kind or (kind == "c_int32_t" and ckind == "c_int"), (name, p, t)
