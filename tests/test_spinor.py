@@ -119,6 +119,38 @@ def test_dense_spinor_hamiltonian(oracle, small):
     assert np.max(np.abs(np.linalg.eigvalsh(H0) - np.sort(np.repeat(e0, 2)))) < 1e-12
 
 
+def test_spinor_scf_oracle_zero_field_is_scalar(oracle):
+    """The oracle's non-collinear SCF without a field is the scalar SCF:
+    the same F, every level twice, m = 0."""
+    rng = np.random.default_rng(0)
+    s = oracle.make_system(6.0, 4.0, 4.0, 4, oracle.random_wells(rng, 2), kT=0.02)
+    r0 = oracle.scf(s, etol=1e-11)
+    s2 = oracle.System(s.cell, s.ecut, s.n_fine, s.n_std, s.kpts, s.wk, 8, s.nelec, s.kT, s.vext, s.wells)
+    r1 = oracle.scf_spinor(s2, oracle.nc_from_fields(s.vext, np.zeros((3, s.nr))), etol=1e-11)
+    assert r1.converged and abs(r1.free_energy - r0.free_energy) < 1e-12
+    assert np.max(np.abs(r1.eigenvalues[0] - np.repeat(r0.eigenvalues[0], 2))) < 1e-10
+    assert np.max(np.abs(r1.magnetisation)) < 1e-12
+
+
+def test_spinor_scf_oracle_spin_rotation_invariance(oracle):
+    """A uniform field turned by a global spin rotation leaves F, mu and the
+    levels unchanged and turns the moment with it (against the field)."""
+    rng = np.random.default_rng(0)
+    s = oracle.make_system(6.0, 4.0, 4.0, 8, oracle.random_wells(rng, 2), kT=0.02)
+    out = []
+    for bvec in ((0.0, 0.0, 0.4), (0.4, 0.0, 0.0), (0.0, 0.24, -0.32)):
+        b = np.repeat(np.asarray(bvec)[:, None], s.nr, axis=1)
+        r = oracle.scf_spinor(s, oracle.nc_from_fields(s.vext, b), etol=1e-12, rtol=1e-9)
+        assert r.converged
+        moment = r.magnetisation.sum(axis=1) * s.volume / s.nr
+        out.append((r.free_energy, r.efermi, r.eigenvalues[0], moment, np.asarray(bvec)))
+    f0, mu0, e0, m0, _ = out[0]
+    for f, mu, e, m, bvec in out[1:]:
+        assert abs(f - f0) < 1e-11 and abs(mu - mu0) < 1e-9 and np.max(np.abs(e - e0)) < 1e-9
+        assert abs(np.linalg.norm(m) - np.linalg.norm(m0)) < 1e-8
+        assert np.dot(m, bvec) / (np.linalg.norm(m) * np.linalg.norm(bvec)) < -1 + 1e-10
+
+
 def test_spinor_symbols_exported():
     import derek_gb300 as dg
     for name in ("derek_gpu_set_nc_pot", "derek_gpu_get_nc_pot", "derek_gpu_density_spinor"):
