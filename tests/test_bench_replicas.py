@@ -32,13 +32,19 @@ def test_replica_totals_over_two_gloo_ranks():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, port, q)) for r in range(2)]
+    # daemon ranks: a rank that hangs cannot keep the test process alive
+    procs = [ctx.Process(target=_rank, args=(r, port, q), daemon=True) for r in range(2)]
     for p in procs:
         p.start()
-    got = [q.get(timeout=120) for _ in procs]
-    for p in procs:
-        p.join(timeout=60)
-        assert p.exitcode == 0
+    try:
+        got = [q.get(timeout=120) for _ in procs]
+        for p in procs:
+            p.join(timeout=60)
+            assert p.exitcode == 0
+    finally:
+        for p in procs:
+            if p.is_alive():
+                p.terminate()
     assert sorted(got) == [(0, 3.0, 20.0, "gloo"), (1, 3.0, 20.0, "gloo")]
 
 
