@@ -497,6 +497,73 @@ def apply_h(sys: System, kb: KBasis, vloc: np.ndarray, psi: np.ndarray) -> np.nd
     return out
 
 
+def apply_h_block(sys: System, kb: KBasis, vloc: np.ndarray, psi: np.ndarray,
+                  chunk: int = 16, workers=None) -> np.ndarray:
+    """apply_h for a block psi (nb, npw), the bands of a chunk transformed
+    together by scipy.fft (norm="forward": the backward transform is the
+    reference's unnormalised dir=-1, the forward one carries the 1/N).  Same
+    arithmetic as apply_h, batched for the large grids."""
+    import scipy.fft as sfft
+    nf = tuple(int(x) for x in sys.n_fine)
+    v = vloc.reshape(nf)
+    out = np.empty_like(psi)
+    for b0 in range(0, psi.shape[0], chunk):
+        p = psi[b0:b0 + chunk]
+        box = np.zeros((p.shape[0], sys.nr), dtype=np.complex128)
+        box[:, kb.fidx] = p
+        r = sfft.ifftn(box.reshape((-1,) + nf), axes=(1, 2, 3), norm="forward", workers=workers)
+        r *= v
+        g = sfft.fftn(r, axes=(1, 2, 3), norm="forward", workers=workers)
+        out[b0:b0 + chunk] = kb.kinetic * p + g.reshape(p.shape[0], -1)[:, kb.fidx]
+    return out
+
+
+def _orthonormalise(X: np.ndarray) -> np.ndarray:
+    """Rows of X made orthonormal: S = conj(X) X^T = L L^H, X <- conj(L)^-1 X."""
+    import scipy.linalg as sla
+    S = X.conj() @ X.T
+    L = np.linalg.cholesky(0.5 * (S + S.conj().T))
+    return sla.solve_triangular(L.conj(), X, lower=True)
+
+
+def _rayleigh_ritz(sys, kb, vloc, X, workers):
+    X = _orthonormalise(X)
+    HX = apply_h_block(sys, kb, vloc, X, workers=workers)
+    Hs = X.conj() @ HX.T
+    w, U = np.linalg.eigh(0.5 * (Hs + Hs.conj().T))
+    return w, U.T @ X, U.T @ HX
+
+
+def eigensolve_filtered(sys: System, kb: KBasis, vloc: np.ndarray, X: np.ndarray, nconv: int,
+                        tol: float = 1e-9, degree: int = 12, max_pass: int = 400, workers=None):
+    """Lowest eigenpairs of H(k) by Chebyshev-filtered subspace iteration with
+    Rayleigh-Ritz (Zhou, Saad, Tiago, Chelikowsky, J. Comput. Phys. 219
+    (2006) 172), in FP64.  X (m, npw) is the start block (m > nconv buffer
+    rows speed up the lowest nconv).  Iterates until the residual norms
+    |H x - eps x| of the lowest nconv Ritz pairs are below tol; returns
+    (eps (m,), X (m, npw) orthonormal Ritz vectors, passes).  The filter damps
+    [eps_top, b] with b = ecut + max V, an upper bound of the spectrum
+    (kinetic <= ecut on the sphere, <psi|V|psi> <= max V |psi|^2)."""
+    b = sys.ecut + float(vloc.max()) + 0.1
+    w, X, HX = _rayleigh_ritz(sys, kb, vloc, X, workers)
+    for p in range(max_pass):
+        R = HX[:nconv] - w[:nconv, None] * X[:nconv]
+        if float(np.max(np.linalg.norm(R, axis=1))) < tol:
+            return w, X, p
+        a, a0 = float(w[-1]), float(w[0])
+        e, c = 0.5 * (b - a), 0.5 * (b + a)
+        sigma = e / (a0 - c)
+        s1 = sigma
+        Y = (HX - c * X) * (s1 / e)
+        Xp = X
+        for _ in range(1, degree):
+            s2 = 1.0 / (2.0 / s1 - sigma)
+            Yn = (2.0 * s2 / e) * (apply_h_block(sys, kb, vloc, Y, workers=workers) - c * Y) - (sigma * s2) * Xp
+            Xp, Y, sigma = Y, Yn, s2
+        w, X, HX = _rayleigh_ritz(sys, kb, vloc, Y, workers)
+    raise RuntimeError(f"eigensolve_filtered: no convergence to {tol} in {max_pass} passes")
+
+
 def dense_h(sys: System, kb: KBasis, vloc: np.ndarray) -> np.ndarray:
     """Dense Npw x Npw Hamiltonian: T + V(G - G') with V(G) = F[V]/N."""
     vG = fft3d(vloc.astype(np.complex128), sys.n_fine, 1).reshape(sys.n_fine) / sys.nr
@@ -519,6 +586,23 @@ def band_density(sys: System, kb: KBasis, psi: np.ndarray, weights: np.ndarray) 
         box[kb.fidx] = psi[b]
         r = fft3d(box, sys.n_fine, -1)
         rho += weights[b] * (r.real ** 2 + r.imag ** 2)
+    return rho / sys.volume
+
+
+def band_density_block(sys: System, kb: KBasis, psi: np.ndarray, weights: np.ndarray,
+                       chunk: int = 16, workers=None) -> np.ndarray:
+    """band_density with the bands of a chunk transformed together (scipy.fft)."""
+    import scipy.fft as sfft
+    nf = tuple(int(x) for x in sys.n_fine)
+    rho = np.zeros(sys.nr, dtype=np.float64)
+    occ = np.nonzero(np.asarray(weights) != 0.0)[0]
+    for c0 in range(0, len(occ), chunk):
+        sel = occ[c0:c0 + chunk]
+        box = np.zeros((len(sel), sys.nr), dtype=np.complex128)
+        box[:, kb.fidx] = psi[sel]
+        r = sfft.ifftn(box.reshape((-1,) + nf), axes=(1, 2, 3), norm="forward", workers=workers)
+        r = r.reshape(len(sel), -1)
+        rho += np.einsum("b,bn->n", np.asarray(weights)[sel], r.real ** 2 + r.imag ** 2)
     return rho / sys.volume
 
 
@@ -725,18 +809,35 @@ class ScfResult:
 
 def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3,
         history: int = 8, q0: float = 0.0, solver: str = "dense", verbose: bool = False,
-        rtol: float = None) -> ScfResult:
+        rtol: float = None, buffer: int = 8, eig_tol: float = 1e-9, workers=None) -> ScfResult:
     """Self-consistent field loop (the intended electronic_scf,
     Source/electronic.f90:86-175: iterate until |E - E_prev| < etol).
 
-    Each iteration diagonalises H[n_in] exactly ("dense", scipy eigh of the
-    Npw x Npw matrix), fills bands with Fermi-Dirac occupations, forms n_out,
-    evaluates the energies of n_out and mixes.  Start density: uniform Ne/Omega.
-    With rtol set, convergence also needs max|n_out - n_in| < rtol.
+    Each iteration diagonalises H[n_in] (solver "dense": scipy eigh of the
+    Npw x Npw matrix; "filtered": eigensolve_filtered warm-started from the
+    previous iteration's Ritz vectors with `buffer` extra rows, residual
+    norms below min(1e-6, 0.01 max|n_out - n_in|) and at least eig_tol, for
+    spheres too large for a dense matrix), fills bands with Fermi-Dirac
+    occupations, forms n_out, evaluates the energies of n_out and mixes.
+    Start density: uniform Ne/Omega.  With rtol set, convergence also needs
+    max|n_out - n_in| < rtol.
     """
     import scipy.linalg as sla
 
     kbs = [KBasis(sys, ik) for ik in range(len(sys.kpts))]
+    blocks = None
+    if solver == "filtered":
+        m = sys.nbands + buffer
+        blocks = []
+        for kb in kbs:
+            # start: the m lowest-kinetic plane waves plus a small seeded perturbation
+            X = np.zeros((m, kb.npw), dtype=np.complex128)
+            X[np.arange(m), np.argsort(kb.kinetic, kind="stable")[:m]] = 1.0
+            X += 1e-3 * start_wavefunctions(7, 0, len(blocks), m, kb.npw)
+            blocks.append(X)
+    elif solver != "dense":
+        raise ValueError(f"unknown solver {solver}")
+    resid = 1.0
     omega = sys.volume
     N = sys.nr
     dv = omega / N
@@ -753,14 +854,25 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
         eigs = np.zeros((len(kbs), sys.nbands))
         vecs = []
         for ik, kb in enumerate(kbs):
-            H = dense_h(sys, kb, vloc)
-            w, v = sla.eigh(H, subset_by_index=[0, sys.nbands - 1], driver="evr")
-            eigs[ik] = w
-            vecs.append(v.T.copy())
+            if blocks is None:
+                H = dense_h(sys, kb, vloc)
+                w, v = sla.eigh(H, subset_by_index=[0, sys.nbands - 1], driver="evr")
+                eigs[ik] = w
+                vecs.append(v.T.copy())
+            else:
+                tol = max(eig_tol, min(1e-6, 0.01 * resid))
+                w, X, _ = eigensolve_filtered(sys, kb, vloc, blocks[ik], sys.nbands, tol=tol,
+                                              workers=workers)
+                blocks[ik] = X
+                eigs[ik] = w[:sys.nbands]
+                vecs.append(X[:sys.nbands])
         f, mu, ent = fermi_occupations(eigs, sys.wk, sys.nelec, sys.kT)
         nout = np.zeros(N)
         for ik, kb in enumerate(kbs):
-            nout += sys.wk[ik] * band_density(sys, kb, vecs[ik], f[ik])
+            if blocks is None:
+                nout += sys.wk[ik] * band_density(sys, kb, vecs[ik], f[ik])
+            else:
+                nout += sys.wk[ik] * band_density_block(sys, kb, vecs[ik], f[ik], workers=workers)
         eband = float((sys.wk[:, None] * f * eigs).sum())
         _, eh = hartree(sys, nout)
         exc_eps, _ = lda_exc_vxc(nout)
