@@ -16,12 +16,15 @@ uniform in the cell), spin-unpolarised, Fermi-Dirac smearing kT = 0.01 Ha:
 
 The generator is numpy's PCG64 with the stated seed, so the inputs are the
 same on every machine.
+
+``params(name)`` returns the systems as plain dicts (cell, ecut, kpts,
+nbands, nelec, kT, wells) and imports nothing from the package, so a CPU-only
+caller can load this file on its own without the GPU library; the workload
+functions and ``WORKLOADS`` return ``SystemSpec`` objects.
 """
 from __future__ import annotations
 
 import numpy as np
-
-from . import SystemSpec, DEREK_GRID_SMOOTH23
 
 
 def mp_grid(n):
@@ -44,39 +47,39 @@ def wells(rng, count):
     return np.concatenate([c, dep[:, None], wid[:, None]], axis=1)
 
 
-def gamma_8e(seed=1):
-    rng = np.random.default_rng(seed)
-    return [SystemSpec(np.eye(3) * 10.0, 10.0, [[0, 0, 0]], 8, 8.0, kT=0.01, wells=wells(rng, 4),
-                       grid_policy=DEREK_GRID_SMOOTH23)], dict(mix_alpha=0.3, kerker_q0=0.0)
+def _sys(L, ecut, kpts, nbands, nelec, w):
+    return dict(cell=np.eye(3) * float(L), ecut=float(ecut), kpts=np.asarray(kpts, dtype=np.float64),
+                nbands=int(nbands), nelec=float(nelec), kT=0.01, wells=w)
 
 
-def kpts64(seed=2):
+def _gamma_8e(seed=1):
     rng = np.random.default_rng(seed)
-    return [SystemSpec(np.eye(3) * 16.0, 20.0, mp_grid((4, 4, 4)), 80, 64.0, kT=0.01,
-                       wells=wells(rng, 16), grid_policy=DEREK_GRID_SMOOTH23)], \
+    return [_sys(10.0, 10.0, [[0, 0, 0]], 8, 8.0, wells(rng, 4))], dict(mix_alpha=0.3, kerker_q0=0.0)
+
+
+def _kpts64(seed=2):
+    rng = np.random.default_rng(seed)
+    return [_sys(16.0, 20.0, mp_grid((4, 4, 4)), 80, 64.0, wells(rng, 16))], \
         dict(mix_alpha=0.3, kerker_q0=0.8)
 
 
-def kpts64_k4(seed=2):
+def _kpts64_k4(seed=2):
     """kpts64 cut to its first 4 k-points: the same kernels on a case small
-    enough for a full profiler capture."""
-    specs, mix = kpts64(seed)
-    specs[0].kpts = specs[0].kpts[:4].copy()
-    if specs[0].wk is not None:
-        specs[0].wk = specs[0].wk[:4].copy()
-    return specs, mix
+    enough for a full profiler capture and for the oracle's fixture."""
+    systems, mix = _kpts64(seed)
+    systems[0]["kpts"] = systems[0]["kpts"][:4].copy()
+    return systems, mix
 
 
-def adjoint9k(seed=3):
+def _adjoint9k(seed=3):
     rng = np.random.default_rng(seed)
     k = np.concatenate([[[0.0, 0.0, 0.0]], mp_grid((2, 2, 2))])
-    return [SystemSpec(np.eye(3) * 12.0, 15.0, k, 20, 16.0, kT=0.01, wells=wells(rng, 8),
-                       grid_policy=DEREK_GRID_SMOOTH23)], dict(mix_alpha=0.3, kerker_q0=0.0)
+    return [_sys(12.0, 15.0, k, 20, 16.0, wells(rng, 8))], dict(mix_alpha=0.3, kerker_q0=0.0)
 
 
-def uneven(count=256, seed=5):
+def _uneven(count=256, seed=5):
     rng = np.random.default_rng(seed)
-    specs = []
+    systems = []
     for _ in range(count):
         L = rng.uniform(8.0, 20.0)
         ne = int(rng.integers(2, 65))
@@ -86,11 +89,40 @@ def uneven(count=256, seed=5):
             kg = tuple(int(x) for x in rng.integers(1, 4, 3))
             if np.prod(kg) <= 27:
                 break
-        specs.append(SystemSpec(np.eye(3) * L, 15.0, mp_grid(kg), nb, float(ne), kT=0.01,
-                                wells=wells(rng, int(rng.integers(2, 13))),
-                                grid_policy=DEREK_GRID_SMOOTH23))
-    return specs, dict(mix_alpha=0.3, kerker_q0=0.8)
+        systems.append(_sys(L, 15.0, mp_grid(kg), nb, float(ne),
+                            wells(rng, int(rng.integers(2, 13)))))
+    return systems, dict(mix_alpha=0.3, kerker_q0=0.8)
 
+
+_PARAMS = {"gamma_8e": _gamma_8e, "kpts64": _kpts64, "kpts64_k4": _kpts64_k4, "adjoint9k": _adjoint9k,
+           "uneven256": _uneven}
+
+
+def params(name, **kw):
+    """(systems as plain dicts, mixing options) of a named workload."""
+    return _PARAMS[name](**kw)
+
+
+def to_specs(systems):
+    from . import SystemSpec, DEREK_GRID_SMOOTH23
+    return [SystemSpec(s["cell"], s["ecut"], s["kpts"], s["nbands"], s["nelec"], kT=s["kT"],
+                       wells=s["wells"], grid_policy=DEREK_GRID_SMOOTH23) for s in systems]
+
+
+def _specs(name):
+    def make(**kw):
+        systems, mix = params(name, **kw)
+        return to_specs(systems), mix
+    make.__name__ = name
+    make.__doc__ = _PARAMS[name].__doc__
+    return make
+
+
+gamma_8e = _specs("gamma_8e")
+kpts64 = _specs("kpts64")
+kpts64_k4 = _specs("kpts64_k4")
+adjoint9k = _specs("adjoint9k")
+uneven = _specs("uneven256")
 
 WORKLOADS = {"gamma_8e": gamma_8e, "kpts64": kpts64, "kpts64_k4": kpts64_k4, "adjoint9k": adjoint9k,
              "uneven256": uneven}

@@ -4,12 +4,13 @@ TEST INFRASTRUCTURE ONLY: used by bench.py's CPU-baseline leg and its
 reference arm (the DEReK reference has no working SCF and cannot be built on
 the benchmark host, so the FP64 numpy restatement stands in for it).
 
-The sample is one Chebyshev-filtered subspace iteration of one k-point with
-the same structure the GPU solver runs per SCF iteration: `degree` filtered
+The sample unit is one Chebyshev-filtered subspace iteration of one k-point
+with the structure the GPU solver runs per SCF iteration: `degree` filtered
 H.psi block applications, one more H.psi for Rayleigh-Ritz, the overlap
-Cholesky orthonormalisation and the dense subspace eigensolve.  The
-ground-state rate is this per-(k-point, iteration) cost scaled by the number
-of k-points and by the H.psi work of a full SCF, both stated by the caller.
+Cholesky orthonormalisation and the dense subspace eigensolve.  A pool of
+worker processes (started with spawn, one per host core, each single
+threaded) runs one such unit per worker per step; the caller scales the
+measured step time to a ground state by the H.psi work of a full SCF.
 """
 from __future__ import annotations
 
@@ -19,6 +20,8 @@ import time
 import numpy as np
 
 from . import derek_oracle as O
+
+_CACHE = {}
 
 
 def _system_from(spec):
@@ -32,28 +35,25 @@ def _system_from(spec):
                     spec["kT"], vext, wells)
 
 
-def subspace_iteration(sys: O.System, ik: int, degree: int, seed: int = 0) -> float:
-    """Seconds for one filtered subspace iteration of k-point ik (FP64 numpy)."""
+def subspace_iteration(sys: O.System, kb: O.KBasis, X: np.ndarray, degree: int) -> float:
+    """Seconds for one filtered subspace iteration of one k-point (FP64)."""
     import scipy.linalg as sla
-    kb = O.KBasis(sys, ik)
-    rng = np.random.default_rng(seed)
-    X = rng.standard_normal((sys.nbands, kb.npw)) + 0j
     v = sys.vext
     t0 = time.perf_counter()
     # filter with fixed bounds (the arithmetic, not the convergence, is timed)
     a0, a, b = -1.0, 0.5, sys.ecut + float(v.max())
     e, c = 0.5 * (b - a), 0.5 * (b + a)
     s1 = e / (a0 - c)
-    Y = (O.apply_h(sys, kb, v, X) - c * X) * (s1 / e)
+    Y = (O.apply_h_block(sys, kb, v, X, workers=1) - c * X) * (s1 / e)
     s = s1
     for _ in range(1, degree):
         sn = 1.0 / (2.0 / s1 - s)
-        Yn = 2.0 * sn / e * (O.apply_h(sys, kb, v, Y) - c * Y) - s * sn * X
+        Yn = 2.0 * sn / e * (O.apply_h_block(sys, kb, v, Y, workers=1) - c * Y) - s * sn * X
         X, Y, s = Y, Yn, sn
     S = Y.conj() @ Y.T
     L = np.linalg.cholesky(S)
-    Xo = sla.solve_triangular(L, Y, lower=True)
-    HX = O.apply_h(sys, kb, v, Xo)
+    Xo = sla.solve_triangular(L.conj(), Y, lower=True)
+    HX = O.apply_h_block(sys, kb, v, Xo, workers=1)
     Hs = Xo.conj() @ HX.T
     w, U = np.linalg.eigh(0.5 * (Hs + Hs.conj().T))
     _ = U.T @ Xo
@@ -61,28 +61,60 @@ def subspace_iteration(sys: O.System, ik: int, degree: int, seed: int = 0) -> fl
 
 
 def _worker(args):
-    spec, ik, degree = args
-    sys = _system_from(spec)
-    return subspace_iteration(sys, ik, degree)
+    spec_key, spec, ik, degree = args
+    key = (spec_key, ik)
+    if key not in _CACHE:
+        if spec_key not in _CACHE:
+            _CACHE[spec_key] = _system_from(spec)
+        sys = _CACHE[spec_key]
+        kb = O.KBasis(sys, ik)
+        X = np.random.default_rng(ik).standard_normal((sys.nbands, kb.npw)) + 0j
+        _CACHE[key] = (kb, X)
+    sys = _CACHE[spec_key]
+    kb, X = _CACHE[key]
+    return subspace_iteration(sys, kb, X, degree)
 
 
-def sample(spec: dict, degree: int, kpoints: int = 1, workers: int = 1) -> dict:
-    """Time `kpoints` k-point iterations, spread over `workers` processes
-    (started with spawn).  Returns seconds per (k-point, iteration) averaged
-    over the sample, wall seconds, and the worker count actually used."""
-    jobs = [(spec, ik % len(spec["kpts"]), degree) for ik in range(kpoints)]
-    t0 = time.perf_counter()
-    if workers <= 1:
-        times = [_worker(j) for j in jobs]
-    else:
+def _single_thread_env():
+    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[v] = "1"
+
+
+class Sampler:
+    """A spawn pool of `workers` single-threaded processes; `step()` runs one
+    subspace iteration of a different k-point in every worker and returns
+    the wall seconds of the step (the slowest worker's unit plus the
+    dispatch).  The first step of each worker also builds its system and
+    sphere, so callers warm up before timing."""
+
+    def __init__(self, spec: dict, degree: int, workers: int):
         import multiprocessing as mp
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(workers) as pool:
-            times = pool.map(_worker, jobs)
-    wall = time.perf_counter() - t0
-    return {"per_k_iteration_s": float(np.mean(times)), "wall_s": wall,
-            "workers": workers, "kpoints": kpoints,
-            "throughput_k_iterations_per_s": kpoints / wall}
+        self.spec, self.degree, self.workers = spec, degree, max(1, int(workers))
+        self.nk = len(np.asarray(spec["kpts"]).reshape(-1, 3))
+        saved = {v: os.environ.get(v) for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+        _single_thread_env()
+        self.pool = mp.get_context("spawn").Pool(self.workers)
+        for v, x in saved.items():
+            if x is None:
+                os.environ.pop(v, None)
+            else:
+                os.environ[v] = x
+
+    def step(self) -> float:
+        jobs = [(id(self), self.spec, i % self.nk, self.degree) for i in range(self.workers)]
+        t0 = time.perf_counter()
+        self.pool.map(_worker, jobs, chunksize=1)
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def cores() -> int:
