@@ -13,6 +13,13 @@
 // Two calls whose kernels overlap on the GPU (different streams, or threads
 // without ordering) race on it and give wrong results.  Every partial is
 // written before it is read in the same call, so nothing needs clearing.
+//
+// The array's device address is looked up once per device, on the first call
+// with that device current, and cached.  The cache does not survive a
+// cudaDeviceReset: a caller that resets a device must not call this entry
+// point again in the same process.  Each launch's own status is taken from
+// cudaLaunchKernel, so an error left pending by unrelated earlier work is
+// neither reported as this call's nor cleared.
 #include <mutex>
 
 #include "common.cuh"
@@ -112,13 +119,22 @@ extern "C" int derek_gpu_overlap_noalloc(const void *x, const void *y, int nb, i
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const int nt = (nb + ST - 1) / ST;
   dim3 grid(nt * nt, nsplit);
-  if (precision == DEREK_PREC_FP64)
-    derek::note_launch(), k_overlap_partial_flat<double><<<grid, 256, 0, cs>>>(
-        static_cast<const double2 *>(x), static_cast<const double2 *>(y), nb, npw, ld, scratch);
-  else
-    derek::note_launch(), k_overlap_partial_flat<float><<<grid, 256, 0, cs>>>(
-        static_cast<const float2 *>(x), static_cast<const float2 *>(y), nb, npw, ld, scratch);
-  derek::note_launch(), k_overlap_reduce_flat<<<(nb * nb + 255) / 256, 256, 0, cs>>>(
-      scratch, nb, nsplit, static_cast<double2 *>(s));
-  return cudaGetLastError() == cudaSuccess ? DEREK_OK : DEREK_ERR_CUDA;
+  long long ldl = ld;
+  void *pargs[] = {const_cast<void **>(&x), const_cast<void **>(&y), &nb, &npw, &ldl, &scratch};
+  const void *partial = precision == DEREK_PREC_FP64
+                            ? reinterpret_cast<const void *>(&k_overlap_partial_flat<double>)
+                            : reinterpret_cast<const void *>(&k_overlap_partial_flat<float>);
+  derek::note_launch();
+  cudaError_t e = cudaLaunchKernel(partial, grid, dim3(256), pargs, 0, cs);
+  if (e == cudaSuccess) {
+    void *rargs[] = {&scratch, &nb, const_cast<int *>(&nsplit), &s};
+    derek::note_launch();
+    e = cudaLaunchKernel(reinterpret_cast<const void *>(&k_overlap_reduce_flat),
+                         dim3((nb * nb + 255) / 256), dim3(256), rargs, 0, cs);
+  }
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // this call's own launch error, recorded just now
+    return DEREK_ERR_CUDA;
+  }
+  return DEREK_OK;
 }

@@ -231,8 +231,11 @@ int derek_gpu_overlap(derek_gpu_t *h, int sys, int k, double *s);
  *   stream   cudaStream_t to launch on (NULL = default stream)
  * Limits: nb <= 128 and npw <= 16 * 4096 = 65536, else DEREK_ERR_UNSUPPORTED.
  * The first call on a device looks up the array's device address, so make
- * that first call before any stream capture.  Calls share the array: calls
- * that overlap on the GPU race and give wrong results. */
+ * that first call before any stream capture.  That address is cached per
+ * device and does not survive cudaDeviceReset: do not call this again after
+ * resetting a device.  Calls share the array: calls that overlap on the GPU
+ * race and give wrong results.  DEREK_ERR_CUDA means one of this call's own
+ * launches failed; an error pending from other work is left as it was. */
 int derek_gpu_overlap_noalloc(const void *x, const void *y, int nb, int npw, long ld,
                               int precision, void *s, void *stream);
 

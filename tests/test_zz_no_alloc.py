@@ -49,6 +49,54 @@ def test_overlap_noalloc_matches_handle_overlap(oracle):
             assert err < 1e-11, (call, err)
 
 
+def _noalloc(dg, x, y, nb, npw, ld, precision, s, stream):
+    return dg.lib.derek_gpu_overlap_noalloc(
+        ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), nb, npw, ctypes.c_long(ld),
+        precision, ctypes.c_void_p(s.data_ptr()), ctypes.c_void_p(stream))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_overlap_noalloc_several_splits_padded_rows(oracle, precision):
+    """npw = 11,000+ plane waves (three 4096-coefficient K-splits, so the
+    reduction sums several partials), distinct X and Y (S is not Hermitian,
+    so a swapped or wrongly conjugated operand fails), rows padded to
+    ld = npw + 40 with garbage in the padding, two calls in a row.  Checked
+    against FP64 numpy conj(X) @ Y.T: 1e-11 relative in FP64; complex64
+    inputs against the same product of the rounded inputs, 1e-5 relative."""
+    import torch
+    import derek_gb300 as dg
+
+    cell = np.eye(3) * 16.0
+    n_std, nf = oracle.grid_sizes(cell, 15.0, 2.0, "smooth23")
+    kb = oracle.KBasis(oracle.make_system(16.0, 15.0, 2.0, 4, np.zeros((0, 5)), kpts=[[0.1, 0.2, 0.3]]), 0)
+    npw, nb = kb.npw, 40
+    assert npw > 2 * 4096
+    ld = npw + 40
+    rng = np.random.default_rng(21)
+    fp64 = precision == "fp64"
+    prec = dg.DEREK_PREC_FP64 if fp64 else dg.DEREK_PREC_MIXED
+    cdt = np.complex128 if fp64 else np.complex64
+    stream = torch.cuda.current_stream().cuda_stream
+    for call in range(2):
+        X = (rng.standard_normal((nb, ld)) + 1j * rng.standard_normal((nb, ld))).astype(cdt)
+        Y = (rng.standard_normal((nb, ld)) + 1j * rng.standard_normal((nb, ld))).astype(cdt)
+        X[:, npw:] = 1e30 if fp64 else 1e20
+        Y[:, npw:] = np.nan
+        real = np.float64 if fp64 else np.float32
+        x = torch.from_numpy(X.view(real).copy()).cuda()
+        y = torch.from_numpy(Y.view(real).copy()).cuda()
+        s = torch.full((nb, nb, 2), np.nan, dtype=torch.float64, device="cuda")
+        assert _noalloc(dg, x, y, nb, npw, ld, prec, s, stream) == 0
+        torch.cuda.synchronize()
+        got = s.cpu().numpy().view(np.complex128).reshape(nb, nb)
+        Xd = X[:, :npw].astype(np.complex128)
+        Yd = Y[:, :npw].astype(np.complex128)
+        ref = Xd.conj() @ Yd.T
+        err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        assert err < (1e-11 if fp64 else 1e-5), (call, err)
+        assert not np.allclose(ref, ref.conj().T)   # distinct operands: S is not Hermitian
+
+
 def test_overlap_noalloc_rejects_sizes_beyond_its_scratch():
     import derek_gb300 as dg
     # nb above 128 or npw above 16 x 4096 exceeds the file-scope scratch array;
