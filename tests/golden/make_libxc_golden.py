@@ -5,16 +5,18 @@ hot path (LDA_X, id 1, and LDA_C_PW, id 12; energy "zk" and potential
   ExLib/libxc/libxc-6.2.2/testsuite/regression/{lda_x,lda_c}/*.{unpol,pol}.{0,1}.bz2
 Unpolarised densities are rhoa + rhob, as testsuite/xc-regression.c:258-262;
 polarised ones keep (rhoa, rhob) and vrho has one column per spin.
-Writes tests/golden/libxc_lda_unpol.json and libxc_lda_pol.json.  Run in a
-tree where the reference is mounted:
-  python tests/golden/make_libxc_golden.py [reference_root]
+Writes tests/golden/libxc_lda_unpol.json and libxc_lda_pol.json:
+  python tests/golden/make_libxc_golden.py <DEReK tree>   (or DEREK_REFERENCE=...)
 """
 import bz2
 import json
 import os
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DEREK_REFERENCE")
+if not ref or not os.path.isdir(os.path.join(ref, "ExLib/libxc/libxc-6.2.2/testsuite")):
+    sys.exit("usage: make_libxc_golden.py <DEReK tree> (or set DEREK_REFERENCE); "
+             f"no libxc 6.2.2 testsuite under {ref!r}")
 base = os.path.join(ref, "ExLib/libxc/libxc-6.2.2/testsuite")
 for spin in ("unpol", "pol"):
     out = {"source": "libxc 6.2.2 testsuite (vendored in the DEReK tree, ExLib/libxc)", "systems": {}}
