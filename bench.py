@@ -123,6 +123,8 @@ def parse():
     p.add_argument("--workload", default="kpts64")
     p.add_argument("--skip-fp64", action="store_true", help="skip the FP64 accuracy gate (debug)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--tune-cache", default=os.path.join(ROOT, "derek_gb300", "tune_cache.json"),
+                   help="autotuner cache (JSON); '' tunes without a cache")
     return p.parse_args()
 
 
@@ -283,6 +285,7 @@ def run_ours(args):
     fp64 = None
     if not args.skip_fp64 and rank0:
         with dg.Handle(specs, precision=dg.DEREK_PREC_FP64, **scf_opts) as h64:
+            plan64 = h64.autotune(args.tune_cache or None)
             ext64 = torch.cuda.ExternalStream(h64.stream())
             timed_scf(h64, ext64, ETOL)                   # warm-up (graph capture)
             rep64, ms64 = timed_scf(h64, ext64, ETOL)
@@ -290,9 +293,11 @@ def run_ours(args):
         fp64 = {"ground_states_per_s": round(n64 / (ms64 / 1e3), 5), "ms_per_step": round(ms64, 1),
                 "iterations": [r["iterations"] for r in rep64],
                 "free_energy": [r["free_energy"] for r in rep64],
-                "stopping_rule": "the same |F - F_prev| < 1e-7 Ha x N_e and solver as the mixed path"}
+                "stopping_rule": "the same |F - F_prev| < 1e-7 Ha x N_e and solver as the mixed path",
+                "plan": plan64}
 
     h = dg.Handle(specs, precision=dg.DEREK_PREC_MIXED, **scf_opts)
+    plan = h.autotune(args.tune_cache or None)
     ext = torch.cuda.ExternalStream(h.stream())
     for _ in range(args.warmup):
         h.electronic_scf(max_scf=100, etol=ETOL)
@@ -384,6 +389,7 @@ def run_ours(args):
         "fp64_path": fp64,
         "e2e": e2e,
         "roofline": roofline,
+        "plan": plan,
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "hpsi_band_applications_per_ground_state": bands_per_gs,

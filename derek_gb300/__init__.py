@@ -370,6 +370,25 @@ class Handle:
                "time_apply_h")
         return tot.value, list(stage)
 
+    def autotune(self, cache_path=None, retune=False):
+        """Time the candidate FFT radix plans, line splits, row layouts and
+        subspace-kernel shapes on this handle and keep the fastest
+        (derek_gpu_autotune); with cache_path the choices are read from and
+        written to that JSON file.  Call it right after creating the handle:
+        it overwrites the wavefunction buffers.  Returns the plan."""
+        path = None if cache_path is None else os.fspath(cache_path).encode()
+        _check(lib.derek_gpu_autotune(self._h, path, _abi.DEREK_TUNE_RETUNE if retune else 0), self._h,
+               "autotune")
+        return self.plan()
+
+    def plan(self):
+        """The handle's current plan (radices, line kernels, row layouts,
+        overlap/rotation paths, Jacobi shape) as a dict."""
+        import json
+        buf = ctypes.create_string_buffer(1 << 16)
+        _check(lib.derek_gpu_plan(self._h, buf, len(buf)), self._h, "plan")
+        return json.loads(buf.value.decode())
+
     def density(self, sys=0):
         nf, _ = self.grid(sys)
         rho = np.zeros(int(np.prod(nf)))

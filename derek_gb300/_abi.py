@@ -18,6 +18,7 @@ DEREK_ERR_NAN = 6
 DEREK_ERR_TIMEOUT = 7
 DEREK_ERR_UNSUPPORTED = 8
 
+DEREK_TUNE_RETUNE = 1
 DEREK_PREC_FP64 = 0
 DEREK_PREC_MIXED = 1
 DEREK_GRID_REFERENCE = 0
@@ -131,6 +132,11 @@ SIGNATURES = {
     "derek_gpu_stream": (_vp, [_vp]),
     "derek_gpu_launch_count": (ctypes.c_ulonglong, []),
     "derek_gpu_time_apply_h": (_i, [_vp, _i, _pd, _pd]),
+    "derek_gpu_autotune": (_i, [_vp, ctypes.c_char_p, _i]),
+    "derek_gpu_set_wait_limit": (_i, [ctypes.c_long]),
+    "derek_gpu_plan": (_i, [_vp, ctypes.c_char_p, _i]),
+    "derek_host_tune_cache_normalise": (_i, [ctypes.c_char_p, ctypes.c_char_p, _i]),
+    "derek_host_radix_candidates": (_i, [_i, ctypes.c_char_p, _i]),
     "derek_gpu_set_start_density": (_i, [_vp, _i, _pd]),
     "derek_info_read": (_i, [ctypes.c_char_p, ctypes.POINTER(InfoParams), ctypes.c_char_p, _i]),
     "derek_gpu_nscf_run": (_i, [_vp, _i, _d, _i, ctypes.POINTER(_i)]),

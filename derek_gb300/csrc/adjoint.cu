@@ -309,7 +309,7 @@ extern "C" int derek_gpu_grad_density_loss(derek_gpu_t *h, int s, const double *
   };
   // P_c y = y - Psi (Psi^H y)
   auto project = [&](double2 *y) {
-    launch_overlap<double>(t, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit, psi, y, h->d_opart,
+    launch_overlap<double>(t, 0, h->nks, h->max_nb, h->max_npw, h->tune.ksplit, psi, y, h->d_opart,
                            h->d_opart_off, h->d_S, h->d_mat_off, 0, st);
     const size_t sm = (size_t)h->max_nb * h->max_nb * sizeof(double2);
     cudaFuncSetAttribute(k_gemm_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -341,7 +341,7 @@ extern "C" int derek_gpu_grad_density_loss(derek_gpu_t *h, int s, const double *
       if (e2) return e2;
     }
     // V_mn and the pair orbitals xi = psi W
-    launch_overlap<double>(t, 0, h->nks, h->max_nb, h->max_npw, kOverlapSplit, psi, W.phi, h->d_opart,
+    launch_overlap<double>(t, 0, h->nks, h->max_nb, h->max_npw, h->tune.ksplit, psi, W.phi, h->d_opart,
                            h->d_opart_off, h->d_Hs, h->d_mat_off, 1, st);
     derek::note_launch(), k_pair_weights<<<h->nks, 256, 0, st>>>(t, h->d_eig, h->d_occ, h->d_Hs, h->d_mat_off, h->d_C);
     CKA(cudaMemcpyAsync(W.xi, psi, np * sizeof(double2), cudaMemcpyDeviceToDevice, st));

@@ -45,15 +45,18 @@ __global__ void k_to_float(long long n, const double *__restrict__ a, float *__r
     b[i] = (float)a[i];
 }
 
+// The three stage kernels of H.psi over one grid-size class.  max_m is the
+// row bound the kernels are dispatched with (a class's tuned disp_m); with
+// tune.generic_lines the shared-memory kernels with runtime line splits run.
 template <typename R>
 static void apply_h_class(derek_gpu *h, const Tables &t, int item_begin, int nitems, int nchunk,
                           const int n[3], int max_m, const void *in, const void *prev, void *out,
                           const Axpby *coef, const R *vloc) {
-  launch_x_inv<R>(t, item_begin, nitems, nchunk, n[0], n[0], max_m, (const cplx<R> *)in,
+  launch_x_inv<R>(t, item_begin, nitems, nchunk, n[0], disp_min(h, n[0]), max_m, (const cplx<R> *)in,
                   (cplx<R> *)h->d_abuf, nullptr, h->stream);
-  launch_plane<R>(t, item_begin, nitems, n[0], n[1], n[2], n[1], n[2], max_m, (cplx<R> *)h->d_abuf,
-                  vloc, h->stream);
-  launch_x_fwd<R>(t, item_begin, nitems, nchunk, n[0], n[0], max_m, (const cplx<R> *)h->d_abuf,
+  launch_plane<R>(t, item_begin, nitems, n[0], n[1], n[2], disp_min(h, n[1]), disp_min(h, n[2]), max_m,
+                  (cplx<R> *)h->d_abuf, vloc, h->stream);
+  launch_x_fwd<R>(t, item_begin, nitems, nchunk, n[0], disp_min(h, n[0]), max_m, (const cplx<R> *)h->d_abuf,
                   (const cplx<R> *)in, (const cplx<R> *)prev, (cplx<R> *)out, coef, h->stream);
 }
 
@@ -66,7 +69,7 @@ static void apply_h_t(derek_gpu *h, const Tables &base, int item_begin, int nite
     for (const auto &c : h->classes) {
       Tables t = base;
       t.item_list = c.d_list;
-      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, c.max_m, in, prev, out, coef, vloc);
+      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, c.disp_m, in, prev, out, coef, vloc);
     }
     return;
   }
@@ -111,11 +114,11 @@ template <typename R> static void density_t(derek_gpu *h, const void *psi) {
   for (const auto &c : h->classes) {
     Tables t = h->tab;
     t.item_list = c.d_list;
-    launch_x_inv<R>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const cplx<R> *)psi,
+    launch_x_inv<R>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const cplx<R> *)psi,
                     (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
   }
-  launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2], h->min_n[1],
-                          h->min_n[2], h->max_m_all, (const cplx<R> *)h->d_abuf, h->d_occw,
+  launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2], disp_min(h, h->min_n[1]),
+                          disp_min(h, h->min_n[2]), h->max_m_all, (const cplx<R> *)h->d_abuf, h->d_occw,
                           h->d_partial, h->d_partial_off, h->stream);
 }
 
@@ -667,6 +670,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       c.count = (int)g.second.size();
       c.nchunk = chunks[g.first];
       c.max_m = mys[g.first];
+      c.disp_m = c.max_m;
       c.d_list = nullptr;
       if (groups.size() > 1) CK(upload(&c.d_list, g.second));
       h->classes.push_back(c);
@@ -1059,10 +1063,10 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       Tables t = h->tab;
       t.item_list = c.d_list;
       if (h->prec == DEREK_PREC_FP64)
-        launch_x_inv<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const double2 *)in,
+        launch_x_inv<double>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const double2 *)in,
                              (double2 *)h->d_abuf, nullptr, h->stream);
       else
-        launch_x_inv<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const float2 *)in,
+        launch_x_inv<float>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const float2 *)in,
                             (float2 *)h->d_abuf, nullptr, h->stream);
     }
     cudaEventRecord(ev[1], h->stream);
@@ -1070,22 +1074,24 @@ int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *m
       Tables t = h->tab;
       t.item_list = c.d_list;
       if (h->prec == DEREK_PREC_FP64)
-        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_m,
-                             (double2 *)h->d_abuf, h->d_vloc, h->stream);
+        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], disp_min(h, c.n[1]), disp_min(h, c.n[2]),
+                             c.disp_m, (double2 *)h->d_abuf, h->d_vloc, h->stream);
       else
-        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], c.n[1], c.n[2], c.max_m,
-                            (float2 *)h->d_abuf, h->d_vloc32, h->stream);
+        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], disp_min(h, c.n[1]), disp_min(h, c.n[2]),
+                            c.disp_m, (float2 *)h->d_abuf, h->d_vloc32, h->stream);
     }
     cudaEventRecord(ev[2], h->stream);
     for (const auto &c : h->classes) {
       Tables t = h->tab;
       t.item_list = c.d_list;
       if (h->prec == DEREK_PREC_FP64)
-        launch_x_fwd<double>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const double2 *)h->d_abuf,
-                             (const double2 *)in, nullptr, (double2 *)h->d_HX, nullptr, h->stream);
+        launch_x_fwd<double>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m,
+                             (const double2 *)h->d_abuf, (const double2 *)in, nullptr, (double2 *)h->d_HX,
+                             nullptr, h->stream);
       else
-        launch_x_fwd<float>(t, 0, c.count, c.nchunk, c.n[0], c.n[0], c.max_m, (const float2 *)h->d_abuf,
-                            (const float2 *)in, nullptr, (float2 *)h->d_HX, nullptr, h->stream);
+        launch_x_fwd<float>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m,
+                            (const float2 *)h->d_abuf, (const float2 *)in, nullptr, (float2 *)h->d_HX,
+                            nullptr, h->stream);
     }
     cudaEventRecord(ev[3], h->stream);
     DEREK_CUDA(h, cudaEventSynchronize(ev[3]));

@@ -121,11 +121,23 @@ struct derek_gpu {
     int count;
     int nchunk;
     int max_m;     // largest |centred Miller index| (x, y or z) of a sphere entry in the class
+    int disp_m;    // row bound the stage kernels are dispatched with (>= max_m; autotuned)
     int *d_list;   // nullptr when the class is the contiguous range of all items
   };
   std::vector<ItemClass> classes;
   std::vector<int> ks_max_m;    // per k-set: largest |centred Miller index| of its sphere
   int max_m_all = 0;
+
+  // ---- plan choices the autotuner (autotune.cu) may change; the defaults
+  // are the untuned plan
+  struct Tune {
+    int ksplit = 2048;       // overlap split-K: complex coefficients per CTA (>= kOverlapSplit)
+    int overlap_tc = -1;     // -1: opts.use_tensor_cores decides; 0/1: CUDA cores / tensor cores
+    int rotate_tc = -1;
+    int jacobi_single = 0;   // 1: one CTA per k-set even where the two-CTA cluster fits
+    int generic_lines = 0;   // 1: shared-memory line kernels with the runtime splits sys[].lp
+    std::string source = "default";   // "default", "tuned" or "cache"
+  } tune;
 
   cudaStream_t stream = nullptr;
   std::string last_error;
@@ -166,6 +178,17 @@ int apply_spinor_items(derek_gpu *h, int item_begin, int nitems, const void *in,
 // True (with last_error set) when h holds a spinor system: the SCF, NSCF,
 // gradients and timing entry points run scalar systems only.
 bool reject_spinor(derek_gpu *h, const char *what);
+// Subspace pieces of the SCF (scf.cu) the autotuner times: tensor-core
+// availability and choice, overlaps S = A^H B and rotations X <- X C over all
+// k-sets, with the handle's tuned split and paths.
+bool tc_capable(const derek_gpu *h);
+bool use_tc_overlap(const derek_gpu *h);
+bool use_tc_rotate(const derek_gpu *h);
+int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int hermitize);
+int rotate_all(derek_gpu *h, void *X, const double2 *C);
+// minimum first argument of the stage launchers: the class's own size, or -1
+// to force the shared-memory kernels with runtime line splits
+inline int disp_min(const derek_gpu *h, int n) { return h->tune.generic_lines ? -1 : n; }
 int density_spinor_items(derek_gpu *h, const void *psi, double *rho);
 
 }  // namespace derek

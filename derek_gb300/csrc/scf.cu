@@ -26,29 +26,43 @@ template <typename T> cudaError_t dalloc(T **p, size_t n) {
   return cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T));
 }
 
+}  // namespace
+
 // -- pieces of an iteration -------------------------------------------------
-bool use_tc(const derek_gpu *h) {
+namespace derek {
+
+// the tensor-core kernels serve complex64 scalar bands, nb <= 128, when the
+// options allow them (use_tensor_cores 1: overlaps, 2: overlaps and rotations)
+bool tc_capable(const derek_gpu *h) {
   return h->prec == DEREK_PREC_MIXED && h->opts.use_tensor_cores && h->max_nb <= kMaxBands && !h->any_spinor;
+}
+bool use_tc_overlap(const derek_gpu *h) {
+  return tc_capable(h) && (h->tune.overlap_tc >= 0 ? h->tune.overlap_tc == 1 : true);
+}
+bool use_tc_rotate(const derek_gpu *h) {
+  return tc_capable(h) && h->opts.use_tensor_cores >= 2 &&
+         (h->tune.rotate_tc >= 0 ? h->tune.rotate_tc == 1 : true);
 }
 
 int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int hermitize) {
-  if (use_tc(h))
-    launch_overlap_tc(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, kOverlapSplit, (const float2 *)A,
+  const int ks = h->tune.ksplit;
+  if (use_tc_overlap(h))
+    launch_overlap_tc(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, ks, (const float2 *)A,
                       (const float2 *)B, h->d_opart, h->d_opart_off, out, h->d_mat_off, hermitize,
                       h->d_status, h->stream);
   else if (h->prec == DEREK_PREC_FP64)
-    launch_overlap<double>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, kOverlapSplit,
+    launch_overlap<double>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, ks,
                            (const double2 *)A, (const double2 *)B, h->d_opart, h->d_opart_off, out,
                            h->d_mat_off, hermitize, h->stream);
   else
-    launch_overlap<float>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, kOverlapSplit,
+    launch_overlap<float>(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, ks,
                           (const float2 *)A, (const float2 *)B, h->d_opart, h->d_opart_off, out,
                           h->d_mat_off, hermitize, h->stream);
   return DEREK_OK;
 }
 
 int rotate_all(derek_gpu *h, void *X, const double2 *C) {
-  if (use_tc(h) && h->opts.use_tensor_cores >= 2)
+  if (use_tc_rotate(h))
     launch_rotate_tc(h->tab_band, 0, h->nks, h->max_nb_band, h->max_npw_band, (float2 *)X, C, h->d_mat_off,
                      h->d_rot_img, h->d_status, h->stream);
   else if (h->prec == DEREK_PREC_FP64)
@@ -59,6 +73,10 @@ int rotate_all(derek_gpu *h, void *X, const double2 *C) {
                          h->stream);
   return DEREK_OK;
 }
+
+}  // namespace derek
+
+namespace {
 
 // orthonormalise buf(cur) and do Rayleigh-Ritz; leaves Ritz values in d_eig
 int cholqr_rr(derek_gpu *h) {
@@ -76,7 +94,7 @@ int cholqr_rr(derek_gpu *h) {
   // saving about one of the four sweeps near convergence.
   const double jtol = h->prec == DEREK_PREC_FP64 ? 1e-14 : 1e-10;
   launch_jacobi(h->tab_band, 0, h->nks, h->max_nb_band, h->d_Hs, h->d_C, h->d_mat_off, h->d_eig,
-                h->d_scratch, 30, jtol, 0, h->d_sweeps, h->stream);
+                h->d_scratch, 30, jtol, 0, h->d_sweeps, h->stream, h->tune.jacobi_single);
   rotate_all(h, X, h->d_C);
   return DEREK_OK;
 }
@@ -146,6 +164,31 @@ int finish_iteration(derek_gpu *h) {
   return DEREK_OK;
 }
 
+// Start vectors in buf(cur): hashed entries (init_vectors 0) or plane waves
+// (1) in X; with 2 the wavefunctions stored by set_wfn (a restart from a
+// saved state) keep their bands and the buffer bands get plane-wave start
+// vectors.
+int start_vectors(derek_gpu *h) {
+  const int init = h->opts.init_vectors;
+  const int *pw = init >= 1 ? h->d_pw_entry : nullptr;
+  const int dst = init == 2 ? (h->cur + 1) % 3 : 0;
+  if (h->prec == DEREK_PREC_FP64)
+    launch_init_psi<double>(h->tab, h->nitems, h->buf(dst), h->opts.seed, pw, h->stream);
+  else
+    launch_init_psi<float>(h->tab, h->nitems, h->buf(dst), h->opts.seed, pw, h->stream);
+  if (init == 2) {
+    // the reported bands of a k-set are its first nbr rows of npw_pad coefficients
+    const size_t es = h->elem_size();
+    for (const auto &K : h->ks)
+      DEREK_CUDA(h, cudaMemcpyAsync((char *)h->buf(dst) + (size_t)K.psi_off * es,
+                                    (const char *)h->cur_psi() + (size_t)K.psi_off * es,
+                                    (size_t)K.nbr * K.npw_pad * es, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  h->cur = dst;
+  DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
 int scf_start(derek_gpu *h, double etol) {
   // reset state: all systems active, uniform start density, start vectors
   for (auto &s : h->sys) s.active = 1;
@@ -183,14 +226,9 @@ int scf_start(derek_gpu *h, double etol) {
   launch_potential(h->tab, h->nsys, (int)h->max_nr, h->max_nmax, h->d_rho_in, h->d_cgrid,
                    h->d_vext, h->d_vhxc, h->d_vloc, h->prec == DEREK_PREC_FP64 ? nullptr : h->d_vloc32,
                    h->d_epart, h->d_state, 1, sg, h->stream);
-  h->cur = 0;
-  const int *pw = h->opts.init_vectors == 1 ? h->d_pw_entry : nullptr;
-  if (h->prec == DEREK_PREC_FP64)
-    launch_init_psi<double>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
-  else
-    launch_init_psi<float>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
-  DEREK_CUDA(h, cudaGetLastError());
-  int s = cholqr_rr(h);
+  int s = start_vectors(h);
+  if (s) return s;
+  s = cholqr_rr(h);
   if (s) return s;
   for (int p = 0; p < h->opts.first_passes; ++p) {
     s = subspace_step(h, h->opts.first_degree);
@@ -326,7 +364,7 @@ extern "C" int derek_scf_alloc(derek_gpu_t *h) {
   A(dalloc(&h->d_hist_off, hist_off.size()));
   A(dalloc(&h->d_status, h->nks));
   A(dalloc(&h->d_sweeps, h->nks));
-  if (use_tc(h)) A(dalloc(&h->d_rot_img, h->nks * rotate_tc_image_bytes(h->max_nb)));
+  if (tc_capable(h)) A(dalloc(&h->d_rot_img, h->nks * rotate_tc_image_bytes(h->max_nb)));
   A(dalloc(&h->d_coef_all, (size_t)h->max_degree * h->nks));
   A(dalloc(&h->d_nin_hist, hoff));
   A(dalloc(&h->d_res_hist, hoff));
@@ -387,16 +425,28 @@ int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
     DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
     return DEREK_OK;
   }
-  if (use_tc(h))
-    launch_overlap_tc(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const float2 *)h->cur_psi(),
+  if (use_tc_overlap(h)) {
+    DEREK_CUDA(h, cudaMemsetAsync(h->d_status + ki, 0, sizeof(int), h->stream));
+    launch_overlap_tc(h->tab, ki, 1, K.nb, K.npw, h->tune.ksplit, (const float2 *)h->cur_psi(),
                       (const float2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S, h->d_mat_off,
                       0, h->d_status, h->stream);
+    int ks_status = 0;
+    DEREK_CUDA(h, cudaMemcpyAsync(&ks_status, h->d_status + ki, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (ks_status) {
+      // a bounded wait ran out: the CTA gave up, drained its own MMAs and
+      // freed its tensor memory; the handle stays usable
+      DEREK_CUDA(h, cudaMemsetAsync(h->d_status + ki, 0, sizeof(int), h->stream));
+      h->last_error = "overlap: tensor-core pipeline wait timed out";
+      return ks_status;
+    }
+  }
   else if (h->prec == DEREK_PREC_FP64)
-    launch_overlap<double>(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const double2 *)h->cur_psi(),
+    launch_overlap<double>(h->tab, ki, 1, K.nb, K.npw, h->tune.ksplit, (const double2 *)h->cur_psi(),
                            (const double2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S,
                            h->d_mat_off, 0, h->stream);
   else
-    launch_overlap<float>(h->tab, ki, 1, K.nb, K.npw, kOverlapSplit, (const float2 *)h->cur_psi(),
+    launch_overlap<float>(h->tab, ki, 1, K.nb, K.npw, h->tune.ksplit, (const float2 *)h->cur_psi(),
                           (const float2 *)h->cur_psi(), h->d_opart, h->d_opart_off, h->d_S,
                           h->d_mat_off, 0, h->stream);
   DEREK_CUDA(h, cudaGetLastError());
@@ -407,6 +457,8 @@ int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
   DEREK_CUDA(h, cudaStreamSynchronize(h->stream));
   return DEREK_OK;
 }
+
+int derek_gpu_set_wait_limit(long iterations) { return set_stage_wait_limit(iterations); }
 
 int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep) {
   if (!h) return DEREK_ERR_BAD_ARG;
@@ -456,13 +508,9 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, 
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_state, st.data(), st.size() * sizeof(SysState),
                                 cudaMemcpyHostToDevice, h->stream));
   DEREK_CUDA(h, cudaMemsetAsync(h->d_status, 0, h->nks * sizeof(int), h->stream));
-  h->cur = 0;
-  const int *pw = h->opts.init_vectors == 1 ? h->d_pw_entry : nullptr;
-  if (h->prec == DEREK_PREC_FP64)
-    launch_init_psi<double>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
-  else
-    launch_init_psi<float>(h->tab, h->nitems, h->d_X, h->opts.seed, pw, h->stream);
-  int s = cholqr_rr(h);
+  int s = start_vectors(h);
+  if (s) return s;
+  s = cholqr_rr(h);
   if (s) return s;
   // the lowest nconv reported bands of every k-set (0: all reported): a band
   // close below the subspace's top converges slowly under the filter, whose

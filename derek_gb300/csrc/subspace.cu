@@ -249,7 +249,8 @@ __global__ void __launch_bounds__(256) k_cholesky_inv(const Tables t, int ks_beg
     const double2 v = Li[j * n + i];
     Cb[e] = make_double2(v.x, -v.y);
   }
-  if (threadIdx.x == 0 && s_fail) status[ksi] = DEREK_ERR_CHOLESKY;
+  // keep an earlier failure of this k-set (a timed-out overlap wait)
+  if (threadIdx.x == 0 && s_fail && status[ksi] == 0) status[ksi] = DEREK_ERR_CHOLESKY;
 }
 
 // ---------------------------------------------------------------------------
@@ -737,7 +738,8 @@ constexpr size_t kJacobiSmem = 227 * 1024 - 4096;   // static reduction arrays t
 
 void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
                    double2 *C, const long long *mat_off, double *eig, double2 *scratch,
-                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st) {
+                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st,
+                   int single) {
   if (nks <= 0) return;
   const size_t nn = (size_t)max_nb * max_nb;
   const size_t tab = jacobi_tables(max_nb);
@@ -749,7 +751,7 @@ void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const dou
   const size_t hv = (size_t)(max_nb + 1) / 2;
   const size_t vhalf = ((size_t)max_nb * hv * (fp32_vectors ? sizeof(float2) : sizeof(double2)) + 15) / 16 * 16;
   const size_t sm_pair = nn * sizeof(double2) + vhalf + tab;
-  if (sm_pair <= kJacobiSmem) {
+  if (!single && sm_pair <= kJacobiSmem) {
     if (fp32_vectors) {
       cudaFuncSetAttribute(k_jacobi_pair<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pair);
       derek::note_launch(), k_jacobi_pair<float><<<2 * nks, 256, sm_pair, st>>>(t, ks_begin, Hs, C, mat_off, eig,

@@ -29,6 +29,8 @@ size_t rotate_tc_image_bytes(int max_nb);
 void launch_rotate_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, float2 *X,
                       const double2 *C, const long long *mat_off, unsigned char *img, int *status,
                       cudaStream_t st);
+// try limit of the tensor-core kernels' pipeline-stage waits (< 0: default)
+int set_stage_wait_limit(long iterations);
 template <typename R>
 void launch_rotate(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, cplx<R> *X,
                    const double2 *C, const long long *mat_off, cudaStream_t st);
@@ -36,10 +38,12 @@ bool cholesky_fits_smem(int max_nb);
 void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *S,
                          double2 *C, const long long *mat_off, double2 *scratch, int *status,
                          cudaStream_t st);
-// fp32_vectors: accumulate the eigenvectors in FP32 (A stays FP64)
+// fp32_vectors: accumulate the eigenvectors in FP32 (A stays FP64); single:
+// one CTA per k-set even where the two-CTA cluster kernel fits
 void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
                    double2 *C, const long long *mat_off, double *eig, double2 *scratch,
-                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st);
+                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st,
+                   int single = 0);
 
 // Per-system SCF scalars kept on the device.
 constexpr int kMaxHist = 16;

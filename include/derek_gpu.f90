@@ -26,6 +26,7 @@ module derek_gpu
        DEREK_ERR_NAN = 6, DEREK_ERR_TIMEOUT = 7, DEREK_ERR_UNSUPPORTED = 8
   integer(c_int), parameter :: DEREK_PREC_FP64 = 0, DEREK_PREC_MIXED = 1
   integer(c_int), parameter :: DEREK_GRID_REFERENCE = 0, DEREK_GRID_SMOOTH23 = 1
+  integer(c_int), parameter :: DEREK_TUNE_RETUNE = 1
 
   type, bind(C) :: derek_sys_desc
      real(c_double)    :: cell(9), inv_cell(9), ecut, g_fine_scale
@@ -284,6 +285,35 @@ module derek_gpu
        type(c_ptr), value          :: h
        integer(c_int), value       :: nrep
        real(c_double), intent(out) :: ms_apply, ms_stage(3)
+     end function
+     integer(c_int) function derek_gpu_autotune(h, cache_path, flags) bind(C, name="derek_gpu_autotune")
+       import :: c_ptr, c_int, c_char
+       type(c_ptr), value                 :: h
+       character(kind=c_char), intent(in) :: cache_path(*)
+       integer(c_int), value              :: flags
+     end function
+     integer(c_int) function derek_gpu_plan(h, buf, len) bind(C, name="derek_gpu_plan")
+       import :: c_ptr, c_int, c_char
+       type(c_ptr), value                  :: h
+       character(kind=c_char), intent(out) :: buf(*)
+       integer(c_int), value               :: len
+     end function
+     integer(c_int) function derek_host_tune_cache_normalise(text, out, len) &
+         bind(C, name="derek_host_tune_cache_normalise")
+       import :: c_int, c_char
+       character(kind=c_char), intent(in)  :: text(*)
+       character(kind=c_char), intent(out) :: out(*)
+       integer(c_int), value               :: len
+     end function
+     integer(c_int) function derek_host_radix_candidates(n, out, len) bind(C, name="derek_host_radix_candidates")
+       import :: c_int, c_char
+       integer(c_int), value               :: n
+       character(kind=c_char), intent(out) :: out(*)
+       integer(c_int), value               :: len
+     end function
+     integer(c_int) function derek_gpu_set_wait_limit(iterations) bind(C, name="derek_gpu_set_wait_limit")
+       import :: c_int, c_long
+       integer(c_long), value :: iterations
      end function
      integer(c_int) function derek_gpu_grad_wells(h, sys, grad) bind(C, name="derek_gpu_grad_wells")
        import :: c_ptr, c_int, c_double

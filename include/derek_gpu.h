@@ -58,6 +58,9 @@ extern "C" {
 #define DEREK_GRID_REFERENCE 0  /* basis_prime_fact: {2,3,5,7,11,13}-smooth */
 #define DEREK_GRID_SMOOTH23  1  /* {2,3}-smooth */
 
+/* derek_gpu_autotune flags */
+#define DEREK_TUNE_RETUNE    1  /* time every candidate even where the cache holds a choice */
+
 typedef struct derek_gpu derek_gpu_t;
 
 /* One independent system.  Mirrors the fields of current_structure /
@@ -103,7 +106,11 @@ typedef struct {
                               stops at |dF| < etol * nelec) */
   int    init_vectors;     /* start vectors: 0 = hashed random entries; 1 = band
                               b on the b-th lowest-kinetic-energy plane wave of
-                              its k-point, plus a 1e-3 hashed perturbation */
+                              its k-point, plus a 1e-3 hashed perturbation;
+                              2 = the wavefunctions stored with set_wfn (a
+                              restart from a saved state, as state_write keeps
+                              model%wfn, Source/state.f90:612), buffer bands
+                              as in 1 */
 } derek_scf_opts;
 
 /* Per-system SCF report (Source/electronic.f90:143-146 table row). */
@@ -243,6 +250,14 @@ int derek_gpu_overlap_noalloc(const void *x, const void *y, int nb, int npw, lon
  * system; scf_run iterates until |dF| < etol or max_scf iterations
  * (Source/electronic.f90:86-175).  rep has one entry per system. */
 int derek_gpu_scf_iterate(derek_gpu_t *h, derek_scf_report *rep);
+
+/* Try limit of the tensor-core kernels' pipeline-stage waits, for every
+ * handle in the process (< 0: the default).  With a small limit a stage wait
+ * runs out: the kernel records DEREK_ERR_TIMEOUT, drains its own MMAs (that
+ * wait keeps the default limit), frees its tensor memory and returns; the
+ * overlap or SCF call reports DEREK_ERR_TIMEOUT and the handle stays usable.
+ * For tests of that path; no counterpart in the reference. */
+int derek_gpu_set_wait_limit(long iterations);
 int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol,
                       derek_scf_report *rep);
 
@@ -261,6 +276,31 @@ int derek_gpu_get_vext(derek_gpu_t *h, int sys, double *vext);
 void *derek_gpu_stream(derek_gpu_t *h);
 unsigned long long derek_gpu_launch_count(void);
 int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage);
+
+/* Autotuner.  Times the candidate plans of this handle's shapes on its own
+ * tables and buffers and keeps the fastest: the radix sequence of every
+ * grid-FFT length, register/fixed-length line kernels against shared-memory
+ * four-step kernels with a runtime split per length, the row layout of each
+ * grid class's H.psi kernels, tensor or CUDA cores and the split-K length of
+ * the overlaps, the rotation path and the Jacobi launch shape.  Every
+ * candidate computes the same result.  With cache_path (NULL: no cache) the
+ * choices are read from and written to a JSON file keyed by device and
+ * shape; DEREK_TUNE_RETUNE re-times what the cache holds.  It overwrites the
+ * wavefunction buffers and subspace matrices, so call it right after
+ * derek_gpu_create (an SCF starts from its own start vectors).  Scalar
+ * systems only.  Replaces the reference's FFTW_ESTIMATE planning
+ * (Source/fft.f90:204-212), which chooses without timing.
+ * derek_gpu_plan writes the handle's current plan as a JSON object (len
+ * bytes available; DEREK_ERR_BAD_ARG when it does not fit). */
+int derek_gpu_autotune(derek_gpu_t *h, const char *cache_path, int flags);
+int derek_gpu_plan(derek_gpu_t *h, char *buf, int len);
+/* Host-only pieces of the autotuner: derek_host_tune_cache_normalise parses
+ * a cache file's text and writes it back in the library's own layout
+ * (DEREK_ERR_BAD_ARG when it does not parse or fit); derek_host_radix_candidates
+ * lists the radix sequences tried for length n as "8x3x3;3x3x8;..." (empty
+ * when n has a prime factor above 13). */
+int derek_host_tune_cache_normalise(const char *text, char *out, int len);
+int derek_host_radix_candidates(int n, char *out, int len);
 
 /* Hellmann-Feynman gradient of the converged free energy with respect to the
  * Gaussian-well parameters of sys: dF/dp = int n(r) dV_ext/dp dr.  Writes
