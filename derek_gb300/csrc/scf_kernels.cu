@@ -304,7 +304,9 @@ __global__ void k_energy_final(const Tables t, int nsys, const double *__restric
   int status = 0;
   for (int k = 0; k < S.nk; ++k)
     if (ks_status[S.ks0 + k]) status = ks_status[S.ks0 + k];
-  if (!(F == F)) status = DEREK_ERR_NAN;
+  // a k-set's own failure (a wait that timed out, a singular overlap) is
+  // the cause of a NaN that follows it, so it is the status reported
+  if (!(F == F) && !status) status = DEREK_ERR_NAN;
   X.status = status;
   if (X.iter > 1 && X.delta < X.etol && (X.rtol <= 0.0 || X.resid < X.rtol)) X.converged = 1;
   if (X.converged || status) sys_rw[s].active = 0;

@@ -58,11 +58,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (long i = 0; i < kWaitLimit; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long limit = kWaitLimit) {
+  for (long i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+
+// Try limit of the pipeline-stage waits (a stage is reused once the MMAs
+// that read it completed).  The host lowers it to test the timeout path
+// (derek_gpu_set_wait_limit); the final wait for a CTA's own MMAs, before it
+// frees its tensor memory, always keeps the full kWaitLimit.
+__device__ long g_stage_wait_limit = kWaitLimit;
 
 // shared-memory matrix descriptor, no swizzle, K-major canonical layout:
 // core matrices of 8 rows x 16 bytes; lbo = stride between core matrices
@@ -229,7 +235,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int s = kb & 1;
     if (kb >= 2) {
       // the MMAs of block kb-2 must have finished reading this stage
-      if (tid == 0) s_ok = mbar_wait(&bars[s], ((kb - 2) >> 1) & 1) ? 1 : 0;
+      if (tid == 0) s_ok = mbar_wait(&bars[s], ((kb - 2) >> 1) & 1, g_stage_wait_limit) ? 1 : 0;
       __syncthreads();
       if (!s_ok) {
         ok = false;
@@ -460,7 +466,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   for (int kb = 0; kb < nkb; ++kb) {
     const int s = kb & 1;
     if (kb >= 2) {
-      if (tid == 0) s_ok = mbar_wait(&bars[s], ((kb - 2) >> 1) & 1) ? 1 : 0;
+      if (tid == 0) s_ok = mbar_wait(&bars[s], ((kb - 2) >> 1) & 1, g_stage_wait_limit) ? 1 : 0;
       __syncthreads();
       if (!s_ok) {
         ok = false;
@@ -548,6 +554,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
   }
+}
+
+int set_stage_wait_limit(long iterations) {
+  const long v = iterations < 0 ? kWaitLimit : iterations;
+  return cudaMemcpyToSymbol(g_stage_wait_limit, &v, sizeof(v)) == cudaSuccess ? DEREK_OK : DEREK_ERR_CUDA;
 }
 
 void launch_rotate_tc(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, float2 *X,

@@ -809,17 +809,20 @@ class ScfResult:
 
 def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3,
         history: int = 8, q0: float = 0.0, solver: str = "dense", verbose: bool = False,
-        rtol: float = None, buffer: int = 8, eig_tol: float = 1e-9, workers=None) -> ScfResult:
+        rtol: float = None, buffer: int = 8, eig_tol: float = 1e-9, workers=None,
+        nin0: np.ndarray = None, blocks0: list = None, keep: dict = None) -> ScfResult:
     """Self-consistent field loop (the intended electronic_scf,
     Source/electronic.f90:86-175: iterate until |E - E_prev| < etol).
 
     Each iteration diagonalises H[n_in] (solver "dense": scipy eigh of the
     Npw x Npw matrix; "filtered": eigensolve_filtered warm-started from the
     previous iteration's Ritz vectors with `buffer` extra rows, residual
-    norms below min(1e-6, 0.01 max|n_out - n_in|) and at least eig_tol, for
+    norms below min(1e-4, 0.01 max|n_out - n_in|) and at least eig_tol, for
     spheres too large for a dense matrix), fills bands with Fermi-Dirac
     occupations, forms n_out, evaluates the energies of n_out and mixes.
-    Start density: uniform Ne/Omega.  With rtol set, convergence also needs
+    Start density: uniform Ne/Omega, or nin0; the filtered solver starts
+    from blocks0 when given (a previous run's keep["blocks"]: a warm start
+    for nearby parameters).  With rtol set, convergence also needs
     max|n_out - n_in| < rtol.
     """
     import scipy.linalg as sla
@@ -835,13 +838,15 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
             X[np.arange(m), np.argsort(kb.kinetic, kind="stable")[:m]] = 1.0
             X += 1e-3 * start_wavefunctions(7, 0, len(blocks), m, kb.npw)
             blocks.append(X)
+        if blocks0 is not None:
+            blocks = [np.array(b) for b in blocks0]
     elif solver != "dense":
         raise ValueError(f"unknown solver {solver}")
     resid = 1.0
     omega = sys.volume
     N = sys.nr
     dv = omega / N
-    nin = np.full(N, sys.nelec / omega)
+    nin = np.full(N, sys.nelec / omega) if nin0 is None else np.array(nin0, dtype=np.float64)
     mixer = PulayMixer(sys, alpha=alpha, history=history, q0=q0)
     e_prev = None
     hist = []
@@ -860,7 +865,7 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
                 eigs[ik] = w
                 vecs.append(v.T.copy())
             else:
-                tol = max(eig_tol, min(1e-6, 0.01 * resid))
+                tol = max(eig_tol, min(1e-4, 0.01 * resid))
                 w, X, _ = eigensolve_filtered(sys, kb, vloc, blocks[ik], sys.nbands, tol=tol,
                                               workers=workers)
                 blocks[ik] = X
@@ -885,6 +890,8 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
         if verbose:
             print(f"scf {it:3d} E={energy:.12f} F={free:.12f} mu={mu:.8f} |R|={resid:.2e}")
         result = ScfResult(False, it, energy, free, mu, eigs, f, nout, hist)
+        if keep is not None and blocks is not None:
+            keep["blocks"] = blocks
         if e_prev is not None and abs(free - e_prev) < etol and (rtol is None or resid < rtol):
             result.converged = True
             break
