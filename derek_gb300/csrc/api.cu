@@ -66,10 +66,16 @@ template <typename R>
 static void apply_h_t(derek_gpu *h, const Tables &base, int item_begin, int nitems, const void *in,
                       const void *prev, void *out, const Axpby *coef, const R *vloc) {
   if (item_begin == 0 && nitems == h->nitems) {
+    // a class in chunks of tune.hpsi_chunk items: a chunk's x-plane buffer
+    // (~0.47 MB per item at 72^3) can stay in L2 between the three stages
     for (const auto &c : h->classes) {
-      Tables t = base;
-      t.item_list = c.d_list;
-      apply_h_class<R>(h, t, 0, c.count, c.nchunk, c.n, c.disp_m, in, prev, out, coef, vloc);
+      const int step = h->tune.hpsi_chunk > 0 ? h->tune.hpsi_chunk : c.count;
+      for (int i0 = 0; i0 < c.count; i0 += step) {
+        Tables t = base;
+        t.item_list = c.d_list ? c.d_list + i0 : nullptr;
+        apply_h_class<R>(h, t, c.d_list ? 0 : i0, std::min(step, c.count - i0), c.nchunk, c.n, c.disp_m, in,
+                         prev, out, coef, vloc);
+      }
     }
     return;
   }
@@ -97,6 +103,12 @@ int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, cons
   else
     apply_h_t<float>(h, h->tab, item_begin, nitems, in, prev, out, coef, h->d_vloc32);
   DEREK_CUDA(h, cudaGetLastError());
+  return DEREK_OK;
+}
+
+int activate_all(derek_gpu *h) {
+  DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
+                                cudaMemcpyHostToDevice, h->stream));
   return DEREK_OK;
 }
 
@@ -685,6 +697,7 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
 }
 
 static int check_sys(derek_gpu_t *h, int s) { return h && s >= 0 && s < h->nsys; }
+
 static int ks_index(derek_gpu_t *h, int s, int k) {
   if (!check_sys(h, s) || k < 0 || k >= h->sys[s].nk) return -1;
   return h->sys[s].ks0 + k;
@@ -899,7 +912,10 @@ int derek_gpu_apply_h(derek_gpu_t *h, int s, int k, double *hpsi) {
   int ki = ks_index(h, s, k);
   if (ki < 0 || !hpsi) return DEREK_ERR_BAD_ARG;
   const KSetDev &K = h->ks[ki];
-  int st = apply_h_items(h, K.item0, K.nb, h->cur_psi(), nullptr, h->d_HX, nullptr);
+  // an SCF leaves its converged systems masked off on the device
+  int st = activate_all(h);
+  if (st) return st;
+  st = apply_h_items(h, K.item0, K.nb, h->cur_psi(), nullptr, h->d_HX, nullptr);
   if (st) return st;
   return copy_slice(h, ki, h->d_HX, hpsi, false);
 }
@@ -1048,58 +1064,64 @@ unsigned long long derek_gpu_launch_count(void) { return launch_total(); }
 int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage) {
   if (!h || nrep <= 0) return DEREK_ERR_BAD_ARG;
   if (reject_spinor(h, "time_apply_h")) return DEREK_ERR_UNSUPPORTED;
-  cudaEvent_t ev[4];
-  for (auto &e : ev) DEREK_CUDA(h, cudaEventCreate(&e));
-  double tot[3] = {0, 0, 0};
   // converged systems are masked off on the device; time every system
   std::vector<SysDev> all = h->sys;
   for (auto &s : all) s.active = 1;
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, all.data(), all.size() * sizeof(SysDev),
                                 cudaMemcpyHostToDevice, h->stream));
+  // the chunks apply_h_items runs, with events around each stage of each chunk
+  struct Chunk {
+    const derek_gpu::ItemClass *c;
+    int i0, n;
+  };
+  std::vector<Chunk> chunks;
+  for (const auto &c : h->classes) {
+    const int step = h->tune.hpsi_chunk > 0 ? h->tune.hpsi_chunk : c.count;
+    for (int i0 = 0; i0 < c.count; i0 += step) chunks.push_back({&c, i0, std::min(step, c.count - i0)});
+  }
+  std::vector<cudaEvent_t> ev(4 * chunks.size());
+  for (auto &e : ev) DEREK_CUDA(h, cudaEventCreate(&e));
+  double tot[3] = {0, 0, 0};
   const void *in = h->cur_psi();
   for (int r = 0; r < nrep; ++r) {
-    cudaEventRecord(ev[0], h->stream);
-    for (const auto &c : h->classes) {
+    for (size_t q = 0; q < chunks.size(); ++q) {
+      const auto &ch = chunks[q];
+      const auto &c = *ch.c;
       Tables t = h->tab;
-      t.item_list = c.d_list;
+      t.item_list = c.d_list ? c.d_list + ch.i0 : nullptr;
+      const int ib = c.d_list ? 0 : ch.i0;
+      cudaEventRecord(ev[4 * q], h->stream);
       if (h->prec == DEREK_PREC_FP64)
-        launch_x_inv<double>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const double2 *)in,
+        launch_x_inv<double>(t, ib, ch.n, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const double2 *)in,
                              (double2 *)h->d_abuf, nullptr, h->stream);
       else
-        launch_x_inv<float>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const float2 *)in,
+        launch_x_inv<float>(t, ib, ch.n, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const float2 *)in,
                             (float2 *)h->d_abuf, nullptr, h->stream);
-    }
-    cudaEventRecord(ev[1], h->stream);
-    for (const auto &c : h->classes) {
-      Tables t = h->tab;
-      t.item_list = c.d_list;
+      cudaEventRecord(ev[4 * q + 1], h->stream);
       if (h->prec == DEREK_PREC_FP64)
-        launch_plane<double>(t, 0, c.count, c.n[0], c.n[1], c.n[2], disp_min(h, c.n[1]), disp_min(h, c.n[2]),
+        launch_plane<double>(t, ib, ch.n, c.n[0], c.n[1], c.n[2], disp_min(h, c.n[1]), disp_min(h, c.n[2]),
                              c.disp_m, (double2 *)h->d_abuf, h->d_vloc, h->stream);
       else
-        launch_plane<float>(t, 0, c.count, c.n[0], c.n[1], c.n[2], disp_min(h, c.n[1]), disp_min(h, c.n[2]),
+        launch_plane<float>(t, ib, ch.n, c.n[0], c.n[1], c.n[2], disp_min(h, c.n[1]), disp_min(h, c.n[2]),
                             c.disp_m, (float2 *)h->d_abuf, h->d_vloc32, h->stream);
-    }
-    cudaEventRecord(ev[2], h->stream);
-    for (const auto &c : h->classes) {
-      Tables t = h->tab;
-      t.item_list = c.d_list;
+      cudaEventRecord(ev[4 * q + 2], h->stream);
       if (h->prec == DEREK_PREC_FP64)
-        launch_x_fwd<double>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m,
+        launch_x_fwd<double>(t, ib, ch.n, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m,
                              (const double2 *)h->d_abuf, (const double2 *)in, nullptr, (double2 *)h->d_HX,
                              nullptr, h->stream);
       else
-        launch_x_fwd<float>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m,
+        launch_x_fwd<float>(t, ib, ch.n, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m,
                             (const float2 *)h->d_abuf, (const float2 *)in, nullptr, (float2 *)h->d_HX,
                             nullptr, h->stream);
+      cudaEventRecord(ev[4 * q + 3], h->stream);
     }
-    cudaEventRecord(ev[3], h->stream);
-    DEREK_CUDA(h, cudaEventSynchronize(ev[3]));
-    for (int k = 0; k < 3; ++k) {
-      float ms = 0;
-      cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
-      tot[k] += ms;
-    }
+    DEREK_CUDA(h, cudaEventSynchronize(ev.back()));
+    for (size_t q = 0; q < chunks.size(); ++q)
+      for (int k = 0; k < 3; ++k) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev[4 * q + k], ev[4 * q + k + 1]);
+        tot[k] += ms;
+      }
   }
   for (auto &e : ev) cudaEventDestroy(e);
   DEREK_CUDA(h, cudaGetLastError());

@@ -13,8 +13,11 @@
 //   rows   the row layout each grid-size class's H.psi stage kernels are
 //          dispatched with (the tightest layout holding the class's spheres,
 //          the compact N/4 + 1 rows, or every row), timed on a full H.psi;
-//   overlap tensor cores or CUDA cores and the split-K length (2048, 4096 or
-//          8192 coefficients per CTA) of S = X^H X;
+//   chunk  the items per chunk of the three H.psi stage launches (all, or
+//          2048 ... 128: a chunk whose x-plane buffer fits in L2 reads it back
+//          from L2), timed on a full H.psi;
+//   overlap tensor cores or CUDA cores and the split-K length (512 ... 8192
+//          coefficients per CTA) of S = X^H X;
 //   rotate tensor cores or CUDA cores for X <- X C;
 //   jacobi one CTA per k-set or a two-CTA cluster.
 // The reference plans its FFTs with FFTW_ESTIMATE (Source/fft.f90:204-212),
@@ -422,6 +425,31 @@ struct Tuner {
     return DEREK_OK;
   }
 
+  // items per chunk of the H.psi stage launches: the x-plane buffer of a
+  // chunk that fits in L2 is re-read from L2 instead of HBM
+  int chunks() {
+    std::string key = std::string("hpsi_chunk prec=") + prec_name(h) + " items=" + std::to_string(h->nitems);
+    for (const auto &c : h->classes) key += " " + std::to_string(c.n[0]) + ":" + std::to_string(c.count);
+    std::string v;
+    if (lookup(key, v)) {
+      h->tune.hpsi_chunk = std::max(0, std::atoi(v.c_str()));
+      ++cached;
+      return DEREK_OK;
+    }
+    float best = 1e30f;
+    int best_c = 0;
+    for (int c : {0, 2048, 1024, 512, 256, 128}) {
+      if (c >= h->nitems) continue;
+      h->tune.hpsi_chunk = c;
+      const float ms = time_hpsi();
+      if (ms < best) best = ms, best_c = c;
+    }
+    h->tune.hpsi_chunk = best_c;
+    cache[key] = std::to_string(best_c);
+    ++tuned;
+    return DEREK_OK;
+  }
+
   std::string shape_key(const char *what) {
     return std::string(what) + " prec=" + prec_name(h) + " nb=" + std::to_string(h->max_nb_band) +
            " npw=" + std::to_string(h->max_npw_band) + " nks=" + std::to_string(h->nks);
@@ -433,7 +461,7 @@ struct Tuner {
     if (lookup(key, v)) {
       char path[16] = {0};
       int ks = 0;
-      if (std::sscanf(v.c_str(), "%15s %d", path, &ks) == 2 && ks >= kOverlapSplit && ks % kOverlapSplit == 0 &&
+      if (std::sscanf(v.c_str(), "%15s %d", path, &ks) == 2 && ks >= kOverlapSplitMin && ks % kOverlapSplitMin == 0 &&
           (std::strcmp(path, "cuda") == 0 || tc_capable(h))) {
         h->tune.overlap_tc = std::strcmp(path, "tc") == 0 ? 1 : 0;
         h->tune.ksplit = ks;
@@ -444,7 +472,7 @@ struct Tuner {
     float best = 1e30f;
     int best_tc = 0, best_ks = kOverlapSplit;
     for (int tc = 0; tc <= (tc_capable(h) ? 1 : 0); ++tc)
-      for (int ks : {kOverlapSplit, 2 * kOverlapSplit, 4 * kOverlapSplit}) {
+      for (int ks : {kOverlapSplitMin, 2 * kOverlapSplitMin, kOverlapSplit, 2 * kOverlapSplit, 4 * kOverlapSplit}) {
         h->tune.overlap_tc = tc;
         h->tune.ksplit = ks;
         const float ms = tm.best(h, 3, [&] { overlap_all(h, h->d_X, h->d_X, h->d_S, 1); });
@@ -545,7 +573,8 @@ std::string plan_json(const derek_gpu *h) {
     o << (first ? "" : ", ") << "\"" << c.n[0] << "x" << c.n[1] << "x" << c.n[2] << "\": \"" << name << "\"";
     first = false;
   }
-  o << "}, \"overlap\": \"" << (use_tc_overlap(h) ? "tc" : "cuda") << " ksplit " << h->tune.ksplit
+  o << "}, \"hpsi_chunk\": " << h->tune.hpsi_chunk;
+  o << ", \"overlap\": \"" << (use_tc_overlap(h) ? "tc" : "cuda") << " ksplit " << h->tune.ksplit
     << "\", \"rotate\": \"" << (use_tc_rotate(h) ? "tc" : "cuda") << "\", \"jacobi\": \""
     << (h->tune.jacobi_single ? "single" : "pair") << "\"}";
   return o.str();
@@ -585,6 +614,7 @@ int derek_gpu_autotune(derek_gpu_t *h, const char *cache_path, int flags) {
   if (!st) st = t.fft_radices();
   if (!st) st = t.lines();
   if (!st) st = t.rows();
+  if (!st) st = t.chunks();
   if (!st) st = apply_h_items(h, 0, h->nitems, h->d_X, nullptr, h->d_HX, nullptr);
   if (!st) st = t.overlap();
   if (!st) st = t.jacobi();

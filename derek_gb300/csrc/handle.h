@@ -136,6 +136,7 @@ struct derek_gpu {
     int rotate_tc = -1;
     int jacobi_single = 0;   // 1: one CTA per k-set even where the two-CTA cluster fits
     int generic_lines = 0;   // 1: shared-memory line kernels with the runtime splits sys[].lp
+    int hpsi_chunk = 0;      // H.psi items per chunk of the three stage launches (0: a class at once)
     std::string source = "default";   // "default", "tuned" or "cache"
   } tune;
 
@@ -186,6 +187,10 @@ bool use_tc_overlap(const derek_gpu *h);
 bool use_tc_rotate(const derek_gpu *h);
 int overlap_all(derek_gpu *h, const void *A, const void *B, double2 *out, int hermitize);
 int rotate_all(derek_gpu *h, void *X, const double2 *C);
+// The host copy of the system table (every system active) back on the
+// device: the SCF masks converged systems off there, the primitives
+// (apply_h, overlap) work on any system.
+int activate_all(derek_gpu *h);
 // minimum first argument of the stage launchers: the class's own size, or -1
 // to force the shared-memory kernels with runtime line splits
 inline int disp_min(const derek_gpu *h, int n) { return h->tune.generic_lines ? -1 : n; }

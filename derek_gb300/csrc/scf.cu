@@ -336,7 +336,7 @@ extern "C" int derek_scf_alloc(derek_gpu_t *h) {
     h->mat_off.push_back(moff);
     moff += (long long)K.nb * K.nb;
     opart_off.push_back(poff);
-    poff += (long long)((K.npw + kOverlapSplit - 1) / kOverlapSplit) * K.nb * K.nb;
+    poff += (long long)((K.npw + kOverlapSplitMin - 1) / kOverlapSplitMin) * K.nb * K.nb;
     h->max_npw = std::max(h->max_npw, K.npw);
   }
   for (const auto &K : h->ks_band) {
@@ -405,6 +405,7 @@ extern "C" {
 
 int derek_gpu_overlap(derek_gpu_t *h, int s, int k, double *out) {
   if (!h || s < 0 || s >= h->nsys || k < 0 || k >= h->sys[s].nk || !out) return DEREK_ERR_BAD_ARG;
+  if (int st = activate_all(h)) return st;   // an SCF leaves converged systems masked off
   const int ki = h->sys[s].ks0 + k;
   const KSetDev &K = h->ks[ki];
   if (h->sys[s].nspinor == 2) {

@@ -7,7 +7,8 @@
 namespace derek {
 
 constexpr int kMaxBands = 128;   // per k-set (rotation kernel register tile)
-constexpr int kOverlapSplit = 2048;
+constexpr int kOverlapSplit = 2048;      // default split-K (complex coefficients per CTA)
+constexpr int kOverlapSplitMin = 512;    // smallest split the partial buffers hold
 
 template <typename R>
 void launch_overlap(const Tables &t, int ks_begin, int nks, int max_nb, int max_npw, int ksplit,

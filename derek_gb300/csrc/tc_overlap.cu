@@ -187,7 +187,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   // thread tid is c = tid + q TC_THREADS.  The raw chunks of the next K block
   // are loaded into registers while the current one is converted.
   constexpr int QJ = 2 * TC_M * 8 / TC_THREADS;   // jobs per thread at nb = 128
-  const int njobs = 2 * nb * 8;
+  // S = X^H X (Y == X): the A job's chunk also gives the B rows, so Y is not
+  // loaded a second time
+  const bool same = X == Y;
+  const int njobs = (same ? 1 : 2) * nb * 8;
   // rows no job writes stay zero: A rows >= nb, B rows >= 2 nb (both stages)
   for (int s2 = 0; s2 < 2; ++s2) {
     unsigned char *A_hi = stage[s2], *A_lo = A_hi + a_bytes, *B_hi = A_lo + a_bytes,
@@ -265,6 +268,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (!isB) {
           *reinterpret_cast<uint4 *>(A_hi + core_off(row, k8)) = hi;
           *reinterpret_cast<uint4 *>(A_lo + core_off(row, k8)) = lo;
+          if (same) {
+            *reinterpret_cast<uint4 *>(B_hi + core_off(row, k8)) = hi;
+            *reinterpret_cast<uint4 *>(B_lo + core_off(row, k8)) = lo;
+            const float w[8] = {v[1], -v[0], v[3], -v[2], v[5], -v[4], v[7], -v[6]};
+            split8(w, hi, lo);
+            *reinterpret_cast<uint4 *>(B_hi + core_off(nb + row, k8)) = hi;
+            *reinterpret_cast<uint4 *>(B_lo + core_off(nb + row, k8)) = lo;
+          }
         } else {
           *reinterpret_cast<uint4 *>(B_hi + core_off(row, k8)) = hi;
           *reinterpret_cast<uint4 *>(B_lo + core_off(row, k8)) = lo;

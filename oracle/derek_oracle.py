@@ -535,20 +535,25 @@ def _rayleigh_ritz(sys, kb, vloc, X, workers):
 
 
 def eigensolve_filtered(sys: System, kb: KBasis, vloc: np.ndarray, X: np.ndarray, nconv: int,
-                        tol: float = 1e-9, degree: int = 12, max_pass: int = 400, workers=None):
+                        tol: float = 1e-9, degree: int = 12, max_pass: int = 400, workers=None,
+                        ntight: int = None, tail_tol: float = 1e-7):
     """Lowest eigenpairs of H(k) by Chebyshev-filtered subspace iteration with
     Rayleigh-Ritz (Zhou, Saad, Tiago, Chelikowsky, J. Comput. Phys. 219
     (2006) 172), in FP64.  X (m, npw) is the start block (m > nconv buffer
     rows speed up the lowest nconv).  Iterates until the residual norms
-    |H x - eps x| of the lowest nconv Ritz pairs are below tol; returns
-    (eps (m,), X (m, npw) orthonormal Ritz vectors, passes).  The filter damps
+    |H x - eps x| of the lowest nconv Ritz pairs are below tol (with ntight
+    given: the lowest ntight below tol and the rest below max(tol, tail_tol),
+    for empty bands whose eigenvalue error, of order residual^2 / gap, stays
+    far below the parity tolerance); returns (eps (m,), X (m, npw)
+    orthonormal Ritz vectors, passes).  The filter damps
     [eps_top, b] with b = ecut + max V, an upper bound of the spectrum
     (kinetic <= ecut on the sphere, <psi|V|psi> <= max V |psi|^2)."""
     b = sys.ecut + float(vloc.max()) + 0.1
     w, X, HX = _rayleigh_ritz(sys, kb, vloc, X, workers)
     for p in range(max_pass):
-        R = HX[:nconv] - w[:nconv, None] * X[:nconv]
-        if float(np.max(np.linalg.norm(R, axis=1))) < tol:
+        R = np.linalg.norm(HX[:nconv] - w[:nconv, None] * X[:nconv], axis=1)
+        nt = nconv if ntight is None else max(1, min(ntight, nconv))
+        if float(np.max(R[:nt])) < tol and (nt == nconv or float(np.max(R[nt:])) < max(tol, tail_tol)):
             return w, X, p
         a, a0 = float(w[-1]), float(w[0])
         e, c = 0.5 * (b - a), 0.5 * (b + a)
@@ -866,8 +871,11 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
                 vecs.append(v.T.copy())
             else:
                 tol = max(eig_tol, min(1e-4, 0.01 * resid))
+                # bands below mu + 40 kT of the previous iteration carry the
+                # density and energy: those converge to tol, empty ones to 1e-7
+                nt = None if result is None else int(np.sum(result.eigenvalues[ik] < result.efermi + 40 * sys.kT)) + 1
                 w, X, _ = eigensolve_filtered(sys, kb, vloc, blocks[ik], sys.nbands, tol=tol,
-                                              workers=workers)
+                                              workers=workers, ntight=nt)
                 blocks[ik] = X
                 eigs[ik] = w[:sys.nbands]
                 vecs.append(X[:sys.nbands])

@@ -101,3 +101,30 @@ def test_restart_from_stored_wavefunctions(oracle):
     assert cold["converged"] and warm["converged"]
     assert warm["iterations"] < cold["iterations"]
     assert abs(warm["free_energy"] - float(d["free_energy"])) < 1e-8
+
+
+def test_primitives_after_a_converged_scf(oracle):
+    """A converged SCF masks its systems off on the device; the overlap and
+    H.psi entry points still work on them afterwards (numpy conj(X) X^T at
+    1e-12, the oracle's H.psi in the SCF's last potential at 1e-11)."""
+    d = _fixture()
+    nb = int(d["nbands"])
+    with _handle(oracle, d, 0) as h:
+        rep = h.electronic_scf(max_scf=300, etol=1e-12)[0]
+        assert rep["converged"]
+        vloc = h.get_vloc()
+        rng = np.random.default_rng(8)
+        k = 1
+        npw = h.npw(0, k)
+        psi = rng.standard_normal((nb, npw)) + 1j * rng.standard_normal((nb, npw))
+        h.set_wfn(psi, 0, k)
+        s = h.wave_dot(0, k)
+        hpsi = h.pot_apply_wfn(0, k)
+    ref = psi.conj() @ psi.T
+    assert np.max(np.abs(s - ref)) / np.max(np.abs(ref)) < 1e-12
+    cell = d["cell"]
+    nf = tuple(int(x) for x in d["n_fine"])
+    sysm = oracle.System(cell, float(d["ecut"]), nf, oracle.grid_sizes(cell, float(d["ecut"]))[0], d["kpts"],
+                         d["wk"], nb, float(d["nelec"]), float(d["kT"]), vloc, d["wells"])
+    href = oracle.apply_h(sysm, oracle.KBasis(sysm, k), vloc, psi)
+    assert np.max(np.abs(hpsi - href)) / np.max(np.abs(href)) < 1e-11
