@@ -39,7 +39,7 @@ def test_tensor_core_wait_timeout_is_reported_and_the_handle_recovers(oracle):
     import derek_gb300 as dg
     d = _fixture()
     rng = np.random.default_rng(3)
-    with _handle(oracle, d, dg.DEREK_PREC_MIXED, use_tensor_cores=2) as h:
+    with _handle(oracle, d, dg.DEREK_PREC_MIXED, use_tensor_cores=2, density_tol=0.0) as h:
         npw = h.npw(0, 0)
         psi = rng.standard_normal((int(d["nbands"]), npw)) + 1j * rng.standard_normal((int(d["nbands"]), npw))
         h.set_wfn(psi, 0, 0)
@@ -58,7 +58,8 @@ def test_tensor_core_wait_timeout_is_reported_and_the_handle_recovers(oracle):
         p32 = psi.astype(np.complex64).astype(np.complex128)
         ref = p32.conj() @ p32.T
         assert np.max(np.abs(s - ref)) / np.max(np.abs(ref)) < 5e-5
-        rep = h.electronic_scf(max_scf=300, etol=1e-9)[0]
+        # the mixed path stops at 1e-7 Ha, as the other mixed-precision tests
+        rep = h.electronic_scf(max_scf=300, etol=1e-7)[0]
     assert rep["converged"]
     assert abs(rep["free_energy"] - float(d["free_energy"])) / float(d["nelec"]) < 1e-6
 

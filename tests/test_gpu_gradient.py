@@ -78,3 +78,35 @@ def test_adjoint_density_loss_gradient_matches_finite_differences(oracle):
         wm[w, p] -= h
         fd = (loss_and_grad(wp, False)[0] - loss_and_grad(wm, False)[0]) / (2 * h)
         assert abs(fd - g[w, p]) < 1e-4 * max(1.0, abs(fd)), (w, p, fd, g[w, p])
+
+
+def test_adjoint_config4_matches_oracle_finite_differences():
+    """The adjoint-gradient workload (L=12 bohr, Ecut 15 Ha, 48^3 grid, Gamma
+    + 2x2x2 k-points, 16 electrons in 20 bands, 8 wells): dL/dp of
+    L = sum (n - n_target)^2 dV from the adjoint solve, and the
+    Hellmann-Feynman dF/dp, against central differences (h = 1e-5) of the FP64
+    oracle's converged SCFs for three parameters (a depth, a width, a centre
+    coordinate; tests/golden/make_adjoint_golden.py).  n_target is the GPU's
+    own FP64 ground state of the second well set, which equals the oracle's
+    to the SCF tolerance."""
+    import os
+    import derek_gb300 as dg
+    from derek_gb300 import workloads
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "adjoint9k.npz")))
+    systems, mix = workloads.params("adjoint9k")
+    assert np.array_equal(systems[0]["wells"], d["wells"])
+    tgt = dict(systems[0], wells=d["target_wells"])
+    opts = dict(mix, density_tol=1e-11)
+    with dg.Handle(workloads.to_specs([tgt]), precision=dg.DEREK_PREC_FP64, **opts) as h:
+        rt = h.electronic_scf(max_scf=400, etol=1e-13)[0]
+        n_t = h.density()
+    assert rt["converged"] and abs(rt["free_energy"] - d["target_free_energy"]) < 1e-8
+    with dg.Handle(workloads.to_specs(systems), precision=dg.DEREK_PREC_FP64, **opts) as h:
+        r0 = h.electronic_scf(max_scf=400, etol=1e-13)[0]
+        hf = h.grad_wells()
+        loss, g = h.grad_density_loss(n_t, tol=1e-11)
+    assert r0["converged"] and abs(r0["free_energy"] - d["free_energy"]) < 1e-8
+    assert abs(loss - d["loss"]) < 1e-8 * max(1.0, abs(float(d["loss"])))
+    for (w, c), fd_l, fd_f in zip(d["params"], d["fd_loss"], d["fd_free"]):
+        assert abs(g[w, c] - fd_l) < 1e-5 * max(1.0, abs(fd_l)), (w, c, g[w, c], fd_l)
+        assert abs(hf[w, c] - fd_f) < 1e-6 * max(1.0, abs(fd_f)), (w, c, hf[w, c], fd_f)

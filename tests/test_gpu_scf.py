@@ -232,3 +232,39 @@ def test_library_built_vext_matches_oracle(oracle, case):
             ref = oracle.vext_jellium_wells(s["cell"], nf, s["nelec"], s["wells"])
             got = h.get_vext(si)
             assert np.max(np.abs(got - ref)) < 1e-13, (si, np.max(np.abs(got - ref)))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kpts64_k4_matches_oracle(precision):
+    """The 64-k-point benchmark system (72^3 grid, Ecut 20 Ha, 64 electrons in
+    80 bands, 16 wells, Kerker + Pulay) on its first 4 k-points, against the
+    FP64 oracle's fixture (tests/golden/make_scf_golden.py scf_kpts64_k4,
+    Chebyshev-filtered oracle eigensolver).  FP64: F, E, Fermi level and all
+    4 x 80 eigenvalues within 1e-8 Ha, density within 1e-7 (relative L2 on
+    every 17th point).  Mixed, stopped at |dF| < 1e-7 Ha per electron as the
+    benchmark: |dF| / N_e < 1e-6 Ha and eigenvalues within 1e-4 Ha."""
+    import derek_gb300 as dg
+    from derek_gb300 import workloads
+    d = load("scf_kpts64_k4")
+    systems, mix = workloads.params("kpts64_k4")
+    assert np.array_equal(systems[0]["wells"], d["wells"]) and np.array_equal(systems[0]["kpts"], d["kpts"])
+    specs = workloads.to_specs(systems)
+    if precision == 0:
+        opts, etol, per_e = dict(density_tol=1e-9), 1e-11, 0
+    else:
+        opts, etol, per_e = dict(density_tol=0.0), 1e-7, 1
+    with dg.Handle(specs, precision=precision, etol_per_electron=per_e, **mix, **opts) as h:
+        rep = h.electronic_scf(max_scf=200, etol=etol)[0]
+        eig = h.eigenvalues()
+        rho = h.density()
+    assert rep["converged"], rep
+    if precision == 0:
+        assert abs(rep["free_energy"] - d["free_energy"]) < 1e-8, (rep["free_energy"], float(d["free_energy"]))
+        assert abs(rep["energy"] - d["energy"]) < 1e-8
+        assert abs(rep["efermi"] - d["efermi"]) < 1e-8
+        assert np.max(np.abs(eig - d["eig"])) < 1e-8, np.max(np.abs(eig - d["eig"]))
+        sub = rho[::int(d["density_stride"])]
+        assert np.linalg.norm(sub - d["density"]) / np.linalg.norm(d["density"]) < 1e-7
+    else:
+        assert abs(rep["free_energy"] - d["free_energy"]) / float(d["nelec"]) < 1e-6
+        assert np.max(np.abs(eig - d["eig"])) < 1e-4
