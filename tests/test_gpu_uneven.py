@@ -5,7 +5,11 @@ the FP64 oracle's converged states of three of them
 
 FP64 path: free energy, energy, Fermi level and eigenvalues within 1e-8 Ha,
 density within 1e-7 (relative L2 on the stored points); every system of the
-slice converges.  Mixed path: |dF| / N_e < 1e-6 Ha per electron.
+slice converges.  Mixed path: |dF| / N_e < 1e-6 Ha per electron.  The
+mixed SCF stops at |dF| < 3e-8 Ha per electron here, below the benchmark's
+1e-7: the benchmark compares two runs stopped by the same rule, this test
+compares with the oracle's fixed point, and at 1e-7 the stopping rule alone
+leaves a system up to ~1e-6 Ha/e from it (measured: system 71 at 1.0e-6).
 """
 import os
 
@@ -35,7 +39,7 @@ def test_uneven_slice_matches_oracle(precision):
         etol, per_e = 1e-11, 0
     else:
         opts.update(density_tol=0.0)
-        etol, per_e = 1e-7, 1
+        etol, per_e = 3e-8, 1
     with dg.Handle(workloads.to_specs(systems), precision=precision, etol_per_electron=per_e, **opts) as h:
         rep = h.electronic_scf(max_scf=300, etol=etol)
         got = {i: (rep[SLICE.index(i)], h.eigenvalues(SLICE.index(i)), h.density(SLICE.index(i)))
