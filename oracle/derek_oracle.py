@@ -536,7 +536,7 @@ def _rayleigh_ritz(sys, kb, vloc, X, workers):
 
 def eigensolve_filtered(sys: System, kb: KBasis, vloc: np.ndarray, X: np.ndarray, nconv: int,
                         tol: float = 1e-9, degree: int = 12, max_pass: int = 400, workers=None,
-                        ntight: int = None, tail_tol: float = 1e-7):
+                        ntight: int = None, tail_tol: float = 1e-7, fixed_passes: int = None):
     """Lowest eigenpairs of H(k) by Chebyshev-filtered subspace iteration with
     Rayleigh-Ritz (Zhou, Saad, Tiago, Chelikowsky, J. Comput. Phys. 219
     (2006) 172), in FP64.  X (m, npw) is the start block (m > nconv buffer
@@ -545,16 +545,21 @@ def eigensolve_filtered(sys: System, kb: KBasis, vloc: np.ndarray, X: np.ndarray
     given: the lowest ntight below tol and the rest below max(tol, tail_tol),
     for empty bands whose eigenvalue error, of order residual^2 / gap, stays
     far below the parity tolerance); returns (eps (m,), X (m, npw)
-    orthonormal Ritz vectors, passes).  The filter damps
+    orthonormal Ritz vectors, passes); with fixed_passes, exactly that many
+    filter passes and no convergence test.  The filter damps
     [eps_top, b] with b = ecut + max V, an upper bound of the spectrum
     (kinetic <= ecut on the sphere, <psi|V|psi> <= max V |psi|^2)."""
     b = sys.ecut + float(vloc.max()) + 0.1
     w, X, HX = _rayleigh_ritz(sys, kb, vloc, X, workers)
-    for p in range(max_pass):
-        R = np.linalg.norm(HX[:nconv] - w[:nconv, None] * X[:nconv], axis=1)
-        nt = nconv if ntight is None else max(1, min(ntight, nconv))
-        if float(np.max(R[:nt])) < tol and (nt == nconv or float(np.max(R[nt:])) < max(tol, tail_tol)):
-            return w, X, p
+    for p in range(max_pass if fixed_passes is None else fixed_passes + 1):
+        if fixed_passes is not None:
+            if p == fixed_passes:
+                return w, X, p
+        else:
+            R = np.linalg.norm(HX[:nconv] - w[:nconv, None] * X[:nconv], axis=1)
+            nt = nconv if ntight is None else max(1, min(ntight, nconv))
+            if float(np.max(R[:nt])) < tol and (nt == nconv or float(np.max(R[nt:])) < max(tol, tail_tol)):
+                return w, X, p
         a, a0 = float(w[-1]), float(w[0])
         e, c = 0.5 * (b - a), 0.5 * (b + a)
         sigma = e / (a0 - c)
@@ -815,7 +820,8 @@ class ScfResult:
 def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3,
         history: int = 8, q0: float = 0.0, solver: str = "dense", verbose: bool = False,
         rtol: float = None, buffer: int = 8, eig_tol: float = 1e-9, workers=None,
-        nin0: np.ndarray = None, blocks0: list = None, keep: dict = None) -> ScfResult:
+        nin0: np.ndarray = None, blocks0: list = None, keep: dict = None,
+        passes: int = None) -> ScfResult:
     """Self-consistent field loop (the intended electronic_scf,
     Source/electronic.f90:86-175: iterate until |E - E_prev| < etol).
 
@@ -828,7 +834,13 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
     Start density: uniform Ne/Omega, or nin0; the filtered solver starts
     from blocks0 when given (a previous run's keep["blocks"]: a warm start
     for nearby parameters).  With rtol set, convergence also needs
-    max|n_out - n_in| < rtol.
+    max|n_out - n_in| < rtol.  With `passes` the filtered solver runs that
+    many filter passes per iteration instead of converging each eigenproblem
+    (the subspace then converges together with the density, as in
+    Chebyshev-filtered SCF); once the SCF test passes, the last iteration's
+    eigenproblem is solved to eig_tol and that iteration's occupations,
+    output density and energies are recomputed from it, so the result is the
+    same fixed point the converged-per-iteration solver reaches.
     """
     import scipy.linalg as sla
 
@@ -856,11 +868,7 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
     e_prev = None
     hist = []
     result = None
-    for it in range(1, max_scf + 1):
-        vh, _ = hartree(sys, nin)
-        _, vxc = lda_exc_vxc(nin)
-        vhxc = vh + vxc
-        vloc = sys.vext + vhxc
+    def evaluate(nin, vhxc, vloc, exact):
         eigs = np.zeros((len(kbs), sys.nbands))
         vecs = []
         for ik, kb in enumerate(kbs):
@@ -870,12 +878,13 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
                 eigs[ik] = w
                 vecs.append(v.T.copy())
             else:
-                tol = max(eig_tol, min(1e-4, 0.01 * resid))
+                tol = eig_tol if exact else max(eig_tol, min(1e-4, 0.01 * resid))
                 # bands below mu + 40 kT of the previous iteration carry the
                 # density and energy: those converge to tol, empty ones to 1e-7
                 nt = None if result is None else int(np.sum(result.eigenvalues[ik] < result.efermi + 40 * sys.kT)) + 1
                 w, X, _ = eigensolve_filtered(sys, kb, vloc, blocks[ik], sys.nbands, tol=tol,
-                                              workers=workers, ntight=nt)
+                                              workers=workers, ntight=nt,
+                                              fixed_passes=None if exact else passes)
                 blocks[ik] = X
                 eigs[ik] = w[:sys.nbands]
                 vecs.append(X[:sys.nbands])
@@ -892,7 +901,14 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
         exc = dv * float(np.dot(nout, exc_eps))
         e_dc = dv * float(np.dot(vhxc, nout))
         energy = eband - e_dc + eh + exc
-        free = energy - sys.kT * ent
+        return eigs, f, mu, ent, nout, energy, energy - sys.kT * ent
+
+    for it in range(1, max_scf + 1):
+        vh, _ = hartree(sys, nin)
+        _, vxc = lda_exc_vxc(nin)
+        vhxc = vh + vxc
+        vloc = sys.vext + vhxc
+        eigs, f, mu, ent, nout, energy, free = evaluate(nin, vhxc, vloc, False)
         resid = float(np.max(np.abs(nout - nin)))
         hist.append((it, energy, free, mu, resid))
         if verbose:
@@ -901,6 +917,14 @@ def scf(sys: System, max_scf: int = 100, etol: float = 1e-10, alpha: float = 0.3
         if keep is not None and blocks is not None:
             keep["blocks"] = blocks
         if e_prev is not None and abs(free - e_prev) < etol and (rtol is None or resid < rtol):
+            if blocks is not None and passes is not None:
+                # the last iteration's eigenproblem solved to eig_tol
+                eigs, f, mu, ent, nout, energy, free = evaluate(nin, vhxc, vloc, True)
+                resid = float(np.max(np.abs(nout - nin)))
+                hist.append((it, energy, free, mu, resid))
+                if verbose:
+                    print(f"exact {it:3d} E={energy:.12f} F={free:.12f} mu={mu:.8f} |R|={resid:.2e}")
+                result = ScfResult(False, it, energy, free, mu, eigs, f, nout, hist)
             result.converged = True
             break
         e_prev = free
