@@ -69,11 +69,13 @@ static void apply_h_t(derek_gpu *h, const Tables &base, int item_begin, int nite
     // a class in chunks of tune.hpsi_chunk items: a chunk's x-plane buffer
     // (~0.47 MB per item at 72^3) can stay in L2 between the three stages
     for (const auto &c : h->classes) {
-      const int step = h->tune.hpsi_chunk > 0 ? h->tune.hpsi_chunk : c.count;
-      for (int i0 = 0; i0 < c.count; i0 += step) {
+      const int *list = c.launch_list();
+      const int count = c.launch_count();
+      const int step = h->tune.hpsi_chunk > 0 ? h->tune.hpsi_chunk : count;
+      for (int i0 = 0; i0 < count; i0 += step) {
         Tables t = base;
-        t.item_list = c.d_list ? c.d_list + i0 : nullptr;
-        apply_h_class<R>(h, t, c.d_list ? 0 : i0, std::min(step, c.count - i0), c.nchunk, c.n, c.disp_m, in,
+        t.item_list = list ? list + i0 : nullptr;
+        apply_h_class<R>(h, t, list ? 0 : i0, std::min(step, count - i0), c.nchunk, c.n, c.disp_m, in,
                          prev, out, coef, vloc);
       }
     }
@@ -106,6 +108,27 @@ int apply_h_items(derek_gpu *h, int item_begin, int nitems, const void *in, cons
   return DEREK_OK;
 }
 
+bool compact_classes(derek_gpu *h, const std::vector<int> &sys_active) {
+  bool changed = false;
+  for (auto &c : h->classes) {
+    std::vector<int> keep;
+    keep.reserve(c.items.size());
+    for (int it : c.items)
+      if (sys_active[h->ks[h->item_ks[it]].sys]) keep.push_back(it);
+    if ((int)keep.size() == c.launch_count()) continue;
+    if (!keep.empty() && cudaMemcpyAsync(c.d_active, keep.data(), keep.size() * sizeof(int),
+                                         cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+      continue;   // keep the previous list: still a superset of the active items
+    c.active_count = (int)keep.size();
+    changed = true;
+  }
+  return changed;
+}
+
+void reset_classes(derek_gpu *h) {
+  for (auto &c : h->classes) c.active_count = -1;
+}
+
 int activate_all(derek_gpu *h) {
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
                                 cudaMemcpyHostToDevice, h->stream));
@@ -125,9 +148,9 @@ int apply_h_items_ex(derek_gpu *h, const Tables &base, int item_begin, int nitem
 template <typename R> static void density_t(derek_gpu *h, const void *psi) {
   for (const auto &c : h->classes) {
     Tables t = h->tab;
-    t.item_list = c.d_list;
-    launch_x_inv<R>(t, 0, c.count, c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m, (const cplx<R> *)psi,
-                    (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
+    t.item_list = c.launch_list();
+    launch_x_inv<R>(t, 0, c.launch_count(), c.nchunk, c.n[0], disp_min(h, c.n[0]), c.disp_m,
+                    (const cplx<R> *)psi, (cplx<R> *)h->d_abuf, h->d_occw, h->stream);
   }
   launch_density_plane<R>(h->tab, 0, h->nks, h->max_n[0], h->max_n[1], h->max_n[2], disp_min(h, h->min_n[1]),
                           disp_min(h, h->min_n[2]), h->max_m_all, (const cplx<R> *)h->d_abuf, h->d_occw,
@@ -304,8 +327,10 @@ int derek_gpu_destroy(derek_gpu_t *h) {
                   h->d_vnc_ext};
   for (void *p : ptrs)
     if (p) cudaFree(p);
-  for (auto &c : h->classes)
+  for (auto &c : h->classes) {
     if (c.d_list) cudaFree(c.d_list);
+    if (c.d_active) cudaFree(c.d_active);
+  }
   derek_scf_free(h);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -685,6 +710,8 @@ int derek_gpu_create(derek_gpu_t **out, const derek_sys_desc *desc, int nsys,
       c.disp_m = c.max_m;
       c.d_list = nullptr;
       if (groups.size() > 1) CK(upload(&c.d_list, g.second));
+      c.items = g.second;
+      CK(cudaMalloc((void **)&c.d_active, std::max<size_t>(c.items.size(), 1) * sizeof(int)));
       h->classes.push_back(c);
     }
   }

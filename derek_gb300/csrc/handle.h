@@ -123,6 +123,14 @@ struct derek_gpu {
     int max_m;     // largest |centred Miller index| (x, y or z) of a sphere entry in the class
     int disp_m;    // row bound the stage kernels are dispatched with (>= max_m; autotuned)
     int *d_list;   // nullptr when the class is the contiguous range of all items
+    // the class's items of the still-active systems, used by the SCF's H.psi
+    // and density passes once many systems have converged (active_count < 0:
+    // the full list)
+    std::vector<int> items;
+    int *d_active = nullptr;
+    int active_count = -1;
+    const int *launch_list() const { return active_count >= 0 ? d_active : d_list; }
+    int launch_count() const { return active_count >= 0 ? active_count : count; }
   };
   std::vector<ItemClass> classes;
   std::vector<int> ks_max_m;    // per k-set: largest |centred Miller index| of its sphere
@@ -191,6 +199,12 @@ int rotate_all(derek_gpu *h, void *X, const double2 *C);
 // device: the SCF masks converged systems off there, the primitives
 // (apply_h, overlap) work on any system.
 int activate_all(derek_gpu *h);
+// SCF work lists: compact_classes keeps, per grid class, the items of the
+// systems still active (sys_active[s] != 0) and returns true when a list
+// changed; reset_classes goes back to the full lists.  Only the all-items
+// H.psi and the density pass use them (set while an SCF runs).
+bool compact_classes(derek_gpu *h, const std::vector<int> &sys_active);
+void reset_classes(derek_gpu *h);
 // minimum first argument of the stage launchers: the class's own size, or -1
 // to force the shared-memory kernels with runtime line splits
 inline int disp_min(const derek_gpu *h, int n) { return h->tune.generic_lines ? -1 : n; }

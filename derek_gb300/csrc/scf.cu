@@ -164,6 +164,36 @@ int finish_iteration(derek_gpu *h) {
   return DEREK_OK;
 }
 
+void drop_graphs(derek_gpu *h) {
+  for (auto &g : h->graph_exec)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+// back to the full work lists; true when some class had a compacted one
+bool reset_lists(derek_gpu *h) {
+  bool any = false;
+  for (const auto &c : h->classes) any |= c.active_count >= 0;
+  reset_classes(h);
+  return any;
+}
+
+// Once the still-active systems hold at most 60 % of the items the H.psi
+// and density passes launch over, those passes get lists of the active
+// systems' items only (the graphs captured with the longer lists are
+// dropped and recaptured): a converged system's items otherwise still cost
+// their blocks' exits and the plane pass's per-tile barriers every iteration.
+void maybe_compact(derek_gpu *h, const std::vector<SysState> &st) {
+  std::vector<int> act(h->nsys);
+  for (int s = 0; s < h->nsys; ++s) act[s] = !st[s].converged && !st[s].status;
+  long long live = 0, launched = 0;
+  for (int it = 0; it < h->nitems; ++it) live += act[h->ks[h->item_ks[it]].sys];
+  for (const auto &c : h->classes) launched += c.launch_count();
+  if (live > 0 && live * 10 <= launched * 6 && compact_classes(h, act)) drop_graphs(h);
+}
+
 // Start vectors in buf(cur): hashed entries (init_vectors 0) or plane waves
 // (1) in X; with 2 the wavefunctions stored by set_wfn (a restart from a
 // saved state) keep their bands and the buffer bands get plane-wave start
@@ -192,6 +222,7 @@ int start_vectors(derek_gpu *h) {
 int scf_start(derek_gpu *h, double etol) {
   // reset state: all systems active, uniform start density, start vectors
   for (auto &s : h->sys) s.active = 1;
+  if (reset_lists(h)) drop_graphs(h);
   DEREK_CUDA(h, cudaMemcpyAsync(h->d_sys, h->sys.data(), h->sys.size() * sizeof(SysDev),
                                 cudaMemcpyHostToDevice, h->stream));
   std::vector<SysState> st(h->nsys);
@@ -579,12 +610,16 @@ int derek_gpu_scf_run(derek_gpu_t *h, int max_scf, double etol, derek_scf_report
       if (x.status) {
         fill_reports(h, st, rep);
         h->last_error = derek_gpu_strerror(x.status);
+        if (reset_lists(h)) drop_graphs(h);
         return x.status;
       }
       all_done &= x.converged != 0;
     }
     if (all_done) break;
+    if (h->nsys > 1) maybe_compact(h, st);
   }
+  // the other entry points (H.psi, NSCF, gradients) work on every item
+  if (reset_lists(h)) drop_graphs(h);
   fill_reports(h, st, rep);
   for (const auto &x : st)
     if (!x.converged) return DEREK_ERR_NOT_CONVERGED;
