@@ -123,6 +123,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="kpts64")
     p.add_argument("--skip-fp64", action="store_true", help="skip the FP64 accuracy gate (debug)")
+    p.add_argument("--use-tensor-cores", type=int, default=None, choices=[0, 1, 2],
+                   help="mixed path: 0 CUDA cores, 1 tensor-core overlaps, 2 overlaps and rotations "
+                        "(default: the library's, 2)")
     p.add_argument("--fp64-warmup", type=int, default=1,
                    help="untimed FP64 solves before the timed one (graph capture)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -278,6 +281,8 @@ def run_ours(args):
     specs, mix = workloads.WORKLOADS[args.workload]()
     ETOL = ETOL_PER_E  # per electron: each system stops at |dF| < ETOL * its N_e
     scf_opts = dict(SOLVER, etol_per_electron=1, **mix)
+    if args.use_tensor_cores is not None:
+        scf_opts["use_tensor_cores"] = args.use_tensor_cores
     out = {"metric": METRIC, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "complex64 (FP32 FFT/H.psi) + FP64 subspace",

@@ -17,8 +17,9 @@
 //          2048 ... 128: a chunk whose x-plane buffer fits in L2 reads it back
 //          from L2), timed on a full H.psi;
 //   overlap tensor cores or CUDA cores and the split-K length (512 ... 8192
-//          coefficients per CTA) of S = X^H X;
-//   rotate tensor cores or CUDA cores for X <- X C;
+//          coefficients per CTA) of S = X^H X (tensor cores only for
+//          subspaces of 64 bands or more: accuracy, see kTcMinBands);
+//   rotate tensor cores or CUDA cores for X <- X C (the same rule);
 //   jacobi one CTA per k-set or a two-CTA cluster.
 // The reference plans its FFTs with FFTW_ESTIMATE (Source/fft.f90:204-212),
 // which picks a plan by heuristics without timing; it has no GPU kernels.
@@ -455,6 +456,15 @@ struct Tuner {
            " npw=" + std::to_string(h->max_npw_band) + " nks=" + std::to_string(h->nks);
   }
 
+  // Tensor cores for the subspace products only where the subspace has at
+  // least kTcMinBands bands.  The split-BF16 products carry ~2^-17 relative
+  // error per term; on the uneven batch (at most 44 bands) the CUDA-core
+  // paths kept 251 of 256 systems within 1e-6 Ha/e of the FP64 path against
+  // 241 with tensor cores, for 7 % more time (measured); at kpts64's 84
+  // bands the tensor cores are faster and within 2.5e-7 Ha/e.
+  static constexpr int kTcMinBands = 64;
+  bool tc_allowed() const { return tc_capable(h) && h->max_nb_band >= kTcMinBands; }
+
   int overlap() {
     const std::string key = shape_key("overlap");
     std::string v;
@@ -462,7 +472,7 @@ struct Tuner {
       char path[16] = {0};
       int ks = 0;
       if (std::sscanf(v.c_str(), "%15s %d", path, &ks) == 2 && ks >= kOverlapSplitMin && ks % kOverlapSplitMin == 0 &&
-          (std::strcmp(path, "cuda") == 0 || tc_capable(h))) {
+          (std::strcmp(path, "cuda") == 0 || tc_allowed())) {
         h->tune.overlap_tc = std::strcmp(path, "tc") == 0 ? 1 : 0;
         h->tune.ksplit = ks;
         ++cached;
@@ -471,7 +481,7 @@ struct Tuner {
     }
     float best = 1e30f;
     int best_tc = 0, best_ks = kOverlapSplit;
-    for (int tc = 0; tc <= (tc_capable(h) ? 1 : 0); ++tc)
+    for (int tc = 0; tc <= (tc_allowed() ? 1 : 0); ++tc)
       for (int ks : {kOverlapSplitMin, 2 * kOverlapSplitMin, kOverlapSplit, 2 * kOverlapSplit, 4 * kOverlapSplit}) {
         h->tune.overlap_tc = tc;
         h->tune.ksplit = ks;
@@ -488,6 +498,10 @@ struct Tuner {
   int rotate() {
     if (!(tc_capable(h) && h->opts.use_tensor_cores >= 2)) return DEREK_OK;
     const std::string key = shape_key("rotate");
+    if (!tc_allowed()) {   // a rule, not a timing: nothing to cache
+      h->tune.rotate_tc = 0;
+      return DEREK_OK;
+    }
     std::string v;
     if (lookup(key, v) && (v == "tc" || v == "cuda")) {
       h->tune.rotate_tc = v == "tc" ? 1 : 0;
