@@ -272,7 +272,8 @@ int derek_gpu_get_vext(derek_gpu_t *h, int sys, double *vext);
  * this process (graph replays count their kernels); derek_gpu_time_apply_h
  * runs H.psi on every band of every k-point nrep times and returns the mean
  * device time per application and per stage kernel (3 values: backward x
- * lines, (y,z) planes with V(r), forward x lines + gather + kinetic). */
+ * lines, (y,z) planes with V(r), forward x lines + gather + kinetic; zero
+ * for an all-spinor batch, whose 2x2 H.psi is timed as one). */
 void *derek_gpu_stream(derek_gpu_t *h);
 unsigned long long derek_gpu_launch_count(void);
 int derek_gpu_time_apply_h(derek_gpu_t *h, int nrep, double *ms_apply, double *ms_stage);

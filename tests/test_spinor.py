@@ -305,9 +305,8 @@ def test_spinor_potential_setters_and_limits(oracle):
         h.set_vloc(v)
         nc1 = h.get_nc_pot()
         assert np.array_equal(nc1[:, 0, 0], v.astype(complex)) and np.array_equal(nc1[:, 1, 1], v.astype(complex))
-        with pytest.raises(dg.DerekError) as e:
-            h.time_apply_h()
-        assert e.value.status == 8
+        ms, stages = h.time_apply_h(nrep=2)    # the 2x2 H.psi timed as one
+        assert ms > 0 and stages == [0.0, 0.0, 0.0]
     scalar = dg.SystemSpec(spec.cell, spec.ecut, spec.kpts, 4, 3.0, vext=spec.vext, n_fine=spec.n_fine)
     with dg.Handle(scalar) as h:
         with pytest.raises(dg.DerekError):
@@ -315,6 +314,9 @@ def test_spinor_potential_setters_and_limits(oracle):
     with dg.Handle([spec, scalar]) as h:   # spinor and scalar systems in one batch: primitives only
         with pytest.raises(dg.DerekError) as e:
             h.electronic_scf(max_scf=2)
+        assert e.value.status == 8
+        with pytest.raises(dg.DerekError) as e:
+            h.time_apply_h()
         assert e.value.status == 8
     too_many = dg.SystemSpec(spec.cell, spec.ecut, spec.kpts, 4, 5.0, vext=spec.vext, n_fine=spec.n_fine,
                              nspinor=2)
