@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(NT, 1) k_density_rows(Tables t, int ks_begin, 
       load_column<N, RY>(v, col);
       // clear this column's rows for the next band's gather
       for (int l = 0; l < nrow; ++l) col[rows_s[l] * PZ] = make_float2(0.f, 0.f);
-      reg_fft<N, +1, 0>(v);
+      reg_fft<N, +1, 0, Lay>(v);
       const float wf = (float)w;
       static_for<0, N>([&](auto mc) {
         constexpr int m = decltype(mc)::value;

@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
         else
           v[j] = make_float2(0.f, 0.f);
       });
-      reg_fft<N, +1, 0>(v);
+      reg_fft<N, +1, 0, Lay>(v);
       store_line<N, 1>(v, line, 1);
     }
     const int next = it + R;
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(NT, 1) k_plane_persist(Tables t, int item_begi
       const float *vz = Vs + p * VP + z;
       float2 v[N];
       load_column<N, RY>(v, col);
-      reg_fft<N, +1, 0>(v);
+      reg_fft<N, +1, 0, Lay>(v);
       static_for<0, N>([&](auto mc) {
         constexpr int mm = decltype(mc)::value;
         const float w = vz[mm * N];

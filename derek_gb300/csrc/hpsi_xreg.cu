@@ -38,6 +38,10 @@ __device__ __forceinline__ void prefetch_l2(const void *p, int bytes) {
 template <int N, int RX> __host__ __device__ constexpr bool x_kept(int j) {
   return mx_of<N>(j) >= -RX && mx_of<N>(j) <= RX;
 }
+// the x-line positions a sphere column can occupy, as a reg_fft input policy
+template <int N, int RX> struct XKept {
+  __host__ __device__ static constexpr bool kept(int j) { return x_kept<N, RX>(j); }
+};
 
 template <int N, int RX>
 __global__ void __launch_bounds__(kXThreads, 3) k_xinv_reg(Tables t, int item_begin, const float2 *__restrict__ psi,
@@ -64,7 +68,7 @@ __global__ void __launch_bounds__(kXThreads, 3) k_xinv_reg(Tables t, int item_be
       if ((unsigned)d < (unsigned)cnt) v[j] = src[d];
     }
   });
-  reg_fft<N, +1, 0>(v);
+  reg_fft<N, +1, 0, XKept<N, RX>>(v);
   const long long ld = K.ncol_pad;
   float2 *dst = abuf + K.a_off + (long long)b * N * ld + c;
   static_for<0, N>([&](auto mc) {

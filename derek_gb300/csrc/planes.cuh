@@ -87,7 +87,7 @@ __device__ __forceinline__ void z_pass(float2 *P, int np, int nrow, const short 
         else
           v[j] = make_float2(0.f, 0.f);
       });
-      reg_fft<N, SIGN, 0>(v);
+      reg_fft<N, SIGN, 0, Lay>(v);
       store_line<N, 1>(v, line, 1);
     } else {
       load_line<N>(v, line, 1);

@@ -85,6 +85,232 @@ __host__ __device__ constexpr CosSin turn_cs(int m, int n) {
 
 constexpr int gcd_int(int a, int b) { return b == 0 ? a : gcd_int(b, a % b); }
 
+// ---- DFTs with compile-time zero inputs -------------------------------------
+// DftZ<R_, R, SIGN, M> computes the same DFT as Dft<R_, R, SIGN> when bit j
+// of M marks the inputs that may be nonzero and every other input is zero.
+// Zero inputs are never read and the arithmetic they would enter is left
+// out (IEEE rules keep the compiler from dropping x + 0 or x * 0 on its
+// own).  Every output is written.  A full mask runs Dft itself, so dense
+// transforms are unchanged.
+constexpr unsigned dz_full(int r) { return r >= 32 ? 0xffffffffu : (1u << r) - 1u; }
+constexpr bool dz_bit(unsigned m, int i) { return ((m >> i) & 1u) != 0; }
+constexpr int dz_popc(unsigned m) {
+  int c = 0;
+  for (; m; m &= m - 1) ++c;
+  return c;
+}
+constexpr int dz_low(unsigned m) {
+  int i = 0;
+  while (!((m >> i) & 1u)) ++i;
+  return i;
+}
+
+template <typename R_, bool A, bool B> __device__ __forceinline__ cplx<R_> zadd(cplx<R_> a, cplx<R_> b) {
+  if constexpr (A && B)
+    return cadd<R_>(a, b);
+  else if constexpr (A)
+    return a;
+  else if constexpr (B)
+    return b;
+  else
+    return mk<R_>((R_)0, (R_)0);
+}
+template <typename R_, bool A, bool B> __device__ __forceinline__ cplx<R_> zsub(cplx<R_> a, cplx<R_> b) {
+  if constexpr (A && B)
+    return csub<R_>(a, b);
+  else if constexpr (A)
+    return a;
+  else if constexpr (B)
+    return mk<R_>(-b.x, -b.y);
+  else
+    return mk<R_>((R_)0, (R_)0);
+}
+
+// a * exp(SIGN 2 pi i m / R); the quarter turns are exact moves
+template <typename R_, int R, int SIGN, int M0> __device__ __forceinline__ cplx<R_> turn(cplx<R_> a) {
+  constexpr int m = ((M0 % R) + R) % R;
+  if constexpr (m == 0) {
+    return a;
+  } else if constexpr (4 * m == R) {
+    return mul_si<R_, SIGN>(a);
+  } else if constexpr (2 * m == R) {
+    return mk<R_>(-a.x, -a.y);
+  } else if constexpr (4 * m == 3 * R) {
+    return mul_si<R_, -SIGN>(a);
+  } else {
+    constexpr CosSin w = turn_cs(m, R);
+    return cmul<R_>(a, mk<R_>((R_)w.c, (R_)(SIGN * w.s)));
+  }
+}
+
+template <typename R_, int R, int SIGN, unsigned M> struct DftZPart;
+
+template <typename R_, int R, int SIGN, unsigned M> struct DftZ {
+  __device__ __forceinline__ static void run(cplx<R_> *v) {
+    if constexpr (M == dz_full(R)) {
+      Dft<R_, R, SIGN>::run(v);
+    } else if constexpr (M == 0) {
+      static_for<0, R>([&](auto kc) { v[decltype(kc)::value] = mk<R_>((R_)0, (R_)0); });
+    } else if constexpr (dz_popc(M) == 1) {
+      constexpr int J = dz_low(M);   // X_k = x_J W^{J k}
+      const cplx<R_> x = v[J];
+      static_for<0, R>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        v[k] = turn<R_, R, SIGN, J * k>(x);
+      });
+    } else {
+      DftZPart<R_, R, SIGN, M>::run(v);
+    }
+  }
+};
+
+// two of three inputs (the radix-3 butterfly of Dft<3>)
+template <typename R_, int SIGN, unsigned M> struct DftZPart<R_, 3, SIGN, M> {
+  __device__ __forceinline__ static void run(cplx<R_> *v) {
+    constexpr bool a = dz_bit(M, 0), b = dz_bit(M, 1), c = dz_bit(M, 2);
+    const R_ h = (R_)0.86602540378443864676;  // sqrt(3)/2
+    const cplx<R_> t1 = zadd<R_, b, c>(v[1], v[2]);
+    const cplx<R_> t2 = cscale<R_>(mul_si<R_, SIGN>(zsub<R_, b, c>(v[1], v[2])), h);
+    cplx<R_> m;
+    if constexpr (a)
+      m = mk<R_>(v[0].x - (R_)0.5 * t1.x, v[0].y - (R_)0.5 * t1.y);
+    else
+      m = mk<R_>((R_)-0.5 * t1.x, (R_)-0.5 * t1.y);
+    v[0] = zadd<R_, a, true>(v[0], t1);
+    v[1] = cadd<R_>(m, t2);
+    v[2] = csub<R_>(m, t2);
+  }
+};
+
+// two or three of four inputs (Dft<4>)
+template <typename R_, int SIGN, unsigned M> struct DftZPart<R_, 4, SIGN, M> {
+  __device__ __forceinline__ static void run(cplx<R_> *v) {
+    constexpr bool b0 = dz_bit(M, 0), b1 = dz_bit(M, 1), b2 = dz_bit(M, 2), b3 = dz_bit(M, 3);
+    constexpr bool e = b0 || b2, o = b1 || b3;
+    const cplx<R_> a = zadd<R_, b0, b2>(v[0], v[2]);
+    const cplx<R_> b = zsub<R_, b0, b2>(v[0], v[2]);
+    const cplx<R_> c = zadd<R_, b1, b3>(v[1], v[3]);
+    const cplx<R_> d = mul_si<R_, SIGN>(zsub<R_, b1, b3>(v[1], v[3]));
+    v[0] = zadd<R_, e, o>(a, c);
+    v[2] = zsub<R_, e, o>(a, c);
+    v[1] = zadd<R_, e, o>(b, d);
+    v[3] = zsub<R_, e, o>(b, d);
+  }
+};
+
+// Dft<8>'s even/odd split with the zeros carried into both halves
+template <typename R_, int SIGN, unsigned M> struct DftZPart<R_, 8, SIGN, M> {
+  __device__ __forceinline__ static void run(cplx<R_> *v) {
+    constexpr unsigned me = (M & 1u) | ((M >> 1) & 2u) | ((M >> 2) & 4u) | ((M >> 3) & 8u);
+    constexpr unsigned mo = ((M >> 1) & 1u) | ((M >> 2) & 2u) | ((M >> 3) & 4u) | ((M >> 4) & 8u);
+    constexpr bool E = me != 0, O = mo != 0;
+    cplx<R_> e[4] = {v[0], v[2], v[4], v[6]};
+    cplx<R_> o[4] = {v[1], v[3], v[5], v[7]};
+    DftZ<R_, 4, SIGN, me>::run(e);
+    DftZ<R_, 4, SIGN, mo>::run(o);
+    const R_ r = (R_)0.70710678118654752440;
+    const cplx<R_> w1 = mk<R_>(r, (R_)SIGN * r);
+    const cplx<R_> w3 = mk<R_>(-r, (R_)SIGN * r);
+    const cplx<R_> o1 = cmul<R_>(o[1], w1);
+    const cplx<R_> o2 = mul_si<R_, SIGN>(o[2]);
+    const cplx<R_> o3 = cmul<R_>(o[3], w3);
+    v[0] = zadd<R_, E, O>(e[0], o[0]);
+    v[4] = zsub<R_, E, O>(e[0], o[0]);
+    v[1] = zadd<R_, E, O>(e[1], o1);
+    v[5] = zsub<R_, E, O>(e[1], o1);
+    v[2] = zadd<R_, E, O>(e[2], o2);
+    v[6] = zsub<R_, E, O>(e[2], o2);
+    v[3] = zadd<R_, E, O>(e[3], o3);
+    v[7] = zsub<R_, E, O>(e[3], o3);
+  }
+};
+
+// other lengths: the direct sum over the nonzero inputs (prime R) or
+// DftGen's split R = P Q with the zero inputs and zero sub-transforms left out
+template <typename R_, int R, int SIGN, unsigned M> struct DftZPart {
+  static constexpr int P = smallest_factor(R);
+  static constexpr int Q = R / P;
+  static constexpr unsigned group(int n2) {
+    unsigned g = 0;
+    for (int n1 = 0; n1 < P; ++n1)
+      if (dz_bit(M, Q * n1 + n2)) g |= 1u << n1;
+    return g;
+  }
+  static constexpr unsigned groups() {
+    unsigned g = 0;
+    for (int n2 = 0; n2 < Q; ++n2)
+      if (group(n2)) g |= 1u << n2;
+    return g;
+  }
+  __device__ __forceinline__ static void run(cplx<R_> *v) {
+    if constexpr (P == R) {
+      cplx<R_> out[R];
+      static_for<0, R>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        R_ ax = 0, ay = 0;
+        static_for<0, R>([&](auto jc) {
+          constexpr int j = decltype(jc)::value;
+          if constexpr (dz_bit(M, j)) {
+            constexpr int m = (j * k) % R;
+            const R_ c = (R_)RadixConst<R>::c(m);
+            const R_ s = (R_)(SIGN * RadixConst<R>::s(m));
+            ax += v[j].x * c - v[j].y * s;
+            ay += v[j].x * s + v[j].y * c;
+          }
+        });
+        out[k] = mk<R_>(ax, ay);
+      });
+      static_for<0, R>([&](auto kc) { v[decltype(kc)::value] = out[decltype(kc)::value]; });
+    } else {
+      cplx<R_> y[R];
+      static_for<0, Q>([&](auto n2c) {
+        constexpr int n2 = decltype(n2c)::value;
+        constexpr unsigned G = group(n2);
+        cplx<R_> t[P];
+        static_for<0, P>([&](auto n1c) {
+          constexpr int n1 = decltype(n1c)::value;
+          if constexpr (dz_bit(G, n1))
+            t[n1] = v[Q * n1 + n2];
+          else
+            t[n1] = mk<R_>((R_)0, (R_)0);
+        });
+        DftZ<R_, P, SIGN, G>::run(t);
+        static_for<0, P>([&](auto k1c) {
+          constexpr int k1 = decltype(k1c)::value;
+          constexpr int m = (n2 * k1) % R;
+          if constexpr (m == 0 || G == 0) {
+            y[n2 * P + k1] = t[k1];
+          } else {
+            const cplx<R_> w = mk<R_>((R_)RadixConst<R>::c(m), (R_)(SIGN * RadixConst<R>::s(m)));
+            y[n2 * P + k1] = cmul<R_>(t[k1], w);
+          }
+        });
+      });
+      constexpr unsigned G2 = groups();
+      static_for<0, P>([&](auto k1c) {
+        constexpr int k1 = decltype(k1c)::value;
+        cplx<R_> t[Q];
+        static_for<0, Q>([&](auto n2c) {
+          constexpr int n2 = decltype(n2c)::value;
+          t[n2] = y[n2 * P + k1];
+        });
+        DftZ<R_, Q, SIGN, G2>::run(t);
+        static_for<0, Q>([&](auto k2c) {
+          constexpr int k2 = decltype(k2c)::value;
+          v[k1 + P * k2] = t[k2];
+        });
+      });
+    }
+  }
+};
+
+// Which line positions of a register transform's input may be nonzero:
+// every one (AllKept), or kept(j) of a layout policy (the row bound of a
+// plane, the |mx| bound of an x-line).
+struct AllKept {
+  __host__ __device__ static constexpr bool kept(int) { return true; }
+};
+
 // Split N = A * B (A, B <= 16) for the register transforms: a coprime pair
 // when one exists (prime-factor algorithm, no twiddles), the smaller larger
 // factor first; otherwise the four-step split plan_a (Cooley-Tukey).
@@ -134,45 +360,73 @@ template <int N> __host__ __device__ constexpr int line_slot(int j, int L) {
 //   Prime factor (gcd(A, B) = 1): x[(B n1 + A n2) mod N] and
 //   X[CRT(k1 mod A, k2 mod B)] make the transform a plain A x B 2D DFT:
 //   W_N^{nk} = W_A^{n1 k1} W_B^{n2 k2}, so there are no twiddles.
-template <int N, int SIGN, int L>
+// Z::kept(j) false: input x[j] is zero (its slot is not read).  The step-1
+// transforms skip those inputs, and a step-1 group with no kept input
+// yields zeros that step 2 leaves out in turn.
+template <int N, class Z> __host__ __device__ constexpr unsigned step1_mask(int n2) {
+  using S = LineSplit<N>;
+  unsigned m = 0;
+  for (int n1 = 0; n1 < S::A; ++n1)
+    if (Z::kept(S::in_index(n1, n2))) m |= 1u << n1;
+  return m;
+}
+template <int N, class Z> __host__ __device__ constexpr unsigned step2_mask() {
+  using S = LineSplit<N>;
+  unsigned m = 0;
+  for (int n2 = 0; n2 < S::B; ++n2)
+    if (step1_mask<N, Z>(n2)) m |= 1u << n2;
+  return m;
+}
+
+template <int N, int SIGN, int L, class Z = AllKept>
 __device__ __forceinline__ void reg_fft(float2 (&v)[N]) {
   using S = LineSplit<N>;
   constexpr int A = S::A;
   constexpr int B = S::B;
   static_for<0, B>([&](auto n2c) {
     constexpr int n2 = decltype(n2c)::value;
-    float2 t[A];
-    static_for<0, A>([&](auto n1c) {
-      constexpr int n1 = decltype(n1c)::value;
-      t[n1] = v[line_slot<N>(S::in_index(n1, n2), L)];
-    });
-    Dft<float, A, SIGN>::run(t);
-    if constexpr (!S::PFA) {
-      static_for<1, A>([&](auto k1c) {
+    constexpr unsigned M1 = step1_mask<N, Z>(n2);
+    if constexpr (M1 != 0) {
+      float2 t[A];
+      static_for<0, A>([&](auto n1c) {
+        constexpr int n1 = decltype(n1c)::value;
+        if constexpr (dz_bit(M1, n1))
+          t[n1] = v[line_slot<N>(S::in_index(n1, n2), L)];
+        else
+          t[n1] = make_float2(0.f, 0.f);
+      });
+      DftZ<float, A, SIGN, M1>::run(t);
+      if constexpr (!S::PFA) {
+        static_for<1, A>([&](auto k1c) {
+          constexpr int k1 = decltype(k1c)::value;
+          constexpr int m = (n2 * k1) % N;
+          if constexpr (m != 0) {
+            constexpr CosSin w = turn_cs(m, N);
+            constexpr float wc = (float)w.c;
+            constexpr float ws = (float)(SIGN * w.s);
+            const float2 a = t[k1];
+            t[k1] = make_float2(a.x * wc - a.y * ws, a.x * ws + a.y * wc);
+          }
+        });
+      }
+      static_for<0, A>([&](auto k1c) {
         constexpr int k1 = decltype(k1c)::value;
-        constexpr int m = (n2 * k1) % N;
-        if constexpr (m != 0) {
-          constexpr CosSin w = turn_cs(m, N);
-          constexpr float wc = (float)w.c;
-          constexpr float ws = (float)(SIGN * w.s);
-          const float2 a = t[k1];
-          t[k1] = make_float2(a.x * wc - a.y * ws, a.x * ws + a.y * wc);
-        }
+        v[line_slot<N>(S::in_index(k1, n2), L)] = t[k1];
       });
     }
-    static_for<0, A>([&](auto k1c) {
-      constexpr int k1 = decltype(k1c)::value;
-      v[line_slot<N>(S::in_index(k1, n2), L)] = t[k1];
-    });
   });
+  constexpr unsigned M2 = step2_mask<N, Z>();
   static_for<0, A>([&](auto k1c) {
     constexpr int k1 = decltype(k1c)::value;
     float2 t[B];
     static_for<0, B>([&](auto n2c) {
       constexpr int n2 = decltype(n2c)::value;
-      t[n2] = v[line_slot<N>(S::in_index(k1, n2), L)];
+      if constexpr (dz_bit(M2, n2))
+        t[n2] = v[line_slot<N>(S::in_index(k1, n2), L)];
+      else
+        t[n2] = make_float2(0.f, 0.f);
     });
-    Dft<float, B, SIGN>::run(t);
+    DftZ<float, B, SIGN, M2>::run(t);
     static_for<0, B>([&](auto k2c) {
       constexpr int k2 = decltype(k2c)::value;
       v[line_slot<N>(S::in_index(k1, k2), L)] = t[k2];
