@@ -5,10 +5,11 @@
 // (column order, see the per-k-set tables), so a thread knows the entry of
 // line position j from the run's first entry, its length and the centred x
 // of its first entry (col_x0): entry = first + (mx(j) - x0) when that lies in
-// the run.  Each thread therefore loads (x_inv) or updates (x_fwd) its
-// column's entries straight from or into its registers, one predicated
-// access per possible line position, with no shared-memory staging and no
-// block barrier: a thread keeps tens of independent loads in flight.
+// the run.  x_inv loads its column's entries straight into its registers,
+// one predicated access per possible line position, with no shared-memory
+// staging and no block barrier: a thread keeps tens of independent loads in
+// flight.  x_fwd writes its run's transformed values into shared memory and
+// the block then walks its contiguous range of entries coalesced.
 // Line positions with |mx| > RX hold no entry of any column (host check on
 // the largest |Miller index| of the spheres); they are compile-time zeros.
 //   x_inv: load the column's entries, backward x transform, write the line
@@ -77,37 +78,63 @@ __global__ void __launch_bounds__(kXThreads, 3) k_xinv_reg(Tables t, int item_be
   });
 }
 
+// x_fwd: the block's 128 columns own one contiguous range [E0, E1) of the
+// sphere's entries.  Each thread transforms its column and writes its run's
+// values (already scaled by 1/N) into shared memory at their entry offsets;
+// after one barrier the block walks [E0, E1) with consecutive threads on
+// consecutive entries, so the epilogue's loads of psi, prev and the kinetic
+// energies and its store of out are coalesced (a thread's own run would make
+// every warp access touch up to 32 cache lines).
 template <int N, int RX>
 __global__ void __launch_bounds__(kXThreads, 3) k_xfwd_reg(Tables t, int item_begin, const float2 *__restrict__ abuf,
                                                            const float2 *__restrict__ psi,
                                                            const float2 *__restrict__ prev,
                                                            float2 *__restrict__ out,
                                                            const Axpby *__restrict__ coef) {
+  extern __shared__ __align__(16) float2 run_vals[];   // kXThreads * (2 RX + 1)
   const int item = t.item_list ? t.item_list[blockIdx.x] : item_begin + blockIdx.x;
   const int ksi = t.item_ks[item];
   const KSetDev &K = t.ks[ksi];
-  const int c = blockIdx.y * kXThreads + threadIdx.x;
-  if (c >= K.ncol) return;   // no barriers below: threads leave independently
+  const int c0 = blockIdx.y * kXThreads;
+  if (c0 >= K.ncol) return;   // uniform: the whole block leaves
   const SysDev &S = t.sys[K.sys];
-  if (!S.active) return;
+  if (!S.active) return;      // uniform
   const int b = t.item_band[item];
   const long long ld = K.ncol_pad;
   const int *cs = t.col_start + K.col_off;
-  const int e0 = cs[c], cnt = cs[c + 1] - e0, x0 = t.col_x0[K.col_off + c];
-  const long long off = K.psi_off + (long long)b * K.npw_pad + e0;
-  const float *kin = t.kin32 + K.ent_off + e0;
-  // the epilogue's runs into L2 while the x-line loads and the transform run
-  prefetch_l2(psi + off, cnt * (int)sizeof(float2));
-  if (prev) prefetch_l2(prev + off, cnt * (int)sizeof(float2));
-  prefetch_l2(kin, cnt * (int)sizeof(float));
-  const float2 *src = abuf + K.a_off + (long long)b * N * ld + c;
-  float2 v[N];
-  static_for<0, N>([&](auto jc) {
-    constexpr int j = decltype(jc)::value;
-    v[j] = src[j * ld];
-  });
-  reg_fft<N, -1, 0>(v);
-  const float inv_n = 1.0f / (float)S.nr;
+  const int cend = min(K.ncol, c0 + kXThreads);
+  const int E0 = cs[c0], E1 = cs[cend];
+  const long long row = K.psi_off + (long long)b * K.npw_pad;
+  const float *kin = t.kin32 + K.ent_off;
+  if (threadIdx.x == 0) {
+    // the epilogue's ranges into L2 while the x-line loads and the transform run
+    prefetch_l2(psi + row + E0, (E1 - E0) * (int)sizeof(float2));
+    if (prev) prefetch_l2(prev + row + E0, (E1 - E0) * (int)sizeof(float2));
+    prefetch_l2(kin + E0, (E1 - E0) * (int)sizeof(float));
+  }
+  const int c = c0 + threadIdx.x;
+  if (c < cend) {
+    const int e0 = cs[c], cnt = cs[c + 1] - e0, x0 = t.col_x0[K.col_off + c];
+    const float2 *src = abuf + K.a_off + (long long)b * N * ld + c;
+    float2 v[N];
+    static_for<0, N>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      v[j] = src[j * ld];
+    });
+    reg_fft<N, -1, 0>(v);
+    const float inv_n = 1.0f / (float)S.nr;
+    float2 *dst = run_vals + (e0 - E0);
+    static_for<0, N>([&](auto mc) {
+      constexpr int m = decltype(mc)::value;
+      if constexpr (x_kept<N, RX>(m)) {
+        const int d = mx_of<N>(m) - x0;
+        if ((unsigned)d < (unsigned)cnt) {
+          const float2 f = v[line_slot<N>(m, 1)];
+          dst[d] = make_float2(f.x * inv_n, f.y * inv_n);
+        }
+      }
+    });
+  }
   float al = 1, be = 0, ga = 0, tk = 1;
   if (coef) {
     al = (float)coef[ksi].alpha;
@@ -116,27 +143,22 @@ __global__ void __launch_bounds__(kXThreads, 3) k_xfwd_reg(Tables t, int item_be
     tk = (float)coef[ksi].tk;
   }
   if (t.item_shift) be += (float)t.item_shift[item];
-  static_for<0, N>([&](auto mc) {
-    constexpr int m = decltype(mc)::value;
-    if constexpr (x_kept<N, RX>(m)) {
-      const int d = mx_of<N>(m) - x0;
-      if ((unsigned)d < (unsigned)cnt) {
-        const float2 p = psi[off + d];
-        const float2 f = v[line_slot<N>(m, 1)];
-        const float k = tk * kin[d];
-        const float hx = f.x * inv_n + k * p.x;
-        const float hy = f.y * inv_n + k * p.y;
-        float ox = al * hx + be * p.x;
-        float oy = al * hy + be * p.y;
-        if (prev) {
-          const float2 q = prev[off + d];
-          ox += ga * q.x;
-          oy += ga * q.y;
-        }
-        out[off + d] = make_float2(ox, oy);
-      }
+  __syncthreads();
+  for (int e = E0 + threadIdx.x; e < E1; e += kXThreads) {
+    const float2 p = psi[row + e];
+    const float2 f = run_vals[e - E0];
+    const float k = tk * kin[e];
+    const float hx = f.x + k * p.x;
+    const float hy = f.y + k * p.y;
+    float ox = al * hx + be * p.x;
+    float oy = al * hy + be * p.y;
+    if (prev) {
+      const float2 q = prev[row + e];
+      ox += ga * q.x;
+      oy += ga * q.y;
     }
-  });
+    out[row + e] = make_float2(ox, oy);
+  }
 }
 
 // |Miller x| bounds of the compact and tight kernels (as the planes' row
@@ -155,7 +177,11 @@ template <int N, int RX>
 static void xfwd_go(const Tables &t, int item_begin, int nitems, int max_ncol, const float2 *abuf,
                     const float2 *psi, const float2 *prev, float2 *out, const Axpby *coef, cudaStream_t st) {
   const int nchunk = (max_ncol + kXThreads - 1) / kXThreads;
-  derek::note_launch(), k_xfwd_reg<N, RX><<<dim3(nitems, nchunk), kXThreads, 0, st>>>(t, item_begin, abuf, psi, prev, out, coef);
+  // every column of a block holds at most 2 RX + 1 entries (|mx| <= RX)
+  const int smem = kXThreads * (2 * RX + 1) * (int)sizeof(float2);
+  auto kern = k_xfwd_reg<N, RX>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  derek::note_launch(), kern<<<dim3(nitems, nchunk), kXThreads, smem, st>>>(t, item_begin, abuf, psi, prev, out, coef);
 }
 
 template <int N>
