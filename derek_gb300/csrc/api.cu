@@ -288,7 +288,7 @@ void derek_gpu_default_opts(derek_scf_opts *o) {
   o->first_degree = 10;
   o->seed = 20240101ULL;
   o->use_graph = 1;
-  o->use_tensor_cores = 2;
+  o->use_tensor_cores = -1;
   o->density_tol = 0.0;
   o->buffer_bands = -1;
   o->etol_per_electron = 0;

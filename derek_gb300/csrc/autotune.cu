@@ -457,12 +457,7 @@ struct Tuner {
   }
 
   // Tensor cores for the subspace products only where the subspace has at
-  // least kTcMinBands bands.  The split-BF16 products carry ~2^-17 relative
-  // error per term; on the uneven batch (at most 44 bands) the CUDA-core
-  // paths kept 251 of 256 systems within 1e-6 Ha/e of the FP64 path against
-  // 241 with tensor cores, for 7 % more time (measured); at kpts64's 84
-  // bands the tensor cores are faster and within 2.5e-7 Ha/e.
-  static constexpr int kTcMinBands = 64;
+  // least kTcMinBands carried bands (handle.h: the split-BF16 accuracy)
   bool tc_allowed() const { return tc_capable(h) && h->max_nb_band >= kTcMinBands; }
 
   int overlap() {
@@ -496,7 +491,7 @@ struct Tuner {
   }
 
   int rotate() {
-    if (!(tc_capable(h) && h->opts.use_tensor_cores >= 2)) return DEREK_OK;
+    if (!(tc_capable(h) && h->opts.use_tensor_cores != 1)) return DEREK_OK;
     const std::string key = shape_key("rotate");
     if (!tc_allowed()) {   // a rule, not a timing: nothing to cache
       h->tune.rotate_tc = 0;

@@ -190,6 +190,15 @@ bool reject_spinor(derek_gpu *h, const char *what);
 // Subspace pieces of the SCF (scf.cu) the autotuner times: tensor-core
 // availability and choice, overlaps S = A^H B and rotations X <- X C over all
 // k-sets, with the handle's tuned split and paths.
+// Smallest subspace (carried bands per k-set) that the default
+// use_tensor_cores = -1 and the autotuner give the tensor cores.  The
+// split-BF16 products carry ~2^-16 relative error per element of a rotated
+// band: on a 12-band subspace (8 electrons) that left the SCF's free energy
+// moving by ~4e-6 Ha per iteration after 200 iterations (measured), and on the
+// uneven batch (at most 44 bands) the CUDA-core paths kept 251 of 256
+// systems within 1e-6 Ha/e of the FP64 path against 241 with tensor cores;
+// at kpts64's 84 bands the tensor cores are faster and within 2.5e-7 Ha/e.
+constexpr int kTcMinBands = 64;
 bool tc_capable(const derek_gpu *h);
 bool use_tc_overlap(const derek_gpu *h);
 bool use_tc_rotate(const derek_gpu *h);

@@ -32,15 +32,19 @@ template <typename T> cudaError_t dalloc(T **p, size_t n) {
 namespace derek {
 
 // the tensor-core kernels serve complex64 scalar bands, nb <= 128, when the
-// options allow them (use_tensor_cores 1: overlaps, 2: overlaps and rotations)
+// options allow them: use_tensor_cores 1 (overlaps) or 2 (overlaps and
+// rotations) at any subspace size, -1 (the default) overlaps and rotations
+// for subspaces of kTcMinBands or more carried bands
 bool tc_capable(const derek_gpu *h) {
-  return h->prec == DEREK_PREC_MIXED && h->opts.use_tensor_cores && h->max_nb <= kMaxBands && !h->any_spinor;
+  if (h->prec != DEREK_PREC_MIXED || !h->opts.use_tensor_cores || h->max_nb > kMaxBands || h->any_spinor)
+    return false;
+  return h->opts.use_tensor_cores > 0 || h->max_nb_band >= kTcMinBands;
 }
 bool use_tc_overlap(const derek_gpu *h) {
   return tc_capable(h) && (h->tune.overlap_tc >= 0 ? h->tune.overlap_tc == 1 : true);
 }
 bool use_tc_rotate(const derek_gpu *h) {
-  return tc_capable(h) && h->opts.use_tensor_cores >= 2 &&
+  return tc_capable(h) && h->opts.use_tensor_cores != 1 &&
          (h->tune.rotate_tc >= 0 ? h->tune.rotate_tc == 1 : true);
 }
 

@@ -95,9 +95,11 @@ typedef struct {
   int    first_degree;     /* filter degree of those passes */
   uint64_t seed;           /* start-vector hash seed */
   int    use_graph;        /* capture each SCF iteration in a CUDA graph */
-  int    use_tensor_cores; /* mixed mode: 2 = tcgen05 split-BF16 overlaps and
-                              rotations (default), 1 = overlaps only,
-                              0 = CUDA cores */
+  int    use_tensor_cores; /* mixed mode: -1 (default) = tcgen05 split-BF16
+                              overlaps and rotations for subspaces of 64
+                              or more carried bands, CUDA cores below;
+                              2 = tensor-core overlaps and rotations, 1 =
+                              overlaps only, at any size; 0 = CUDA cores */
   double density_tol;      /* also require max|n_out - n_in| < density_tol
                               (0 = energy criterion only, as the reference) */
   int    buffer_bands;     /* extra unreported bands carried by the filtered
