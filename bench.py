@@ -190,8 +190,8 @@ class Clocks:
 
 # DRAM bytes per (k-point, band) item of one H.psi, summed over k_xinv_reg,
 # k_plane_persist and k_xfwd_reg, from one ncu capture of the 4-k-point case
-# (336 items: 144.8 + 256.5 + 239.0 MB).
-TRAFFIC_PER_ITEM = 640.3e6 / 336
+# (336 items: 143.5 + 256.3 + 235.8 MB).
+TRAFFIC_PER_ITEM = 635.6e6 / 336
 # nominal FP32 rate of a GB300: 152 SMs x 128 lanes x 2 flops x 2.07 GHz
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
