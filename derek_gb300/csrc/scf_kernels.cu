@@ -147,20 +147,49 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
   }
   if (threadIdx.x == 0) {
     s_hi = red[0] + 40.0 * kT + 1.0;
-    s_mu = 0.5 * (s_lo + s_hi);
+    // from the previous SCF iteration's Fermi level when there is one (the
+    // state is reset at SCF start, so every run takes the same path)
+    const double prev = st[s].mu;
+    s_mu = st[s].iter > 0 && prev > s_lo && prev < s_hi ? prev : 0.5 * (s_lo + s_hi);
     s_done = 0;
+  }
+  // each thread's eigenvalues and weights in registers (up to kOccReg per
+  // thread), read once instead of once per Newton step
+  constexpr int kOccReg = 6;
+  const bool in_reg = ntot <= kOccReg * (int)blockDim.x;
+  double er[kOccReg], wr[kOccReg];
+#pragma unroll
+  for (int q = 0; q < kOccReg; ++q) {
+    const int i = threadIdx.x + q * (int)blockDim.x;
+    er[q] = 0.0;
+    wr[q] = 0.0;   // no contribution from slots past ntot
+    if (in_reg && i < ntot) {
+      const KSetDev &K = t.ks[S.ks0 + i / nb];
+      er[q] = eig[K.item0 + i % nb];
+      wr[q] = K.wk * g;
+    }
   }
   __syncthreads();
   // safeguarded Newton on N(mu) - Ne
   for (int it = 0; it < 200; ++it) {
     const double mu = s_mu;
     double cnt = 0, der = 0;
-    for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
-      const KSetDev &K = t.ks[S.ks0 + i / nb];
-      const double x = fmin(fmax((eig[K.item0 + i % nb] - mu) / kT, -200.0), 200.0);
-      const double f = 1.0 / (1.0 + exp(x));
-      cnt += K.wk * g * f;
-      der += K.wk * g * f * (1.0 - f) / kT;
+    if (in_reg) {
+#pragma unroll
+      for (int q = 0; q < kOccReg; ++q) {
+        const double x = fmin(fmax((er[q] - mu) / kT, -200.0), 200.0);
+        const double f = 1.0 / (1.0 + exp(x));
+        cnt += wr[q] * f;
+        der += wr[q] * f * (1.0 - f) / kT;
+      }
+    } else {
+      for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
+        const KSetDev &K = t.ks[S.ks0 + i / nb];
+        const double x = fmin(fmax((eig[K.item0 + i % nb] - mu) / kT, -200.0), 200.0);
+        const double f = 1.0 / (1.0 + exp(x));
+        cnt += K.wk * g * f;
+        der += K.wk * g * f * (1.0 - f) / kT;
+      }
     }
     cnt = block_sum(cnt, red);
     der = block_sum(der, red);
