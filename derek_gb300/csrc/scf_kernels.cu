@@ -157,13 +157,15 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
   // thread), read once instead of once per Newton step
   constexpr int kOccReg = 6;
   const bool in_reg = ntot <= kOccReg * (int)blockDim.x;
+  // slots of this thread: i = threadIdx.x + q blockDim.x < ntot for q < nq
+  const int nq = (int)threadIdx.x < ntot ? (ntot - 1 - (int)threadIdx.x) / (int)blockDim.x + 1 : 0;
   double er[kOccReg], wr[kOccReg];
 #pragma unroll
   for (int q = 0; q < kOccReg; ++q) {
     const int i = threadIdx.x + q * (int)blockDim.x;
     er[q] = 0.0;
-    wr[q] = 0.0;   // no contribution from slots past ntot
-    if (in_reg && i < ntot) {
+    wr[q] = 0.0;
+    if (in_reg && q < nq) {
       const KSetDev &K = t.ks[S.ks0 + i / nb];
       er[q] = eig[K.item0 + i % nb];
       wr[q] = K.wk * g;
@@ -177,10 +179,12 @@ __global__ void __launch_bounds__(1024) k_occupations(const Tables t, const doub
     if (in_reg) {
 #pragma unroll
       for (int q = 0; q < kOccReg; ++q) {
-        const double x = fmin(fmax((er[q] - mu) / kT, -200.0), 200.0);
-        const double f = 1.0 / (1.0 + exp(x));
-        cnt += wr[q] * f;
-        der += wr[q] * f * (1.0 - f) / kT;
+        if (q < nq) {
+          const double x = fmin(fmax((er[q] - mu) / kT, -200.0), 200.0);
+          const double f = 1.0 / (1.0 + exp(x));
+          cnt += wr[q] * f;
+          der += wr[q] * f * (1.0 - f) / kT;
+        }
       }
     } else {
       for (int i = threadIdx.x; i < ntot; i += blockDim.x) {
