@@ -82,11 +82,8 @@ int rotate_all(derek_gpu *h, void *X, const double2 *C) {
 
 namespace {
 
-// orthonormalise buf(cur) and do Rayleigh-Ritz; leaves Ritz values in d_eig.
-// scf: inside an SCF, where the Jacobi target follows each system's state
-// (loose while the density is far from self-consistent); the frozen-potential
-// solve keeps the fixed target.
-int cholqr_rr(derek_gpu *h, bool scf) {
+// orthonormalise buf(cur) and do Rayleigh-Ritz; leaves Ritz values in d_eig
+int cholqr_rr(derek_gpu *h) {
   void *X = h->cur_psi();
   overlap_all(h, X, X, h->d_S, 1);
   launch_cholesky_inv(h->tab_band, 0, h->nks, h->max_nb_band, h->d_S, h->d_C, h->d_mat_off, h->d_scratch,
@@ -101,8 +98,7 @@ int cholqr_rr(derek_gpu *h, bool scf) {
   // saving about one of the four sweeps near convergence.
   const double jtol = h->prec == DEREK_PREC_FP64 ? 1e-14 : 1e-10;
   launch_jacobi(h->tab_band, 0, h->nks, h->max_nb_band, h->d_Hs, h->d_C, h->d_mat_off, h->d_eig,
-                h->d_scratch, 30, jtol, 0, h->d_sweeps, h->stream, h->tune.jacobi_single,
-                scf ? h->d_state : nullptr);
+                h->d_scratch, 30, jtol, 0, h->d_sweeps, h->stream, h->tune.jacobi_single);
   rotate_all(h, X, h->d_C);
   return DEREK_OK;
 }
@@ -122,10 +118,10 @@ int filter(derek_gpu *h, int m) {
   return DEREK_OK;
 }
 
-int subspace_step(derek_gpu *h, int m, bool scf) {
+int subspace_step(derek_gpu *h, int m) {
   int st = filter(h, m);
   if (st) return st;
-  return cholqr_rr(h, scf);
+  return cholqr_rr(h);
 }
 
 // the non-collinear SCF's grids (on = 0 for scalar batches)
@@ -267,10 +263,10 @@ int scf_start(derek_gpu *h, double etol) {
                    h->d_epart, h->d_state, 1, sg, h->stream);
   int s = start_vectors(h);
   if (s) return s;
-  s = cholqr_rr(h, true);
+  s = cholqr_rr(h);
   if (s) return s;
   for (int p = 0; p < h->opts.first_passes; ++p) {
-    s = subspace_step(h, h->opts.first_degree, true);
+    s = subspace_step(h, h->opts.first_degree);
     if (s) return s;
   }
   h->scf_started = true;
@@ -280,7 +276,7 @@ int scf_start(derek_gpu *h, double etol) {
 int steady_iteration(derek_gpu *h) {
   const int m = h->opts.cheb_degree;
   if (!h->opts.use_graph) {
-    int s = subspace_step(h, m, true);
+    int s = subspace_step(h, m);
     if (s) return s;
     return finish_iteration(h);
   }
@@ -297,7 +293,7 @@ int steady_iteration(derek_gpu *h) {
     cudaGraph_t g = nullptr;
     const unsigned long long before = launch_total();
     DEREK_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int s = subspace_step(h, m, true);
+    int s = subspace_step(h, m);
     if (!s) s = finish_iteration(h);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     // captured launches run only when the graph is replayed
@@ -550,7 +546,7 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, 
   DEREK_CUDA(h, cudaMemsetAsync(h->d_status, 0, h->nks * sizeof(int), h->stream));
   int s = start_vectors(h);
   if (s) return s;
-  s = cholqr_rr(h, false);
+  s = cholqr_rr(h);
   if (s) return s;
   // the lowest nconv reported bands of every k-set (0: all reported): a band
   // close below the subspace's top converges slowly under the filter, whose
@@ -568,7 +564,7 @@ int derek_gpu_nscf_run(derek_gpu_t *h, int max_iter, double eig_tol, int nconv, 
   double last = -1.0;   // largest change of the last iteration
   int last_ks = -1, last_b = -1;
   for (; it < max_iter; ++it) {
-    s = subspace_step(h, h->opts.cheb_degree, false);
+    s = subspace_step(h, h->opts.cheb_degree);
     if (s) return s;
     DEREK_CUDA(h, cudaMemcpyAsync(eig.data(), h->d_eig, eig.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                   h->stream));

@@ -296,21 +296,6 @@ __device__ __forceinline__ void rr_pair(int k, int r, int ne, int &p, int &q) {
   q = max(a, b);
 }
 
-// Off-diagonal target of a Jacobi solve inside an SCF (adapt != nullptr):
-// 1e-6 relative before the first density (the Ritz vectors of a start or
-// first-pass subspace are far from the fixed point), then 1e-4 x the last
-// iteration's max|n_out - n_in|, between the caller's tight target and 1e-6.
-// A loose solve leaves the subspace itself unchanged: its Ritz values carry
-// the square of the off-diagonal error and its vectors mix within the
-// subspace at that level, far below the density error of that iteration.
-__device__ __forceinline__ double jacobi_tol(const SysState *adapt, int sys, double tight) {
-  if (!adapt) return tight;
-  constexpr double loose = 1e-6;
-  const SysState &x = adapt[sys];
-  if (x.iter == 0) return fmax(tight, loose);
-  return fmin(fmax(tight, 1e-4 * x.resid), fmax(tight, loose));
-}
-
 template <typename VT>
 __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
                                                 const double2 *__restrict__ Hs,
@@ -318,15 +303,13 @@ __global__ void __launch_bounds__(256) k_jacobi(const Tables t, int ks_begin,
                                                 const long long *__restrict__ mat_off,
                                                 double *__restrict__ eig,
                                                 double2 *__restrict__ scratch, int max_sweeps,
-                                                double tol_tight, int a_in_smem, int v_in_smem,
-                                                int *__restrict__ sweeps_out,
-                                                const SysState *__restrict__ adapt) {
+                                                double tol, int a_in_smem, int v_in_smem,
+                                                int *__restrict__ sweeps_out) {
   using V2 = cplx<VT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ksi = ks_begin + blockIdx.x;
   const KSetDev &K = t.ks[ksi];
   if (!t.sys[K.sys].active) return;
-  const double tol = jacobi_tol(adapt, K.sys, tol_tight);
   const int n = K.nb;
   const int ne = n + (n & 1);  // even count for the tournament; index n is a dummy
   const int np = ne / 2;
@@ -518,8 +501,7 @@ template <typename VT>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
     k_jacobi_pair(const Tables t, int ks_begin, const double2 *__restrict__ Hs,
                   double2 *__restrict__ Cout, const long long *__restrict__ mat_off,
-                  double *__restrict__ eig, int max_sweeps, double tol_tight, int *__restrict__ sweeps_out,
-                  const SysState *__restrict__ adapt) {
+                  double *__restrict__ eig, int max_sweeps, double tol, int *__restrict__ sweeps_out) {
   using V2 = cplx<VT>;
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
@@ -528,7 +510,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
   const int ksi = ks_begin + blockIdx.x / 2;
   const KSetDev &K = t.ks[ksi];
   if (!t.sys[K.sys].active) return;   // both CTAs of the cluster leave together
-  const double tol = jacobi_tol(adapt, K.sys, tol_tight);   // both CTAs read the same state
   const int n = K.nb;
   const int ne = n + (n & 1);
   const int np = ne / 2;
@@ -758,7 +739,7 @@ constexpr size_t kJacobiSmem = 227 * 1024 - 4096;   // static reduction arrays t
 void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
                    double2 *C, const long long *mat_off, double *eig, double2 *scratch,
                    int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st,
-                   int single, const SysState *adapt) {
+                   int single) {
   if (nks <= 0) return;
   const size_t nn = (size_t)max_nb * max_nb;
   const size_t tab = jacobi_tables(max_nb);
@@ -774,22 +755,22 @@ void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const dou
     if (fp32_vectors) {
       cudaFuncSetAttribute(k_jacobi_pair<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pair);
       derek::note_launch(), k_jacobi_pair<float><<<2 * nks, 256, sm_pair, st>>>(t, ks_begin, Hs, C, mat_off, eig,
-                                                                             max_sweeps, tol, sweeps_out, adapt);
+                                                                             max_sweeps, tol, sweeps_out);
     } else {
       cudaFuncSetAttribute(k_jacobi_pair<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pair);
       derek::note_launch(), k_jacobi_pair<double><<<2 * nks, 256, sm_pair, st>>>(t, ks_begin, Hs, C, mat_off, eig,
-                                                                              max_sweeps, tol, sweeps_out, adapt);
+                                                                              max_sweeps, tol, sweeps_out);
     }
     return;
   }
   if (fp32_vectors) {
     cudaFuncSetAttribute(k_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     derek::note_launch(), k_jacobi<float><<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps,
-                                                                tol, a_smem, v_smem, sweeps_out, adapt);
+                                                                tol, a_smem, v_smem, sweeps_out);
   } else {
     cudaFuncSetAttribute(k_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     derek::note_launch(), k_jacobi<double><<<nks, 256, sm, st>>>(t, ks_begin, Hs, C, mat_off, eig, scratch, max_sweeps,
-                                                                 tol, a_smem, v_smem, sweeps_out, adapt);
+                                                                 tol, a_smem, v_smem, sweeps_out);
   }
 }
 

@@ -41,7 +41,10 @@ void launch_cholesky_inv(const Tables &t, int ks_begin, int nks, int max_nb, con
                          cudaStream_t st);
 // fp32_vectors: accumulate the eigenvectors in FP32 (A stays FP64); single:
 // one CTA per k-set even where the two-CTA cluster kernel fits
-
+void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
+                   double2 *C, const long long *mat_off, double *eig, double2 *scratch,
+                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st,
+                   int single = 0);
 
 // Per-system SCF scalars kept on the device.
 constexpr int kMaxHist = 16;
@@ -60,14 +63,5 @@ struct SysState {
   double gram[kMaxHist * kMaxHist];
   double coef[kMaxHist];
 };
-
-// Jacobi eigensolve of each k-set's Hs (off-diagonal target tol relative to
-// ||Hs||_F).  adapt != nullptr (inside an SCF): the target follows the
-// system's SCF state, loose (1e-6) before the first density and 1e-4 x the
-// last density residual after it, never tighter than tol.
-void launch_jacobi(const Tables &t, int ks_begin, int nks, int max_nb, const double2 *Hs,
-                   double2 *C, const long long *mat_off, double *eig, double2 *scratch,
-                   int max_sweeps, double tol, int fp32_vectors, int *sweeps_out, cudaStream_t st,
-                   int single = 0, const SysState *adapt = nullptr);
 
 }  // namespace derek
