@@ -8,7 +8,9 @@
 // with g = 2 (n - n_target), iterated with Anderson mixing.  chi0 of the
 // smeared (metallic) ground state is written as density-functional
 // perturbation theory for metals (S. de Gironcoli, Phys. Rev. B 51, 6773
-// (1995)) split at the filtered subspace M of nb bands:
+// (1995)) split at a subspace M of each k-set: its leading bands that are
+// converged eigenvectors (Ritz residual below kRitzConv), and at least every
+// band with occupation above 1e-12:
 //   dn = sum_k w_k/Omega [ sum_{n,m in M} w_nm psi_n^* psi_m V_mn
 //                        + sum_n 2 f_n Re psi_n^* x_n ]  - dmu n_F,
 //   w_nm = (f_n - f_m)/(e_n - e_m) (f'_n when degenerate), V_mn = <m|dV|n>,
@@ -17,6 +19,7 @@
 //   dmu = sum w_k f'_n V_nn / sum w_k f'_n,  n_F = sum w_k/Omega f'_n |psi_n|^2.
 // The real cross density Re psi^* xi is formed as (|psi + xi|^2 - |psi - xi|^2)/4
 // with the density kernels.  FP64 path only.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -268,24 +271,70 @@ extern "C" int derek_gpu_grad_density_loss(derek_gpu_t *h, int s, const double *
   CKA(cudaMemcpyAsync(W.g, g.data(), nr * sizeof(double), cudaMemcpyHostToDevice, st));
   launch_fxc(nr, h->d_rho_out + S.grid_off, W.fxc, st);
 
-  // item weights
+  // The split subspace M of each k-set: its leading bands whose Ritz
+  // residual |(H - e_m) psi_m| is below kRitzConv, and at least every band
+  // with occupation above 1e-12.  The pair sum over M and the Sternheimer
+  // solve on its complement add up to the exact response only when M is an
+  // invariant subspace; the top carried bands of an SCF are not converged
+  // eigenvectors, so they go to the complement, where the Sternheimer solve
+  // treats them with H itself.
+  std::vector<double> shift(ni);
+  for (int it = 0; it < ni; ++it) shift[it] = -eig[it];
+  CKA(cudaMemcpyAsync(W.shift, shift.data(), ni * sizeof(double), cudaMemcpyHostToDevice, st));
+  std::vector<double> rres(ni);
+  {
+    Tables ts = t;
+    ts.item_shift = W.shift;
+    int e0 = apply_h_items_ex(h, ts, 0, ni, psi, nullptr, W.ap, nullptr, h->d_vloc);
+    if (e0) return e0;
+    derek::note_launch(), k_item_dot<<<ni, 256, 0, st>>>(t, W.ap, W.ap, W.pap);
+    CKA(cudaMemcpyAsync(rres.data(), W.pap, ni * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CKA(cudaStreamSynchronize(st));
+  }
+  constexpr double kRitzConv = 1e-7;
+  std::vector<int> nsplit(h->nks, 0);
+  {
+    std::vector<int> lead(h->nks, 0), last_occ(h->nks, -1);
+    std::vector<char> broken(h->nks, 0);
+    for (int it = 0; it < ni; ++it) {
+      const int ksi = h->item_ks[it], b = h->item_band[it];
+      if (!broken[ksi] && std::sqrt(rres[it]) < kRitzConv && b == lead[ksi]) ++lead[ksi];
+      else if (b == lead[ksi]) broken[ksi] = 1;
+      if (occ[it] > 1e-12) last_occ[ksi] = std::max(last_occ[ksi], b);
+    }
+    for (int k = 0; k < h->nks; ++k) nsplit[k] = std::max({lead[k], last_occ[k] + 1, 1});
+  }
+  std::vector<KSetDev> ks_split(h->ks);
+  for (int k = 0; k < h->nks; ++k) ks_split[k].nb = nsplit[k];
+  KSetDev *d_ks_split = nullptr;
+  CKA(dmalloc(&d_ks_split, ks_split.size()));
+  struct FreeKs {
+    KSetDev *p;
+    ~FreeKs() {
+      if (p) cudaFree(p);
+    }
+  } free_ks{d_ks_split};
+  CKA(cudaMemcpyAsync(d_ks_split, ks_split.data(), ks_split.size() * sizeof(KSetDev), cudaMemcpyHostToDevice, st));
+  Tables tM = t;   // the split subspace: k-set tables with nb = |M|
+  tM.ks = d_ks_split;
+
+  // item weights (bands outside M take no pair or Sternheimer term)
   const double kT = S.kT;
-  std::vector<double> w_pair(ni), w_stern(ni), w_fermi(ni), mask(ni), shift(ni);
+  std::vector<double> w_pair(ni), w_stern(ni), w_fermi(ni), mask(ni);
   double fsum = 0;
   std::vector<double> fprime(ni);
   for (int it = 0; it < ni; ++it) {
     const KSetDev &K = h->ks[h->item_ks[it]];
+    const bool inM = h->item_band[it] < nsplit[h->item_ks[it]];
     const double ft = 0.5 * occ[it];
     fprime[it] = -2.0 * ft * (1.0 - ft) / kT;
-    w_pair[it] = 0.25 * K.wk / S.volume;                  // (|psi+xi|^2 - |psi-xi|^2)/4
-    w_stern[it] = 0.25 * 2.0 * occ[it] * K.wk / S.volume;  // 2 f Re psi* x
+    w_pair[it] = inM ? 0.25 * K.wk / S.volume : 0.0;                  // (|psi+xi|^2 - |psi-xi|^2)/4
+    w_stern[it] = inM ? 0.25 * 2.0 * occ[it] * K.wk / S.volume : 0.0;  // 2 f Re psi* x
     w_fermi[it] = fprime[it] * K.wk / S.volume;
-    mask[it] = occ[it] > 1e-12 ? 1.0 : 0.0;
-    shift[it] = -eig[it];
+    mask[it] = inM && occ[it] > 1e-12 ? 1.0 : 0.0;
     fsum += K.wk * fprime[it];
   }
   CKA(cudaMemcpyAsync(W.mask, mask.data(), ni * sizeof(double), cudaMemcpyHostToDevice, st));
-  CKA(cudaMemcpyAsync(W.shift, shift.data(), ni * sizeof(double), cudaMemcpyHostToDevice, st));
   std::vector<Axpby> vc(h->nks, Axpby{1.0, 0.0, 0.0, 0.0});
   CKA(cudaMemcpyAsync(W.vcoef, vc.data(), vc.size() * sizeof(Axpby), cudaMemcpyHostToDevice, st));
 
@@ -309,11 +358,11 @@ extern "C" int derek_gpu_grad_density_loss(derek_gpu_t *h, int s, const double *
   };
   // P_c y = y - Psi (Psi^H y)
   auto project = [&](double2 *y) {
-    launch_overlap<double>(t, 0, h->nks, h->max_nb, h->max_npw, h->tune.ksplit, psi, y, h->d_opart,
+    launch_overlap<double>(tM, 0, h->nks, h->max_nb, h->max_npw, h->tune.ksplit, psi, y, h->d_opart,
                            h->d_opart_off, h->d_S, h->d_mat_off, 0, st);
     const size_t sm = (size_t)h->max_nb * h->max_nb * sizeof(double2);
     cudaFuncSetAttribute(k_gemm_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    derek::note_launch(), k_gemm_sub<<<dim3((h->max_npw + 31) / 32, h->nks), 256, sm, st>>>(t, psi, h->d_S, h->d_mat_off, y);
+    derek::note_launch(), k_gemm_sub<<<dim3((h->max_npw + 31) / 32, h->nks), 256, sm, st>>>(tM, psi, h->d_S, h->d_mat_off, y);
   };
   // Fermi-level density n_F (fixed for the whole solve); rho_in and the item
   // weights are used as scratch and restored at the end
@@ -341,11 +390,11 @@ extern "C" int derek_gpu_grad_density_loss(derek_gpu_t *h, int s, const double *
       if (e2) return e2;
     }
     // V_mn and the pair orbitals xi = psi W
-    launch_overlap<double>(t, 0, h->nks, h->max_nb, h->max_npw, h->tune.ksplit, psi, W.phi, h->d_opart,
+    launch_overlap<double>(tM, 0, h->nks, h->max_nb, h->max_npw, h->tune.ksplit, psi, W.phi, h->d_opart,
                            h->d_opart_off, h->d_Hs, h->d_mat_off, 1, st);
-    derek::note_launch(), k_pair_weights<<<h->nks, 256, 0, st>>>(t, h->d_eig, h->d_occ, h->d_Hs, h->d_mat_off, h->d_C);
+    derek::note_launch(), k_pair_weights<<<h->nks, 256, 0, st>>>(tM, h->d_eig, h->d_occ, h->d_Hs, h->d_mat_off, h->d_C);
     CKA(cudaMemcpyAsync(W.xi, psi, np * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    launch_rotate<double>(t, 0, h->nks, h->max_nb, h->max_npw, W.xi, h->d_C, h->d_mat_off, st);
+    launch_rotate<double>(tM, 0, h->nks, h->max_nb, h->max_npw, W.xi, h->d_C, h->d_mat_off, st);
     e = cross_density(psi, W.xi, w_pair, W.dn_out);
     if (e) return e;
     // diagonal V_nn for the Fermi shift
@@ -355,7 +404,7 @@ extern "C" int derek_gpu_grad_density_loss(derek_gpu_t *h, int s, const double *
       CKA(cudaStreamSynchronize(st));
       for (int it = 0; it < ni; ++it) {
         const int ksi = h->item_ks[it], b = h->item_band[it];
-        vnn[it] = vm[h->mat_off[ksi] + (long long)b * h->ks[ksi].nb + b].x;
+        vnn[it] = b < nsplit[ksi] ? vm[h->mat_off[ksi] + (long long)b * nsplit[ksi] + b].x : 0.0;
       }
     }
     double dmu_num = 0;
