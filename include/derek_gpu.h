@@ -315,8 +315,10 @@ int derek_gpu_grad_wells(derek_gpu_t *h, int sys, double *grad);
 
 /* Gradient of the density-matching loss L = sum_r (n - n_target)^2 dV with
  * respect to the Gaussian-well parameters of sys, through the converged SCF:
- * one self-consistent linear-response (adjoint) solve with Sternheimer
- * equations for the bands of the filtered subspace.  No counterpart in the
+ * one self-consistent linear-response (adjoint) solve: a sum over pairs of
+ * the converged leading bands of each k-point (Ritz residual below 1e-7,
+ * every occupied band included) and Sternheimer equations on their
+ * complement, which takes the unconverged top bands.  No counterpart in the
  * reference.  Needs an FP64 handle over one system and a converged SCF;
  * n_target has nr values; writes L to *loss and nwells*5 derivatives
  * (cx, cy, cz, depth, width order) to grad.  max_iter <= 0 and tol <= 0
